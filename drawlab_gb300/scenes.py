@@ -1,0 +1,391 @@
+"""Procedural scenes (the workloads the path tracer is measured and checked on).
+
+No scene files ship with the reference, so every workload is generated here
+from a seed:
+
+* ``cornell()``        -- Cornell box: 5 quads + 2 rotated cuboids + ceiling
+                          light, 256x256 (34 triangles).
+* ``material_spheres()`` -- 64 level-4 icospheres (5120 triangles each) on a
+                          40x40 ground quad with seeded materials, 4 quad area
+                          lights and a point light, 1920x1080 (327,682 tris).
+* ``mis_plates()``     -- four GGX plates under four spherical lights of equal
+                          power, 1280x720 (Veach-style MIS stress scene).
+
+A scene is a :class:`SceneData` holding numpy arrays; ``descs()`` packs it into
+the ``dl_*_desc`` structs of include/drawlab.h for the GPU library, the oracle
+and the reference harness alike.
+
+Quads follow the reference's ``rectangle`` shape exactly
+(src/tracer/mesh/rectangle.cpp:11-40): vertices pos, pos+v0, pos+v1,
+pos+v0+v1, faces (0,1,2), (3,2,1), every vertex normal normalize(v0 x v1).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+
+@dataclass
+class Mesh:
+    positions: np.ndarray           # (V, 3) float32
+    indices: np.ndarray             # (F, 3) uint32
+    normals: np.ndarray | None = None
+    texcoords: np.ndarray | None = None
+    material: int = 0
+    light: int = -1
+
+
+@dataclass
+class Material:
+    type: int = abi.DL_MAT_DIFFUSE
+    albedo: tuple = (0.5, 0.5, 0.5)
+    specular: tuple = (0.5, 0.5, 0.5)
+    alpha: tuple = (0.1, 0.1)
+    int_ior: float = 1.5046
+    ext_ior: float = 1.000277
+
+
+@dataclass
+class Light:
+    type: int = abi.DL_LIGHT_AREA
+    mesh: int = -1
+    radiance: tuple = (1.0, 1.0, 1.0)
+    position: tuple = (0.0, 0.0, 0.0)
+    env_rgb: np.ndarray | None = None   # (H, W, 3) float32
+    env_scale: float = 1.0
+    env_visual: int = 1
+
+
+@dataclass
+class Camera:
+    width: int = 256
+    height: int = 256
+    eye: tuple = (0.0, 0.0, 1.0)
+    lookat: tuple = (0.0, 0.0, 0.0)
+    up: tuple = (0.0, 1.0, 0.0)
+    fov: float = 30.0
+
+
+@dataclass
+class SceneData:
+    name: str
+    meshes: list = field(default_factory=list)
+    materials: list = field(default_factory=list)
+    lights: list = field(default_factory=list)
+    camera: Camera = field(default_factory=Camera)
+    spp: int = 16
+    max_depth: int = 0
+    rr_depth: int = 3
+
+    @property
+    def num_triangles(self) -> int:
+        return int(sum(m.indices.shape[0] for m in self.meshes))
+
+    def add_material(self, mat: Material) -> int:
+        self.materials.append(mat)
+        return len(self.materials) - 1
+
+    def add_mesh(self, mesh: Mesh) -> int:
+        self.meshes.append(mesh)
+        return len(self.meshes) - 1
+
+    def add_area_light(self, mesh_index: int, radiance) -> int:
+        self.lights.append(Light(type=abi.DL_LIGHT_AREA, mesh=mesh_index,
+                                 radiance=tuple(float(x) for x in radiance)))
+        self.meshes[mesh_index].light = len(self.lights) - 1
+        return len(self.lights) - 1
+
+    def triangles(self) -> np.ndarray:
+        """All triangles as (F, 3, 3) float32, meshes concatenated in order."""
+        out = [m.positions[m.indices.astype(np.int64)] for m in self.meshes]
+        return np.concatenate(out, axis=0).astype(np.float32)
+
+    def descs(self):
+        """Pack into ctypes descriptors.  Returns (holder, meshes, nm, mats,
+        nmat, lights, nl, camera); keep ``holder`` alive while they are used."""
+        keep = []
+
+        def fptr(a):
+            if a is None:
+                return C.POINTER(C.c_float)()
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(C.c_float))
+
+        nm = len(self.meshes)
+        md = (abi.dl_mesh_desc * max(nm, 1))()
+        for i, m in enumerate(self.meshes):
+            idx = np.ascontiguousarray(m.indices, dtype=np.uint32)
+            keep.append(idx)
+            md[i].positions = fptr(m.positions)
+            md[i].normals = fptr(m.normals)
+            md[i].texcoords = fptr(m.texcoords)
+            md[i].indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+            md[i].num_vertices = m.positions.shape[0]
+            md[i].num_triangles = idx.shape[0]
+            md[i].material = m.material
+            md[i].light = m.light
+        nmat = len(self.materials)
+        mat = (abi.dl_material_desc * max(nmat, 1))()
+        for i, x in enumerate(self.materials):
+            mat[i].type = x.type
+            mat[i].albedo[:] = [float(v) for v in x.albedo]
+            mat[i].specular[:] = [float(v) for v in x.specular]
+            mat[i].alpha[:] = [float(v) for v in x.alpha]
+            mat[i].int_ior = x.int_ior
+            mat[i].ext_ior = x.ext_ior
+        nl = len(self.lights)
+        ld = (abi.dl_light_desc * max(nl, 1))()
+        for i, x in enumerate(self.lights):
+            ld[i].type = x.type
+            ld[i].mesh = x.mesh
+            ld[i].radiance[:] = [float(v) for v in x.radiance]
+            ld[i].position[:] = [float(v) for v in x.position]
+            if x.env_rgb is not None:
+                ld[i].env_rgb = fptr(x.env_rgb)
+                ld[i].env_height = x.env_rgb.shape[0]
+                ld[i].env_width = x.env_rgb.shape[1]
+            ld[i].env_scale = x.env_scale
+            ld[i].env_visual = x.env_visual
+        cam = abi.dl_camera_desc()
+        c = self.camera
+        cam.type = abi.DL_CAMERA_VIRTUAL
+        cam.width, cam.height = c.width, c.height
+        cam.eye[:] = [float(v) for v in c.eye]
+        cam.lookat[:] = [float(v) for v in c.lookat]
+        cam.up[:] = [float(v) for v in c.up]
+        cam.fov = c.fov
+        keep.extend([md, mat, ld, cam])
+        return keep, md, nm, mat, nmat, ld, nl, cam
+
+
+# ------------------------------------------------------------------ geometry
+
+def rectangle(pos, v0, v1) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """The reference's ``rectangle`` shape: (positions, indices, normals)."""
+    pos = np.asarray(pos, np.float32)
+    v0 = np.asarray(v0, np.float32)
+    v1 = np.asarray(v1, np.float32)
+    n = np.cross(v0, v1).astype(np.float32)
+    n = (n / np.float32(np.sqrt(np.float32(n @ n)))).astype(np.float32)
+    p = np.stack([pos, pos + v0, pos + v1, pos + v0 + v1]).astype(np.float32)
+    f = np.array([[0, 1, 2], [3, 2, 1]], np.uint32)
+    return p, f, np.tile(n, (4, 1)).astype(np.float32)
+
+
+def _rot_y(deg: float) -> np.ndarray:
+    a = math.radians(deg)
+    c, s = math.cos(a), math.sin(a)
+    return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]], np.float64)
+
+
+def cuboid(center, size, rot_y_deg: float):
+    """Axis-aligned box of `size` rotated about y, as 6 outward-facing quads
+    (rectangle layout each): 24 vertices, 12 triangles, flat normals."""
+    hx, hy, hz = (0.5 * s for s in size)
+    R = _rot_y(rot_y_deg)
+    c = np.asarray(center, np.float64)
+    # (corner, edge0, edge1) with edge0 x edge1 pointing outwards
+    faces = [
+        ((-hx, -hy, hz), (2 * hx, 0, 0), (0, 2 * hy, 0)),    # +z
+        ((hx, -hy, -hz), (-2 * hx, 0, 0), (0, 2 * hy, 0)),   # -z
+        ((hx, -hy, hz), (0, 0, -2 * hz), (0, 2 * hy, 0)),    # +x
+        ((-hx, -hy, -hz), (0, 0, 2 * hz), (0, 2 * hy, 0)),   # -x
+        ((-hx, hy, hz), (2 * hx, 0, 0), (0, 0, -2 * hz)),    # +y
+        ((-hx, -hy, -hz), (2 * hx, 0, 0), (0, 0, 2 * hz)),   # -y
+    ]
+    P, F, N = [], [], []
+    for k, (p0, e0, e1) in enumerate(faces):
+        p0 = R @ np.asarray(p0) + c
+        e0 = R @ np.asarray(e0)
+        e1 = R @ np.asarray(e1)
+        p, f, n = rectangle(p0, e0, e1)
+        P.append(p)
+        F.append(f + 4 * k)
+        N.append(n)
+    return np.concatenate(P), np.concatenate(F).astype(np.uint32), np.concatenate(N)
+
+
+def icosphere(level: int, center=(0, 0, 0), radius: float = 1.0):
+    """Subdivided icosahedron: 20*4^level triangles, smooth unit normals."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+             (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    V = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+         (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(level):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = V[a] + V[b]
+                V.append(m / np.linalg.norm(m))
+                cache[key] = len(V) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        F = nf
+    Vn = np.array(V, np.float64)
+    P = (Vn * radius + np.asarray(center, np.float64)).astype(np.float32)
+    return P, np.array(F, np.uint32), Vn.astype(np.float32)
+
+
+_ICO_CACHE: dict = {}
+
+
+def _unit_icosphere(level: int):
+    if level not in _ICO_CACHE:
+        _ICO_CACHE[level] = icosphere(level)
+    return _ICO_CACHE[level]
+
+
+def sphere_mesh(level: int, center, radius: float):
+    P, F, N = _unit_icosphere(level)
+    Pd = (P.astype(np.float64) * radius + np.asarray(center, np.float64)).astype(np.float32)
+    return Pd, F.copy(), N.copy()
+
+
+# -------------------------------------------------------------------- scenes
+
+def cornell(width: int = 256, height: int = 256, spp: int = 16, max_depth: int = 8) -> SceneData:
+    """Cornell box: 2x2x2 box of 5 quads, two cuboids rotated +-17 degrees,
+    0.5x0.4 ceiling area light of radiance (17, 12, 4)."""
+    s = SceneData("cornell", spp=spp, max_depth=max_depth, rr_depth=3)
+    grey = s.add_material(Material(albedo=(0.725, 0.725, 0.725)))
+    red = s.add_material(Material(albedo=(0.63, 0.065, 0.05)))
+    green = s.add_material(Material(albedo=(0.14, 0.45, 0.09)))
+    black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+    quads = [
+        ((-1, -1, -1), (0, 0, 2), (2, 0, 0), grey),    # floor, +y
+        ((-1, 1, -1), (2, 0, 0), (0, 0, 2), grey),     # ceiling, -y
+        ((-1, -1, -1), (2, 0, 0), (0, 2, 0), grey),    # back, +z
+        ((-1, -1, -1), (0, 2, 0), (0, 0, 2), red),     # left, +x
+        ((1, -1, -1), (0, 0, 2), (0, 2, 0), green),    # right, -x
+    ]
+    for pos, v0, v1, m in quads:
+        p, f, n = rectangle(pos, v0, v1)
+        s.add_mesh(Mesh(p, f, n, material=m))
+    # cuboids lifted 1e-3 off the floor so no face is coplanar with another
+    p, f, n = cuboid((-0.33, -1 + 0.6 + 1e-3, -0.28), (0.6, 1.2, 0.6), 17.0)
+    s.add_mesh(Mesh(p, f, n, material=grey))
+    p, f, n = cuboid((0.34, -1 + 0.3 + 1e-3, 0.32), (0.6, 0.6, 0.6), -17.0)
+    s.add_mesh(Mesh(p, f, n, material=grey))
+    p, f, n = rectangle((-0.25, 0.999, -0.2), (0.5, 0, 0), (0, 0, 0.4))
+    li = s.add_mesh(Mesh(p, f, n, material=black))
+    s.add_area_light(li, (17.0, 12.0, 4.0))
+    s.camera = Camera(width=width, height=height, eye=(0.0, 0.0, 3.9), lookat=(0.0, 0.0, 0.0),
+                      up=(0.0, 1.0, 0.0), fov=39.3)
+    return s
+
+
+def material_spheres(width: int = 1920, height: int = 1080, spp: int = 64, max_depth: int = 16,
+                     seed: int = 2, num_spheres: int = 64, level: int = 4) -> SceneData:
+    """64 icospheres on a 40x40 ground quad with seeded materials (diffuse,
+    mirror, dielectric, GGX, anisotropic GGX), 4 quad area lights of radiance
+    U[5,30] and one point light of intensity 200."""
+    rng = np.random.default_rng(seed)
+    s = SceneData("material_spheres", spp=spp, max_depth=max_depth, rr_depth=3)
+    ground = s.add_material(Material(albedo=(0.5, 0.5, 0.5)))
+    p, f, n = rectangle((-20, 0, -20), (0, 0, 40), (40, 0, 0))
+    s.add_mesh(Mesh(p, f, n, material=ground))
+    placed = []
+    tries = 0
+    while len(placed) < num_spheres:
+        tries += 1
+        if tries > 100000:
+            raise RuntimeError("sphere placement failed")
+        r = float(rng.uniform(0.3, 1.0))
+        x, z = (float(v) for v in rng.uniform(-18.0, 18.0, size=2))
+        if all((x - px) ** 2 + (z - pz) ** 2 > (r + pr + 0.05) ** 2 for px, pz, pr in placed):
+            placed.append((x, z, r))
+    for x, z, r in placed:
+        kind = int(rng.integers(0, 5))
+        if kind == 0:
+            m = Material(type=abi.DL_MAT_DIFFUSE, albedo=tuple(rng.uniform(0.1, 0.9, 3)))
+        elif kind == 1:
+            m = Material(type=abi.DL_MAT_MIRROR)
+        elif kind == 2:
+            m = Material(type=abi.DL_MAT_DIELECTRIC, int_ior=1.5, ext_ior=1.000277)
+        elif kind == 3:
+            a = float(rng.uniform(0.05, 0.5))
+            m = Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1), alpha=(a, a))
+        else:
+            ax, ay = (float(v) for v in rng.uniform(0.02, 0.4, 2))
+            m = Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1), alpha=(ax, ay))
+        mi = s.add_material(m)
+        p, f, n = sphere_mesh(level, (x, r + 1e-3, z), r)
+        s.add_mesh(Mesh(p, f, n, material=mi))
+    black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+    for k in range(4):
+        L = float(rng.uniform(5.0, 30.0))
+        cx, cz = (float(v) for v in rng.uniform(-12.0, 12.0, 2))
+        w, d = (float(v) for v in rng.uniform(2.0, 4.0, 2))
+        h = float(rng.uniform(8.0, 12.0))
+        p, f, n = rectangle((cx - w / 2, h, cz - d / 2), (w, 0, 0), (0, 0, d))   # faces -y
+        li = s.add_mesh(Mesh(p, f, n, material=black))
+        s.add_area_light(li, (L, L, L))
+    s.lights.append(Light(type=abi.DL_LIGHT_POINT, radiance=(200.0, 200.0, 200.0),
+                          position=(0.0, 6.0, 4.0)))
+    s.camera = Camera(width=width, height=height, eye=(0.0, 9.0, 26.0), lookat=(0.0, 0.0, 0.0),
+                      up=(0.0, 1.0, 0.0), fov=45.0)
+    return s
+
+
+def mis_plates(width: int = 1280, height: int = 720, spp: int = 256, max_depth: int = 8,
+               level: int = 3) -> SceneData:
+    """Four 4x0.6 GGX plates (alpha 0.005, 0.02, 0.05, 0.2; pd 0, ps 1) facing
+    the camera under four spherical lights of radius 0.03, 0.1, 0.3, 0.9 with
+    radiance scaled as 1/r^2, in front of a diffuse 0.4 backdrop."""
+    s = SceneData("mis_plates", spp=spp, max_depth=max_depth, rr_depth=3)
+    eye = np.array([0.0, 2.0, 15.0])
+    target = np.array([0.0, -2.0, 2.5])
+    back = s.add_material(Material(albedo=(0.4, 0.4, 0.4)))
+    p, f, n = rectangle((-20, -4.2, -6), (40, 0, 0), (0, 30, 0))      # back wall, +z
+    s.add_mesh(Mesh(p, f, n, material=back))
+    p, f, n = rectangle((-20, -4.2, -6), (0, 0, 30), (40, 0, 0))      # floor, +y
+    s.add_mesh(Mesh(p, f, n, material=back))
+    light_center = np.array([0.0, 2.5, 0.0])
+    for k, (alpha, zc) in enumerate(zip((0.005, 0.02, 0.05, 0.2), (4.0, 2.7, 1.4, 0.1))):
+        c = np.array([0.0, -2.8 + 0.25 * k, zc])
+        to_eye = eye - c
+        to_eye /= np.linalg.norm(to_eye)
+        to_l = light_center - c
+        to_l /= np.linalg.norm(to_l)
+        nrm = to_eye + to_l
+        nrm /= np.linalg.norm(nrm)
+        ex = np.array([4.0, 0.0, 0.0])
+        ey = np.cross(nrm, ex)
+        ey = 0.6 * ey / np.linalg.norm(ey)
+        pos = c - 0.5 * ex - 0.5 * ey
+        e0, e1 = (ex, ey) if np.dot(np.cross(ex, ey), nrm) > 0 else (ey, ex)
+        mi = s.add_material(Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1),
+                                     alpha=(alpha, alpha)))
+        p, f, n = rectangle(pos, e0, e1)
+        s.add_mesh(Mesh(p, f, n, material=mi))
+    black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+    for x, r in zip((-3.75, -1.25, 1.25, 3.75), (0.03, 0.1, 0.3, 0.9)):
+        L = 0.8 / (r * r) * 0.1
+        p, f, n = sphere_mesh(level, (x, light_center[1], light_center[2]), r)
+        li = s.add_mesh(Mesh(p, f, n, material=black))
+        s.add_area_light(li, (L, L, L))
+    s.camera = Camera(width=width, height=height, eye=tuple(eye), lookat=tuple(target),
+                      up=(0.0, 1.0, 0.0), fov=28.0)
+    return s
+
+
+SCENES = {
+    "cornell": cornell,
+    "material_spheres": material_spheres,
+    "mis_plates": mis_plates,
+}

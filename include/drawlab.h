@@ -1,0 +1,269 @@
+/*
+ * drawlab.h -- C ABI of the GB300 wavefront path tracer.
+ *
+ * Plain C types only (pointers, sizes, PODs): any FFI (ctypes, cgo, JNI,
+ * N-API) can bind it.  Every entry point returns an int status (DL_OK on
+ * success); dl_last_error() gives the message of the last failure on a
+ * context.  No C++ exception crosses this boundary.
+ *
+ * The reference (xuxmin/DrawLab) exposes the same path as C++ virtual
+ * interfaces.  Each entry point below names the reference interface it
+ * stands in for (paths are relative to the reference project root).
+ *
+ * Threading: calls on one dl_context are serialised by the caller.  Distinct
+ * contexts are independent.  One CUDA stream per context.
+ */
+#ifndef DRAWLAB_H
+#define DRAWLAB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DL_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+enum dl_status {
+    DL_OK = 0,
+    DL_ERR_INVALID_ARG = 1,
+    DL_ERR_OOM = 2,
+    DL_ERR_CUDA = 3,
+    DL_ERR_TIMEOUT = 4,
+    DL_ERR_QUEUE_OVERFLOW = 5,
+    DL_ERR_PARSE = 6,
+    DL_ERR_UNSUPPORTED = 7,
+    DL_ERR_IO = 8
+};
+
+typedef struct dl_context dl_context;
+typedef struct dl_scene dl_scene;
+
+/* ------------------------------------------------------- scene descriptors */
+
+/* Triangle mesh.  Stands in for drawlab::Mesh (include/tracer/mesh.h:20-252):
+ * positions m_V, normals m_N, texcoords m_UV, faces m_F.  normals/texcoords
+ * may be NULL.  A mesh carries one material and, optionally, one area light
+ * (Mesh::addChild, src/tracer/mesh/mesh.cpp:47-69). */
+typedef struct dl_mesh_desc {
+    const float* positions;   /* num_vertices x 3 */
+    const float* normals;     /* num_vertices x 3, or NULL */
+    const float* texcoords;   /* num_vertices x 2, or NULL */
+    const uint32_t* indices;  /* num_triangles x 3 */
+    int64_t num_vertices;
+    int64_t num_triangles;
+    int32_t material;         /* index into the material array */
+    int32_t light;            /* index of the area light bound to it, or -1 */
+} dl_mesh_desc;
+
+/* BSDF plugins (include/tracer/bsdf.h:46-110), XML type strings in brackets. */
+enum dl_material_type {
+    DL_MAT_DIFFUSE = 0,     /* "diffuse"    src/tracer/bsdf/diffuse.cpp */
+    DL_MAT_MIRROR = 1,      /* "mirror"     src/tracer/bsdf/mirror.cpp */
+    DL_MAT_DIELECTRIC = 2,  /* "dielectric" src/tracer/bsdf/dielectric.cpp */
+    DL_MAT_MICROFACET = 3,  /* "microfacet" src/tracer/bsdf/microfacet.cpp (Beckmann) */
+    DL_MAT_ANISO_GGX = 4    /* "aniso_ggx"  src/optix/cuda/material/aniso_ggx.cu */
+};
+
+typedef struct dl_material_desc {
+    int32_t type;         /* dl_material_type */
+    float albedo[3];      /* diffuse albedo | microfacet kd | aniso_ggx pd */
+    float specular[3];    /* aniso_ggx ps */
+    float alpha[2];       /* microfacet alpha in [0]; aniso_ggx (ax, ay) */
+    float int_ior;        /* dielectric / microfacet interior IOR */
+    float ext_ior;        /* dielectric / microfacet exterior IOR */
+} dl_material_desc;
+
+/* Emitter plugins (include/tracer/emitter.h:7-117). */
+enum dl_light_type {
+    DL_LIGHT_AREA = 0,    /* "area"   src/tracer/emitter/area.cpp */
+    DL_LIGHT_POINT = 1,   /* "point"  src/tracer/emitter/point.cpp */
+    DL_LIGHT_ENVMAP = 2   /* "envmap" src/tracer/emitter/envmap.cpp + include/optix/light/envmap.h */
+};
+
+/* The order of the light array is the emitter order of the scene: the
+ * uniform emitter pick of Scene::sampleEmitterDirection
+ * (src/tracer/scene/scene.cpp:148-163) indexes it. */
+typedef struct dl_light_desc {
+    int32_t type;          /* dl_light_type */
+    int32_t mesh;          /* area: index of the emitting mesh */
+    float radiance[3];     /* area radiance | point intensity */
+    float position[3];     /* point position */
+    const float* env_rgb;  /* envmap: env_height x env_width x 3 floats, lat-long */
+    int32_t env_width;
+    int32_t env_height;
+    float env_scale;       /* envmap "scale" (default 1) */
+    int32_t env_visual;    /* envmap "visual": seen by camera rays (default 1) */
+} dl_light_desc;
+
+enum dl_camera_type {
+    DL_CAMERA_VIRTUAL = 0  /* "virtual" src/tracer/camera/virtual.cpp:14-123 */
+};
+
+typedef struct dl_camera_desc {
+    int32_t type;          /* dl_camera_type */
+    int32_t width;
+    int32_t height;
+    float eye[3];
+    float lookat[3];
+    float up[3];
+    float fov;             /* vertical field of view, degrees */
+} dl_camera_desc;
+
+/* ------------------------------------------------------------------ context */
+
+/* Create a context on CUDA device `device` (one stream, device memory owned
+ * by the context).  No reference counterpart: the reference owns one OptiX
+ * DeviceContext per renderer (src/optix/host/device_context.cpp:55). */
+int dl_context_create(int device, dl_context** out);
+int dl_context_destroy(dl_context* ctx);
+/* Message of the last failed call on ctx ("" if none).  Valid until the next
+ * call on ctx.  ctx may be NULL for failures of dl_context_create. */
+const char* dl_last_error(const dl_context* ctx);
+/* ABI version compiled into the library (DL_ABI_VERSION). */
+int dl_abi_version(void);
+
+/* -------------------------------------------------------------------- scene */
+
+/* Build a scene from arrays: uploads geometry, builds the SAH BVH on the
+ * host and copies it to the device.  Replaces loadFromXML + Scene::addChild +
+ * Scene::activate + OCTree::build (src/core/parser/parser.cpp:19-387,
+ * src/tracer/scene/scene.cpp:19-106, src/tracer/accel/octree.cpp:135-151). */
+int dl_scene_create_from_arrays(dl_context* ctx,
+                                const dl_mesh_desc* meshes, int32_t num_meshes,
+                                const dl_material_desc* materials, int32_t num_materials,
+                                const dl_light_desc* lights, int32_t num_lights,
+                                const dl_camera_desc* camera,
+                                dl_scene** out);
+
+/* Load a scene in the reference's XML format (mitsuba-style tags: scene,
+ * mesh, bsdf, emitter, camera, integrator, sampler, rfilter; properties and
+ * transforms).  Replaces loadFromXML (src/core/parser/parser.cpp:19-387).
+ * The sampler's sampleCount and the rfilter become the scene's default
+ * render options (see dl_scene_default_opts). */
+int dl_scene_create_from_xml(dl_context* ctx, const char* path, dl_scene** out);
+int dl_scene_destroy(dl_scene* scene);
+
+typedef struct dl_scene_info {
+    int64_t num_triangles;
+    int64_t num_bvh_nodes;
+    int32_t num_meshes;
+    int32_t num_materials;
+    int32_t num_lights;
+    int32_t width;
+    int32_t height;
+    int32_t bvh_depth;
+    double bvh_build_seconds;
+    double bvh_sah_cost;
+    int64_t device_bytes;
+} dl_scene_info;
+int dl_scene_get_info(const dl_scene* scene, dl_scene_info* info);
+
+/* ---------------------------------------------------------------- tracing */
+
+/* Rays are packed 8 floats each: ox, oy, oz, tmin, dx, dy, dz, tmax.
+ * Reference: Ray3f (include/core/math/ray.h:22-81); M_EPSILON = 1e-4 is the
+ * reference's default tmin. */
+
+/* Closest hit.  Replaces Accel::rayIntersect(ray, its, false) / OCTree
+ * (include/tracer/accel.h:52, src/tracer/accel/octree.cpp:53-110,153-212)
+ * with the Moller-Trumbore test of Mesh::rayIntersect
+ * (src/tracer/mesh/mesh.cpp:180-220).  prim_id is the global triangle index
+ * (meshes concatenated in order), -1 on a miss; t, u, v as the reference
+ * computes them.  Host buffers. */
+int dl_trace_closest(dl_scene* scene, const float* rays, int64_t n,
+                     int32_t* prim_id, float* t, float* u, float* v);
+
+/* Any hit (shadow query).  Replaces Accel::rayIntersect(ray, its, true) /
+ * OCTree::recursiveAnyhit (src/tracer/accel/octree.cpp:112-133). */
+int dl_trace_any(dl_scene* scene, const float* rays, int64_t n, uint8_t* occluded);
+
+/* Device-pointer forms of the two calls above (inputs already resident in
+ * device memory; launched on the context stream, which the call leaves
+ * unsynchronised).  hits: n x {t, u, v, prim_id bits} float4. */
+int dl_trace_closest_device(dl_scene* scene, const float* d_rays, int64_t n, float* d_hits);
+int dl_trace_any_device(dl_scene* scene, const float* d_rays, int64_t n, uint8_t* d_occluded);
+
+/* -------------------------------------------------------------- rendering */
+
+enum dl_filter {
+    DL_FILTER_GAUSSIAN = 0,  /* src/tracer/rfilter/rfilter.cpp:13-35, radius 2, stddev 0.5 */
+    DL_FILTER_BOX = 1        /* src/tracer/rfilter/rfilter.cpp:83-96, radius 0.5 */
+};
+
+enum dl_render_flags {
+    /* Point light with the receiver cosine and MIS weight 1 (OptiX form,
+     * include/optix/light/point.h:15-42, src/optix/cuda/hitgroup_pgs.cu:99).
+     * Off: the reference CPU form (no cosine, power-heuristic weight,
+     * src/tracer/emitter/point.cpp:17-33, src/tracer/integrator/path.cpp:53). */
+    DL_RENDER_FIX_POINT_LIGHT = 1u << 0,
+    /* Pick emitters by power through an alias table instead of uniformly. */
+    DL_RENDER_POWER_LIGHT_PICK = 1u << 1
+};
+
+/* Render options.  Reference: PathIntegrator (src/tracer/integrator/path.cpp),
+ * Independent sampler (src/tracer/sampler/independent.cpp) and the
+ * CPURenderer sample loop (src/tracer/backend/cpu_renderer.cpp:22-55). */
+typedef struct dl_render_opts {
+    int32_t spp;             /* samples per pixel */
+    int32_t max_depth;       /* <= 0: unbounded, as the reference; else at most
+                                max_depth scattering events per path */
+    int32_t rr_depth;        /* Russian roulette when depth > rr_depth (reference: 3) */
+    int32_t filter;          /* dl_filter */
+    uint64_t seed;           /* pcg32 seed of every path stream */
+    uint32_t flags;          /* dl_render_flags */
+    int32_t spp_offset;      /* index of the first sample (disjoint ranges for replicas) */
+    int64_t max_paths_in_flight; /* wavefront pool size; 0 = automatic */
+} dl_render_opts;
+
+/* Default options for a scene (spp / filter from XML when loaded from XML;
+ * otherwise spp 1, unbounded depth, rr_depth 3, Gaussian filter, seed 0). */
+int dl_scene_default_opts(const dl_scene* scene, dl_render_opts* opts);
+
+/* Render the scene's camera view.  rgb_out: height x width x 3 floats
+ * (row 0 = top image row, as the reference's bitmap), each pixel the
+ * filter-weighted mean of its samples (ImageBlock::put / toBitmap,
+ * src/core/bitmap/block.cpp:58-113).  Host buffer. */
+int dl_render(dl_scene* scene, const dl_render_opts* opts, float* rgb_out);
+
+/* Same render, but returns the raw film: (height + 2b) x (width + 2b) x 4
+ * floats (weighted RGB sums and weight sum, b = filter border: 2 for the
+ * Gaussian, 0 for the box).  Films of disjoint sample ranges add up. */
+int dl_render_film(dl_scene* scene, const dl_render_opts* opts, float* film_out);
+
+/* Device form of dl_render_film: film written to a device buffer on the
+ * context stream; the call returns without synchronising. */
+int dl_render_film_device(dl_scene* scene, const dl_render_opts* opts, float* d_film);
+
+/* Radiance of individual camera paths, the reference's
+ * Integrator::Li(scene, sampler, ray) (include/tracer/integrator.h:38) for
+ * the paths (x, y, s) given as n triples: pixel x, pixel y, sample index s.
+ * Each path draws its pixel sample, aperture sample and all bounce samples
+ * from its own pcg32 stream, exactly as dl_render does for that (x, y, s).
+ * L_out: n x 3 radiance; pos_out: n x 2 film position of the sample (may be
+ * NULL).  Host buffers. */
+int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
+          const int32_t* xys, float* L_out, float* pos_out);
+
+/* --------------------------------------------------------------- statistics */
+
+typedef struct dl_stats {
+    int64_t camera_rays;       /* paths started */
+    int64_t extension_rays;    /* closest-hit rays traced (camera rays included) */
+    int64_t shadow_rays;       /* any-hit rays traced */
+    int64_t invalid_samples;   /* samples dropped by the film (NaN/Inf/negative) */
+    int64_t iterations;        /* wavefront iterations of the last render */
+    double render_ms;          /* device time of the last render */
+    double trace_ms;           /* device time of the last dl_trace_* call */
+} dl_stats;
+
+/* Counters of the last dl_render* / dl_li / dl_trace_* call on ctx. */
+int dl_stats_get(const dl_context* ctx, dl_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DRAWLAB_H */

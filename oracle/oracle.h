@@ -1,0 +1,68 @@
+/*
+ * oracle.h -- CPU restatement of the xuxmin/DrawLab path-tracer hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Tests, __graft_entry__.smoke() and bench.py's
+ * CPU baseline call it as the checker; the product never links it.
+ *
+ * Scene input is the dl_*_desc arrays of include/drawlab.h.  Every entry
+ * point restates the reference function named beside it (paths relative to
+ * the reference project root).
+ */
+#ifndef DRAWLAB_ORACLE_H
+#define DRAWLAB_ORACLE_H
+
+#include <stdint.h>
+
+#include "drawlab.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Build the scene and its octree (Scene::addChild/activate, OCTree::build). */
+void* orc_scene_create(const dl_mesh_desc* meshes, int32_t num_meshes,
+                       const dl_material_desc* materials, int32_t num_materials,
+                       const dl_light_desc* lights, int32_t num_lights,
+                       const dl_camera_desc* camera, int32_t filter);
+void orc_scene_destroy(void* scene);
+const char* orc_last_error(void);
+
+/* OCTree closest hit / any hit (src/tracer/accel/octree.cpp:53-133). */
+int orc_trace_closest(void* scene, const float* rays, int64_t n, int32_t* prim, float* t,
+                      float* u, float* v, int32_t threads);
+int orc_trace_any(void* scene, const float* rays, int64_t n, uint8_t* occluded,
+                  int32_t threads);
+
+/* The reference CPU render: spiral 32x32 blocks, one pcg32 stream per block
+ * seeded with the block offset (src/tracer/backend/cpu_renderer.cpp:22-135).
+ * max_blocks > 0 renders only the first max_blocks blocks of the spiral. */
+int orc_render_blocks(void* scene, const dl_render_opts* opts, int32_t threads,
+                      int32_t max_blocks, float* rgb_out, float* film_out, double* seconds);
+
+/* Per-path streams (the GPU renderer's sampling): every (x, y, s) path seeds
+ * its own pcg32.  Film and rgb as dl_render_film / dl_render. */
+int orc_render_paths(void* scene, const dl_render_opts* opts, int32_t threads,
+                     float* rgb_out, float* film_out, double* seconds);
+
+/* Li of explicit (x, y, s) paths (as dl_li). */
+int orc_li(void* scene, const dl_render_opts* opts, int64_t n, const int32_t* xys,
+           float* L_out, float* pos_out, int32_t threads);
+
+/* BSDF::eval / pdf / sample on given local directions (see ref_bsdf_query). */
+int orc_bsdf_query(const dl_material_desc* m, int64_t n, const float* wi, const float* wo,
+                   const float* smp, float* eval, float* pdf, float* s_wo, float* s_w,
+                   float* s_eta, int32_t* s_measure);
+
+/* Frame(n) (include/core/math/frame.h:104-123). */
+int orc_frame(int64_t n, const float* nrm, float* t, float* b);
+
+/* Scene::sampleEmitterDirection at given points (see ref_emitter_sample). */
+int orc_emitter_sample(void* scene, const dl_render_opts* opts, int64_t n, const float* pts,
+                       const float* nrm, const float* smp, float* d, float* dist, float* pdf,
+                       float* spec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

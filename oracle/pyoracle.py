@@ -1,0 +1,245 @@
+"""ctypes wrappers of the oracle (``liboracle.so``, the CPU restatement) and
+of the reference harness (``libdlref.so``, the reference's own CPU code).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+if str(REPO) not in sys.path:
+    sys.path.insert(0, str(REPO))
+
+from drawlab_gb300 import abi  # noqa: E402
+
+_fp = C.POINTER(C.c_float)
+
+
+def _f(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _load(path: Path) -> C.CDLL:
+    return C.CDLL(str(path))
+
+
+_oracle_lib = None
+_ref_lib = None
+
+
+def oracle_lib() -> C.CDLL:
+    global _oracle_lib
+    if _oracle_lib is None:
+        sys.path.insert(0, str(HERE))
+        import build as _b  # oracle/build.py
+        path = _b.build_oracle()
+        lib = _load(path)
+        lib.orc_scene_create.restype = C.c_void_p
+        lib.orc_last_error.restype = C.c_char_p
+        _oracle_lib = lib
+    return _oracle_lib
+
+
+def ref_available() -> bool:
+    sys.path.insert(0, str(HERE))
+    import build as _b
+    return _b.reference_root() is not None or (HERE / "_ref" / "libdlref.so").exists()
+
+
+def ref_lib() -> C.CDLL | None:
+    global _ref_lib
+    if _ref_lib is None:
+        sys.path.insert(0, str(HERE))
+        import build as _b
+        path = _b.build_ref()
+        if path is None:
+            p = HERE / "_ref" / "libdlref.so"
+            if not p.exists():
+                return None
+            path = p
+        lib = _load(path)
+        lib.ref_scene_create.restype = C.c_void_p
+        lib.ref_last_error.restype = C.c_char_p
+        _ref_lib = lib
+    return _ref_lib
+
+
+def _threads(t):
+    return int(t if t else (os.cpu_count() or 1))
+
+
+class OracleScene:
+    """The CPU restatement bound to one scene."""
+
+    def __init__(self, scene, filter: int = abi.DL_FILTER_GAUSSIAN):
+        self.lib = oracle_lib()
+        self.scene = scene
+        keep, md, nm, mat, nmat, ld, nl, cam = scene.descs()
+        self._keep = keep
+        h = self.lib.orc_scene_create(md, nm, mat, nmat, ld, nl, C.byref(cam), filter)
+        if not h:
+            raise RuntimeError("oracle scene: %s" % self.lib.orc_last_error().decode())
+        self.h = C.c_void_p(h)
+        self.width, self.height = scene.camera.width, scene.camera.height
+        self.border = 2 if filter == abi.DL_FILTER_GAUSSIAN else 0
+
+    def __del__(self):
+        try:
+            self.lib.orc_scene_destroy(self.h)
+        except Exception:
+            pass
+
+    def trace_closest(self, rays: np.ndarray, threads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        self.lib.orc_trace_closest(self.h, _f(rays), C.c_int64(n), _f(prim), _f(t), _f(u), _f(v),
+                                   _threads(threads))
+        return prim, t, u, v
+
+    def trace_any(self, rays: np.ndarray, threads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        self.lib.orc_trace_any(self.h, _f(rays), C.c_int64(n), _f(occ), _threads(threads))
+        return occ
+
+    def render_blocks(self, opts, threads=None, max_blocks=0, film=False):
+        rgb = np.zeros((self.height, self.width, 3), np.float32)
+        fb = np.zeros((self.height + 2 * self.border, self.width + 2 * self.border, 4), np.float32)
+        sec = C.c_double()
+        self.lib.orc_render_blocks(self.h, C.byref(opts), _threads(threads), max_blocks, _f(rgb),
+                                   _f(fb), C.byref(sec))
+        return (rgb, fb, sec.value) if film else (rgb, sec.value)
+
+    def render_paths(self, opts, threads=None, film=False):
+        rgb = np.zeros((self.height, self.width, 3), np.float32)
+        fb = np.zeros((self.height + 2 * self.border, self.width + 2 * self.border, 4), np.float32)
+        sec = C.c_double()
+        self.lib.orc_render_paths(self.h, C.byref(opts), _threads(threads), _f(rgb), _f(fb),
+                                  C.byref(sec))
+        return (rgb, fb, sec.value) if film else (rgb, sec.value)
+
+    def li(self, opts, xys: np.ndarray, threads=None):
+        xys = np.ascontiguousarray(xys, np.int32)
+        n = xys.shape[0]
+        L = np.empty((n, 3), np.float32)
+        pos = np.empty((n, 2), np.float32)
+        self.lib.orc_li(self.h, C.byref(opts), C.c_int64(n), _f(xys), _f(L), _f(pos),
+                        _threads(threads))
+        return L, pos
+
+    def emitter_sample(self, opts, pts, nrm, smp):
+        n = pts.shape[0]
+        pts, nrm, smp = (np.ascontiguousarray(a, np.float32) for a in (pts, nrm, smp))
+        d = np.empty((n, 3), np.float32)
+        dist = np.empty(n, np.float32)
+        pdf = np.empty(n, np.float32)
+        spec = np.empty((n, 3), np.float32)
+        self.lib.orc_emitter_sample(self.h, C.byref(opts), C.c_int64(n), _f(pts), _f(nrm),
+                                    _f(smp), _f(d), _f(dist), _f(pdf), _f(spec))
+        return d, dist, pdf, spec
+
+
+class RefScene:
+    """The reference's own CPU code bound to one scene (x86 container only)."""
+
+    def __init__(self, scene, filter: int = abi.DL_FILTER_GAUSSIAN, spp: int = 1):
+        self.lib = ref_lib()
+        if self.lib is None:
+            raise RuntimeError("reference harness unavailable")
+        self.scene = scene
+        keep, md, nm, mat, nmat, ld, nl, cam = scene.descs()
+        self._keep = keep
+        h = self.lib.ref_scene_create(md, nm, mat, nmat, ld, nl, C.byref(cam), filter, spp)
+        if not h:
+            raise RuntimeError("reference scene: %s" % self.lib.ref_last_error().decode())
+        self.h = C.c_void_p(h)
+        self.width, self.height = scene.camera.width, scene.camera.height
+        self.border = 2 if filter == abi.DL_FILTER_GAUSSIAN else 0
+
+    def trace_closest(self, rays, threads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        self.lib.ref_trace_closest(self.h, _f(rays), C.c_int64(n), _f(prim), _f(t), _f(u), _f(v),
+                                   _threads(threads))
+        return prim, t, u, v
+
+    def trace_any(self, rays, threads=None):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        self.lib.ref_trace_any(self.h, _f(rays), C.c_int64(n), _f(occ), _threads(threads))
+        return occ
+
+    def render_blocks(self, threads=None, max_blocks=0, film=False):
+        rgb = np.zeros((self.height, self.width, 3), np.float32)
+        fb = np.zeros((self.height + 2 * self.border, self.width + 2 * self.border, 4), np.float32)
+        sec = C.c_double()
+        self.lib.ref_render_blocks(self.h, _threads(threads), max_blocks, _f(rgb), _f(fb),
+                                   C.byref(sec))
+        return (rgb, fb, sec.value) if film else (rgb, sec.value)
+
+    def li(self, seed: int, xys, threads=None):
+        xys = np.ascontiguousarray(xys, np.int32)
+        n = xys.shape[0]
+        L = np.empty((n, 3), np.float32)
+        pos = np.empty((n, 2), np.float32)
+        self.lib.ref_li(self.h, C.c_uint64(seed), C.c_int64(n), _f(xys), _f(L), _f(pos),
+                        _threads(threads))
+        return L, pos
+
+    def emitter_sample(self, pts, nrm, smp):
+        n = pts.shape[0]
+        pts, nrm, smp = (np.ascontiguousarray(a, np.float32) for a in (pts, nrm, smp))
+        d = np.empty((n, 3), np.float32)
+        dist = np.empty(n, np.float32)
+        pdf = np.empty(n, np.float32)
+        spec = np.empty((n, 3), np.float32)
+        self.lib.ref_emitter_sample(self.h, C.c_int64(n), _f(pts), _f(nrm), _f(smp), _f(d),
+                                    _f(dist), _f(pdf), _f(spec))
+        return d, dist, pdf, spec
+
+
+def bsdf_query(lib_kind: str, mat, wi, wo, smp):
+    """BSDF eval/pdf/sample through the oracle ("oracle") or the reference ("ref")."""
+    wi, wo, smp = (np.ascontiguousarray(a, np.float32) for a in (wi, wo, smp))
+    n = wi.shape[0]
+    out = dict(eval=np.empty((n, 3), np.float32), pdf=np.empty(n, np.float32),
+               wo=np.empty((n, 3), np.float32), weight=np.empty((n, 3), np.float32),
+               eta=np.empty(n, np.float32), measure=np.empty(n, np.int32))
+    md = abi.dl_material_desc()
+    md.type = mat.type
+    md.albedo[:] = [float(v) for v in mat.albedo]
+    md.specular[:] = [float(v) for v in mat.specular]
+    md.alpha[:] = [float(v) for v in mat.alpha]
+    md.int_ior = mat.int_ior
+    md.ext_ior = mat.ext_ior
+    lib = oracle_lib() if lib_kind == "oracle" else ref_lib()
+    fn = lib.orc_bsdf_query if lib_kind == "oracle" else lib.ref_bsdf_query
+    fn(C.byref(md), C.c_int64(n), _f(wi), _f(wo), _f(smp), _f(out["eval"]), _f(out["pdf"]),
+       _f(out["wo"]), _f(out["weight"]), _f(out["eta"]), _f(out["measure"]))
+    return out
+
+
+def frame(lib_kind: str, nrm):
+    nrm = np.ascontiguousarray(nrm, np.float32)
+    n = nrm.shape[0]
+    t = np.empty((n, 3), np.float32)
+    b = np.empty((n, 3), np.float32)
+    if lib_kind == "oracle":
+        oracle_lib().orc_frame(C.c_int64(n), _f(nrm), _f(t), _f(b))
+    else:
+        ref_lib().ref_frame(C.c_int64(n), _f(nrm), _f(t), _f(b))
+    return t, b
