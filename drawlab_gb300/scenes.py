@@ -384,8 +384,47 @@ def mis_plates(width: int = 1280, height: int = 720, spp: int = 256, max_depth: 
     return s
 
 
+def reference_spheres(width: int = 96, height: int = 64, spp: int = 4, max_depth: int = 0,
+                      seed: int = 5) -> SceneData:
+    """Small scene using only what the reference CPU backend implements:
+    six level-2 icospheres (diffuse, mirror, dielectric, Beckmann microfacet)
+    on a ground quad, two quad area lights and a point light."""
+    rng = np.random.default_rng(seed)
+    s = SceneData("reference_spheres", spp=spp, max_depth=max_depth, rr_depth=3)
+    ground = s.add_material(Material(albedo=(0.6, 0.6, 0.6)))
+    p, f, n = rectangle((-6, 0, -6), (0, 0, 12), (12, 0, 0))
+    s.add_mesh(Mesh(p, f, n, material=ground))
+    kinds = [
+        Material(type=abi.DL_MAT_DIFFUSE, albedo=(0.8, 0.3, 0.2)),
+        Material(type=abi.DL_MAT_MIRROR),
+        Material(type=abi.DL_MAT_DIELECTRIC, int_ior=1.5, ext_ior=1.000277),
+        Material(type=abi.DL_MAT_MICROFACET, albedo=(0.2, 0.2, 0.4), alpha=(0.28, 0.28), int_ior=1.7),
+        Material(type=abi.DL_MAT_MICROFACET, albedo=(0.5, 0.4, 0.1), alpha=(0.08, 0.08)),
+        Material(type=abi.DL_MAT_DIFFUSE, albedo=(0.2, 0.7, 0.3)),
+    ]
+    for k, m in enumerate(kinds):
+        mi = s.add_material(m)
+        x = -3.75 + 1.5 * k
+        z = float(rng.uniform(-1.0, 1.0))
+        r = float(rng.uniform(0.45, 0.7))
+        p, f, n = sphere_mesh(2, (x, r + 1e-3, z), r)
+        s.add_mesh(Mesh(p, f, n, material=mi))
+    black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+    p, f, n = rectangle((-3.0, 5.0, -1.0), (2.0, 0, 0), (0, 0, 1.5))
+    li = s.add_mesh(Mesh(p, f, n, material=black))
+    s.add_area_light(li, (12.0, 10.0, 8.0))
+    p, f, n = rectangle((1.0, 4.0, -2.5), (0, 0, 1.0), (1.5, 0, 0))
+    li = s.add_mesh(Mesh(p, f, n, material=black))
+    s.add_area_light(li, (5.0, 8.0, 12.0))
+    s.lights.append(Light(type=abi.DL_LIGHT_POINT, radiance=(30.0, 30.0, 40.0), position=(2.0, 4.0, 2.0)))
+    s.camera = Camera(width=width, height=height, eye=(0.0, 3.0, 9.0), lookat=(0.0, 0.5, 0.0),
+                      up=(0.0, 1.0, 0.0), fov=40.0)
+    return s
+
+
 SCENES = {
     "cornell": cornell,
     "material_spheres": material_spheres,
     "mis_plates": mis_plates,
+    "reference_spheres": reference_spheres,
 }

@@ -139,16 +139,12 @@ void* ref_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
             m->addChild(make_bsdf(mats[meshes[i].material]));
             built[i] = m;
         }
-        std::vector<bool> added(nm, false);
-        auto add_mesh = [&](int i) {
-            if (added[i]) return;
-            built[i]->activate();
-            rs->scene->addChild(built[i]);
-            added[i] = true;
-        };
-        // Scene children are added so that the emitter order equals the order
-        // of the light array (Scene::addChild appends mesh emitters when the
-        // mesh is added, src/tracer/scene/scene.cpp:36-81).
+        // Meshes are added in array order (that is the octree's triangle
+        // order), each with its area emitter; point lights follow.  The
+        // scene's emitter order (Scene::addChild, src/tracer/scene/scene.cpp:
+        // 36-81) must then equal the light-array order, else the scene is
+        // rejected: area lights in mesh order first, point lights last.
+        std::vector<int> order;
         for (int l = 0; l < nl; l++) {
             const dl_light_desc& L = lights[l];
             if (L.type == DL_LIGHT_AREA) {
@@ -158,19 +154,28 @@ void* ref_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
                 e->activate();
                 if (L.mesh < 0 || L.mesh >= nm) throw Exception("bad light mesh");
                 built[L.mesh]->addChild(e);
-                add_mesh(L.mesh);
-            } else if (L.type == DL_LIGHT_POINT) {
-                PropertyList pl;
-                pl.setColor("intensity", c3(L.radiance));
-                pl.setPoint("position", Point3f(L.position[0], L.position[1], L.position[2]));
-                Object* e = ObjectFactory::createInstance("point", pl);
-                e->activate();
-                rs->scene->addChild(e);
-            } else {
+            } else if (L.type != DL_LIGHT_POINT) {
                 throw Exception("light type not available in the reference CPU backend");
             }
         }
-        for (int i = 0; i < nm; i++) add_mesh(i);
+        for (int i = 0; i < nm; i++) {
+            built[i]->activate();
+            rs->scene->addChild(built[i]);
+            if (meshes[i].light >= 0) order.push_back(meshes[i].light);
+        }
+        for (int l = 0; l < nl; l++) {
+            const dl_light_desc& L = lights[l];
+            if (L.type != DL_LIGHT_POINT) continue;
+            PropertyList pl;
+            pl.setColor("intensity", c3(L.radiance));
+            pl.setPoint("position", Point3f(L.position[0], L.position[1], L.position[2]));
+            Object* e = ObjectFactory::createInstance("point", pl);
+            e->activate();
+            rs->scene->addChild(e);
+            order.push_back(l);
+        }
+        for (int l = 0; l < (int)order.size(); l++)
+            if (order[l] != l) throw Exception("light order not representable by the reference");
 
         PropertyList cp;
         cp.setInteger("width", cam->width);
