@@ -1,0 +1,311 @@
+"""Benchmark: the procedural material scene (327,682 triangles, 1920x1080,
+64 spp, max depth 16) rendered by the GB300 wavefront path tracer.
+
+One step = one full frame: 1920*1080*64 = 132.7M camera paths.  The scene
+(geometry, BVH, materials, lights) is resident on the device before timing.
+
+  value      samples/s of the whole job (device time from CUDA events on the
+             library's stream, summed over the K timed steps; L2 flushed
+             between steps)
+  e2e        the same metric through dl_render with a host output buffer
+             (film resolve + device-to-host copy of the image inside the call)
+  roofline   closest-hit traversal kernel: algorithmic bytes (node and
+             triangle fetches counted by a counting replay of the same frame,
+             plus ray in / hit out) / its summed launch time, against the
+             measured HBM copy bandwidth
+  cpu_baseline  the CPU restatement of the reference renderer (spiral 32x32
+             blocks, per-block pcg32) on a bounded set of blocks of the same
+             frame, all host cores
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU (torchrun, one rank per GPU): replicas render disjoint sample ranges
+(weak scaling), no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOAD = dict(workload="material_spheres", width=1920, height=1080, spp=64, max_depth=16,
+                triangles=327682, spheres=64, sphere_level=4, area_lights=4, point_lights=1)
+METRIC = "samples/s (material-sphere scene 1920x1080, 64 spp, depth 16)"
+
+# algorithmic bytes per closest-hit ray: node = 64 B (both child boxes + refs),
+# triangle = 48 B (3 x float4), ray in 32 B, hit out 16 B
+NODE_BYTES, TRI_BYTES, RAY_IN, HIT_OUT = 64, 48, 32, 16
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+            os.unlink(self.path)
+        except Exception:
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except Exception:
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(n)
+        if sm:
+            out["sm_mhz"] = statistics.median(sm)
+            out["sm_max_mhz"] = max(mx)
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(sm)
+        return out
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(scene_data, seconds_target=15.0, max_blocks=None):
+    """Oracle block renderer (reference semantics) on the first blocks of the
+    spiral: samples/s with every host core."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle as po
+    from drawlab_gb300 import abi
+
+    orc = po.OracleScene(scene_data)
+    cores = os.cpu_count() or 1
+    opts = abi.make_opts(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"])
+    # calibrate on a few blocks, then size the sample to ~seconds_target
+    blocks = max(cores, 4)
+    _, sec = orc.render_blocks(opts, threads=cores, max_blocks=blocks)
+    if max_blocks is None:
+        per_block = sec / blocks * cores
+        max_blocks = int(max(cores, min(400, seconds_target * cores / max(per_block, 1e-6))))
+    _, sec = orc.render_blocks(opts, threads=cores, max_blocks=max_blocks)
+    samples = max_blocks * 32 * 32 * WORKLOAD["spp"]
+    return {"value": samples / sec, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": "%d of the 2040 32x32 blocks (spiral order from the image centre), 64 spp, "
+                      "depth 16, %.1f s" % (max_blocks, sec)}, orc
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from drawlab_gb300 import scenes
+    sc = scenes.material_spheres()
+    base, orc = cpu_baseline(sc, seconds_target=6.0)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from drawlab_gb300 import abi
+    cores = os.cpu_count() or 1
+    opts = abi.make_opts(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"])
+    blocks = max(cores, 16)
+    for _ in range(args.warmup):
+        orc.render_blocks(opts, threads=cores, max_blocks=blocks)
+    tot_s = 0.0
+    for _ in range(args.steps):
+        _, s = orc.render_blocks(opts, threads=cores, max_blocks=blocks)
+        tot_s += s
+    samples = blocks * 32 * 32 * WORKLOAD["spp"] * args.steps
+    value = samples / tot_s
+    line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seed 2)",
+            "impl": "reference",
+            "config": dict(WORKLOAD, step="%d blocks of 32x32 pixels at 64 spp" % blocks),
+            "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
+                             "sample": "%d blocks per step (spiral order), 64 spp, depth 16; the reference "
+                                       "sources do not travel to this host, so the CPU restatement "
+                                       "(bit-exact with the reference elsewhere) runs" % blocks},
+            "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spp", type=int, default=WORKLOAD["spp"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = dist_env()
+    import torch
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    import __graft_entry__ as ge
+    ge.build()
+    from drawlab_gb300 import abi, api, scenes
+
+    sc = scenes.material_spheres()
+    ctx = api.Context(local)
+    gs = api.Scene.from_data(ctx, sc)
+    info = gs.info()
+    W, H, spp = sc.camera.width, sc.camera.height, args.spp
+    opts = abi.make_opts(spp=spp, max_depth=WORKLOAD["max_depth"], seed=0, spp_offset=rank * spp)
+    b = 2
+    film = torch.empty(((H + 2 * b) * (W + 2 * b) * 4,), dtype=torch.float32, device="cuda")
+    flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    def step():
+        ctx.check(ctx.lib.dl_render_film_device(gs.h, abi.C.byref(opts), abi.C.c_void_p(film.data_ptr())))
+
+    ctx.set_kernel_timing(False)
+    for _ in range(args.warmup):
+        step()
+    ctx.set_kernel_timing(True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms, ext_ms, sh_ms, shade_ms, ret_ms = 0.0, 0.0, 0.0, 0.0, 0.0
+    ext_rays = sh_rays = cam_rays = launches = 0
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            step()
+            st = ctx.stats()
+            dev_ms += st.render_ms
+            ext_ms += st.extend_ms
+            sh_ms += st.shadow_ms
+            shade_ms += st.shade_ms
+            ret_ms += st.retire_ms
+            ext_rays += st.extension_rays
+            sh_rays += st.shadow_rays
+            cam_rays += st.camera_rays
+            launches += st.kernel_launches
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ck = clocks.summary()
+    ctx.set_kernel_timing(False)
+    t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev_ms_max = float(t.item())
+    samples = W * H * spp * args.steps * ws
+    value = samples / (dev_ms_max / 1000.0)
+    mrays = (ext_rays + sh_rays) * ws / (dev_ms_max / 1000.0) / 1e6
+
+    # e2e: public C-ABI render into a host buffer
+    rgb = np.empty((H, W, 3), np.float32)
+    gs.render(opts)
+    e2e_s = 0.0
+    for _ in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        gs.render(opts)
+        e2e_s += time.perf_counter() - t1
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_value = W * H * spp * e2e_steps / e2e_s
+
+    # roofline of the closest-hit kernel
+    counts = gs.traversal_counts(opts)
+    hbm, peak_kind = peaks()
+    ext_tot = counts.extension_rays
+    n_node = counts.node_visits / max(1, counts.extension_rays + counts.shadow_rays)
+    n_tri = counts.triangle_tests / max(1, counts.extension_rays + counts.shadow_rays)
+    bytes_per_ray = n_node * NODE_BYTES + n_tri * TRI_BYTES + RAY_IN + HIT_OUT
+    achieved = ext_rays * bytes_per_ray / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else 0.0
+
+    if rank == 0:
+        base = None
+        if not args.no_cpu_baseline:
+            base, _ = cpu_baseline(sc)
+        line = {
+            "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural scene, seed 2; no scene files ship with the reference)",
+            "config": dict(WORKLOAD, spp=spp, l2_flush="256 MB buffer written between timed steps",
+                           paths_in_flight=min(1 << 22, W * H * spp), parallelism="replicas" if ws > 1 else "single"),
+            "mrays_per_s": mrays,
+            "rays": {"camera": cam_rays, "extension": ext_rays, "shadow": sh_rays},
+            "wall_s": wall,
+            "kernel_ms": {"extend": ext_ms, "shadow": sh_ms, "shade": shade_ms, "retire": ret_ms,
+                          "total_device": dev_ms},
+            "gpu_launches": launches,
+            "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 3 * 4,
+                    "call": "dl_render (render options by value; image returned to host memory)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "k_extend (closest-hit traversal)",
+                         "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": n_node,
+                         "tri_tests_per_ray": n_tri},
+            "clocks": ck,
+            "scene": {"triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
+                      "bvh_depth": info.bvh_depth, "bvh_build_s": info.bvh_build_seconds,
+                      "sah_cost": info.bvh_sah_cost},
+            "cpu_baseline": base,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -136,6 +136,20 @@ class dl_stats(C.Structure):
         ("iterations", C.c_int64),
         ("render_ms", C.c_double),
         ("trace_ms", C.c_double),
+        ("extend_ms", C.c_double),
+        ("shadow_ms", C.c_double),
+        ("shade_ms", C.c_double),
+        ("retire_ms", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+
+class dl_traversal_counts(C.Structure):
+    _fields_ = [
+        ("extension_rays", C.c_int64),
+        ("shadow_rays", C.c_int64),
+        ("node_visits", C.c_int64),
+        ("triangle_tests", C.c_int64),
     ]
 
 

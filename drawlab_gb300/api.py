@@ -1,0 +1,195 @@
+"""Python binding of the C ABI (include/drawlab.h) over ctypes.
+
+The library is the in-tree ``drawlab_gb300/_build/libdlgpu.so`` built by
+``drawlab_gb300.build``; there is no other code path: if the library is
+missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .scenes import SceneData
+
+_LIB_PATH = Path(__file__).resolve().parent / "_build" / "libdlgpu.so"
+_lib = None
+
+# every entry point of include/drawlab.h: name -> (restype, argtypes)
+_vp = C.c_void_p
+_i64 = C.c_int64
+_i32 = C.c_int32
+SIGNATURES = {
+    "dl_abi_version": (C.c_int, []),
+    "dl_last_error": (C.c_char_p, [_vp]),
+    "dl_context_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "dl_context_destroy": (C.c_int, [_vp]),
+    "dl_scene_create_from_arrays": (C.c_int, [_vp, _vp, _i32, _vp, _i32, _vp, _i32, _vp, C.POINTER(_vp)]),
+    "dl_scene_create_from_xml": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp)]),
+    "dl_scene_destroy": (C.c_int, [_vp]),
+    "dl_scene_get_info": (C.c_int, [_vp, _vp]),
+    "dl_scene_default_opts": (C.c_int, [_vp, _vp]),
+    "dl_trace_closest": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "dl_trace_any": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "dl_trace_closest_device": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "dl_trace_any_device": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "dl_render": (C.c_int, [_vp, _vp, _vp]),
+    "dl_render_film": (C.c_int, [_vp, _vp, _vp]),
+    "dl_render_film_device": (C.c_int, [_vp, _vp, _vp]),
+    "dl_li": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "dl_stats_get": (C.c_int, [_vp, _vp]),
+    "dl_render_traversal_counts": (C.c_int, [_vp, _vp, _vp]),
+    "dl_context_set_kernel_timing": (C.c_int, [_vp, C.c_int]),
+}
+
+
+class DrawlabError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, str(status)), msg))
+        self.status = status
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def lib() -> C.CDLL:
+    """Load libdlgpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise RuntimeError("libdlgpu.so is not built (run drawlab_gb300.build.build())")
+        L = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """A device context: one CUDA stream, device memory owned by the library."""
+
+    def __init__(self, device: int = 0):
+        self.lib = lib()
+        h = C.c_void_p()
+        rc = self.lib.dl_context_create(device, C.byref(h))
+        if rc != abi.DL_OK:
+            raise DrawlabError(rc, self.lib.dl_last_error(None).decode())
+        self.h = h
+
+    def check(self, rc: int):
+        if rc != abi.DL_OK:
+            raise DrawlabError(rc, self.lib.dl_last_error(self.h).decode())
+
+    def set_kernel_timing(self, enabled: bool):
+        self.check(self.lib.dl_context_set_kernel_timing(self.h, 1 if enabled else 0))
+
+    def stats(self) -> abi.dl_stats:
+        s = abi.dl_stats()
+        self.check(self.lib.dl_stats_get(self.h, C.byref(s)))
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dl_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """A scene resident on the device (geometry, BVH, materials, lights)."""
+
+    def __init__(self, ctx: Context, handle: C.c_void_p, data: SceneData | None = None):
+        self.ctx = ctx
+        self.h = handle
+        self.data = data
+        info = self.info()
+        self.width, self.height = info.width, info.height
+
+    @classmethod
+    def from_data(cls, ctx: Context, data: SceneData) -> "Scene":
+        keep, md, nm, mat, nmat, ld, nl, cam = data.descs()
+        h = C.c_void_p()
+        ctx.check(ctx.lib.dl_scene_create_from_arrays(ctx.h, C.cast(md, C.c_void_p), nm, C.cast(mat, C.c_void_p),
+                                                      nmat, C.cast(ld, C.c_void_p), nl, C.byref(cam), C.byref(h)))
+        del keep
+        return cls(ctx, h, data)
+
+    @classmethod
+    def from_xml(cls, ctx: Context, path: str) -> "Scene":
+        h = C.c_void_p()
+        ctx.check(ctx.lib.dl_scene_create_from_xml(ctx.h, str(path).encode(), C.byref(h)))
+        return cls(ctx, h)
+
+    def info(self) -> abi.dl_scene_info:
+        i = abi.dl_scene_info()
+        self.ctx.check(self.ctx.lib.dl_scene_get_info(self.h, C.byref(i)))
+        return i
+
+    def default_opts(self) -> abi.dl_render_opts:
+        o = abi.dl_render_opts()
+        self.ctx.check(self.ctx.lib.dl_scene_default_opts(self.h, C.byref(o)))
+        return o
+
+    def trace_closest(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        prim = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        self.ctx.check(self.ctx.lib.dl_trace_closest(self.h, _ptr(rays), n, _ptr(prim), _ptr(t), _ptr(u), _ptr(v)))
+        return prim, t, u, v
+
+    def trace_any(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        self.ctx.check(self.ctx.lib.dl_trace_any(self.h, _ptr(rays), n, _ptr(occ)))
+        return occ
+
+    def render(self, opts: abi.dl_render_opts) -> np.ndarray:
+        rgb = np.empty((self.height, self.width, 3), np.float32)
+        self.ctx.check(self.ctx.lib.dl_render(self.h, C.byref(opts), _ptr(rgb)))
+        return rgb
+
+    def render_film(self, opts: abi.dl_render_opts) -> np.ndarray:
+        b = 0 if opts.filter == abi.DL_FILTER_BOX else 2
+        film = np.empty((self.height + 2 * b, self.width + 2 * b, 4), np.float32)
+        self.ctx.check(self.ctx.lib.dl_render_film(self.h, C.byref(opts), _ptr(film)))
+        return film
+
+    def li(self, opts: abi.dl_render_opts, xys: np.ndarray):
+        xys = np.ascontiguousarray(xys, np.int32)
+        n = xys.shape[0]
+        L = np.empty((n, 3), np.float32)
+        pos = np.empty((n, 2), np.float32)
+        self.ctx.check(self.ctx.lib.dl_li(self.h, C.byref(opts), n, _ptr(xys), _ptr(L), _ptr(pos)))
+        return L, pos
+
+    def traversal_counts(self, opts: abi.dl_render_opts) -> abi.dl_traversal_counts:
+        c = abi.dl_traversal_counts()
+        self.ctx.check(self.ctx.lib.dl_render_traversal_counts(self.h, C.byref(opts), C.byref(c)))
+        return c
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.dl_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,331 @@
+// The C ABI of include/drawlab.h: argument checks, error capture, buffer
+// staging and dispatch to the scene builder, the trace kernels and the
+// wavefront renderer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "internal.h"
+#include "scene.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+template <typename F>
+int guard(dl_context* ctx, F&& fn) {
+    try {
+        if (ctx) {
+            ctx->error.clear();
+            cudaError_t e = cudaSetDevice(ctx->device);
+            if (e != cudaSuccess) throw dl::Error(DL_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        }
+        fn();
+        return DL_OK;
+    } catch (const dl::Error& e) {
+        if (ctx) ctx->error = e.what(); else g_create_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        if (ctx) ctx->error = "host allocation failed"; else g_create_error = "host allocation failed";
+        return DL_ERR_OOM;
+    } catch (const std::exception& e) {
+        if (ctx) ctx->error = e.what(); else g_create_error = e.what();
+        return DL_ERR_INVALID_ARG;
+    }
+}
+
+void need(bool ok, const char* what) {
+    if (!ok) throw dl::Error(DL_ERR_INVALID_ARG, what);
+}
+
+void check_opts(const dl_render_opts* o) {
+    need(o != nullptr, "opts is NULL");
+    need(o->spp >= 1, "spp must be >= 1");
+    need(o->rr_depth >= 0, "rr_depth must be >= 0");
+    need(o->filter == DL_FILTER_GAUSSIAN || o->filter == DL_FILTER_BOX, "unknown filter");
+    need(o->spp_offset >= 0, "spp_offset must be >= 0");
+    need(o->max_paths_in_flight >= 0 && o->max_paths_in_flight <= ((int64_t)1 << 28), "max_paths_in_flight out of range");
+    need((o->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT)) == 0, "unsupported render flags");
+}
+
+}  // namespace
+
+extern "C" {
+
+int dl_abi_version(void) { return DL_ABI_VERSION; }
+
+const char* dl_last_error(const dl_context* ctx) { return ctx ? ctx->error.c_str() : g_create_error.c_str(); }
+
+int dl_context_create(int device, dl_context** out) {
+    g_create_error.clear();
+    if (!out) {
+        g_create_error = "out is NULL";
+        return DL_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    dl_context* ctx = nullptr;
+    int rc = guard(nullptr, [&] {
+        int n = 0;
+        cudaError_t e = cudaGetDeviceCount(&n);
+        if (e != cudaSuccess || n == 0) throw dl::Error(DL_ERR_CUDA, "no CUDA device available");
+        if (device < 0 || device >= n) throw dl::Error(DL_ERR_INVALID_ARG, "device index out of range");
+        DL_CUDA(cudaSetDevice(device));
+        ctx = new dl_context();
+        ctx->device = device;
+        DL_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        DL_CUDA(cudaEventCreate(&ctx->ev0));
+        DL_CUDA(cudaEventCreate(&ctx->ev1));
+        DL_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    });
+    if (rc != DL_OK) {
+        delete ctx;
+        return rc;
+    }
+    *out = ctx;
+    return DL_OK;
+}
+
+int dl_context_destroy(dl_context* ctx) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return DL_OK;
+}
+
+int dl_scene_create_from_arrays(dl_context* ctx, const dl_mesh_desc* meshes, int32_t num_meshes,
+                                const dl_material_desc* materials, int32_t num_materials,
+                                const dl_light_desc* lights, int32_t num_lights, const dl_camera_desc* camera,
+                                dl_scene** out) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    dl_scene* S = nullptr;
+    int rc = guard(ctx, [&] {
+        need(out != nullptr, "out is NULL");
+        *out = nullptr;
+        S = new dl_scene();
+        S->ctx = ctx;
+        dl::build_scene(S, meshes, num_meshes, materials, num_materials, lights, num_lights, camera);
+    });
+    if (rc != DL_OK) {
+        delete S;
+        return rc;
+    }
+    *out = S;
+    return DL_OK;
+}
+
+int dl_scene_create_from_xml(dl_context* ctx, const char* path, dl_scene** out) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    int rc = DL_OK;
+    int g = guard(ctx, [&] {
+        need(path != nullptr && out != nullptr, "path/out is NULL");
+        rc = dl::load_xml_scene(ctx, path, out);
+    });
+    return g != DL_OK ? g : rc;
+}
+
+int dl_scene_destroy(dl_scene* scene) {
+    if (!scene) return DL_ERR_INVALID_ARG;
+    cudaSetDevice(scene->ctx->device);
+    cudaStreamSynchronize(scene->ctx->stream);
+    delete scene;
+    return DL_OK;
+}
+
+int dl_scene_get_info(const dl_scene* scene, dl_scene_info* info) {
+    if (!scene || !info) return DL_ERR_INVALID_ARG;
+    *info = scene->info;
+    return DL_OK;
+}
+
+int dl_scene_default_opts(const dl_scene* scene, dl_render_opts* opts) {
+    if (!scene || !opts) return DL_ERR_INVALID_ARG;
+    *opts = scene->defaults;
+    return DL_OK;
+}
+
+int dl_trace_closest_device(dl_scene* S, const float* d_rays, int64_t n, float* d_hits) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (d_rays && d_hits)), "bad ray buffers");
+        ctx->trace.occ.ensure(64);
+        dl::trace_closest_launch(S, d_rays, n, d_hits, ctx->trace.occ.ptr, false);
+    });
+}
+
+int dl_trace_any_device(dl_scene* S, const float* d_rays, int64_t n, uint8_t* d_occ) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (d_rays && d_occ)), "bad ray buffers");
+        ctx->trace.occ.ensure(64);
+        dl::trace_any_launch(S, d_rays, n, d_occ, ctx->trace.occ.ptr, false);
+    });
+}
+
+int dl_trace_closest(dl_scene* S, const float* rays, int64_t n, int32_t* prim_id, float* t, float* u, float* v) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (rays && prim_id && t && u && v)), "bad ray buffers");
+        if (n == 0) return;
+        cudaStream_t st = ctx->stream;
+        dl::TraceBuffers& B = ctx->trace;
+        B.rays.ensure((size_t)n * 32);
+        B.hits.ensure((size_t)n * 16);
+        B.occ.ensure(64);
+        B.stage.ensure((size_t)n * 16);
+        DL_CUDA(cudaEventRecord(ctx->ev0, st));
+        DL_CUDA(cudaMemcpyAsync(B.rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, st));
+        dl::trace_closest_launch(S, B.rays.as<float>(), n, B.hits.as<float>(), B.occ.ptr, false);
+        DL_CUDA(cudaMemcpyAsync(B.stage.ptr, B.hits.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+        unsigned int err = 0;
+        DL_CUDA(cudaMemcpyAsync(&err, B.occ.ptr, 4, cudaMemcpyDeviceToHost, st));
+        DL_CUDA(cudaEventRecord(ctx->ev1, st));
+        DL_CUDA(cudaStreamSynchronize(st));
+        if (err) throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+        const float* h = B.stage.as<float>();
+        for (int64_t i = 0; i < n; i++) {
+            t[i] = h[4 * i];
+            u[i] = h[4 * i + 1];
+            v[i] = h[4 * i + 2];
+            std::memcpy(&prim_id[i], &h[4 * i + 3], 4);
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        ctx->stats.trace_ms = ms;
+    });
+}
+
+int dl_trace_any(dl_scene* S, const float* rays, int64_t n, uint8_t* occluded) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (rays && occluded)), "bad ray buffers");
+        if (n == 0) return;
+        cudaStream_t st = ctx->stream;
+        dl::TraceBuffers& B = ctx->trace;
+        B.rays.ensure((size_t)n * 32);
+        B.hits.ensure((size_t)n);
+        B.occ.ensure(64);
+        DL_CUDA(cudaEventRecord(ctx->ev0, st));
+        DL_CUDA(cudaMemcpyAsync(B.rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, st));
+        dl::trace_any_launch(S, B.rays.as<float>(), n, B.hits.as<uint8_t>(), B.occ.ptr, false);
+        DL_CUDA(cudaMemcpyAsync(occluded, B.hits.ptr, (size_t)n, cudaMemcpyDeviceToHost, st));
+        unsigned int err = 0;
+        DL_CUDA(cudaMemcpyAsync(&err, B.occ.ptr, 4, cudaMemcpyDeviceToHost, st));
+        DL_CUDA(cudaEventRecord(ctx->ev1, st));
+        DL_CUDA(cudaStreamSynchronize(st));
+        if (err) throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        ctx->stats.trace_ms = ms;
+    });
+}
+
+int dl_render_film_device(dl_scene* S, const dl_render_opts* opts, float* d_film) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    return guard(S->ctx, [&] {
+        check_opts(opts);
+        need(d_film != nullptr, "d_film is NULL");
+        dl::render_run(S, *opts, d_film, 0, nullptr, nullptr, nullptr, false, nullptr);
+    });
+}
+
+int dl_render_film(dl_scene* S, const dl_render_opts* opts, float* film_out) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        check_opts(opts);
+        need(film_out != nullptr, "film_out is NULL");
+        int64_t nf = dl::film_floats(S->dev.cam.w, S->dev.cam.h, opts->filter);
+        ctx->render.film.ensure((size_t)nf * 4);
+        dl::render_run(S, *opts, ctx->render.film.as<float>(), 0, nullptr, nullptr, nullptr, false, nullptr);
+        DL_CUDA(cudaMemcpyAsync(film_out, ctx->render.film.ptr, (size_t)nf * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int dl_render(dl_scene* S, const dl_render_opts* opts, float* rgb_out) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        check_opts(opts);
+        need(rgb_out != nullptr, "rgb_out is NULL");
+        int64_t nf = dl::film_floats(S->dev.cam.w, S->dev.cam.h, opts->filter);
+        size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;
+        ctx->render.film.ensure((size_t)nf * 4);
+        ctx->render.rgb.ensure(nrgb * 4);
+        dl::render_run(S, *opts, ctx->render.film.as<float>(), 0, nullptr, nullptr, nullptr, false, nullptr);
+        dl::resolve_film(S, ctx->render.film.as<float>(), opts->filter, ctx->render.rgb.as<float>());
+        DL_CUDA(cudaMemcpyAsync(rgb_out, ctx->render.rgb.ptr, nrgb * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int dl_li(dl_scene* S, const dl_render_opts* opts, int64_t n, const int32_t* xys, float* L_out, float* pos_out) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(opts != nullptr, "opts is NULL");
+        need(n >= 0 && (n == 0 || (xys && L_out)), "bad path buffers");
+        if (n == 0) return;
+        const dl::DevCamera& cam = S->dev.cam;
+        for (int64_t i = 0; i < n; i++)
+            need(xys[3 * i] >= 0 && xys[3 * i] < cam.w && xys[3 * i + 1] >= 0 && xys[3 * i + 1] < cam.h &&
+                     xys[3 * i + 2] >= 0,
+                 "path (x, y, s) out of range");
+        dl_render_opts o = *opts;
+        o.spp = 1;
+        check_opts(&o);
+        cudaStream_t st = ctx->stream;
+        dl::RenderBuffers& B = ctx->render;
+        B.li_xys.ensure((size_t)n * 12);
+        B.li_out.ensure((size_t)n * 12);
+        B.li_pos.ensure((size_t)n * 8);
+        DL_CUDA(cudaMemcpyAsync(B.li_xys.ptr, xys, (size_t)n * 12, cudaMemcpyHostToDevice, st));
+        dl::render_run(S, o, nullptr, n, B.li_xys.as<int>(), B.li_out.as<float>(), B.li_pos.as<float>(), false,
+                       nullptr);
+        DL_CUDA(cudaMemcpyAsync(L_out, B.li_out.ptr, (size_t)n * 12, cudaMemcpyDeviceToHost, st));
+        if (pos_out) DL_CUDA(cudaMemcpyAsync(pos_out, B.li_pos.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+        DL_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int dl_render_traversal_counts(dl_scene* S, const dl_render_opts* opts, dl_traversal_counts* out) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        check_opts(opts);
+        need(out != nullptr, "out is NULL");
+        int64_t nf = dl::film_floats(S->dev.cam.w, S->dev.cam.h, opts->filter);
+        ctx->render.film.ensure((size_t)nf * 4);
+        dl::RenderCounters rc;
+        dl::render_run(S, *opts, ctx->render.film.as<float>(), 0, nullptr, nullptr, nullptr, true, &rc);
+        out->extension_rays = (int64_t)rc.stat_ext;
+        out->shadow_rays = (int64_t)rc.stat_shadow;
+        out->node_visits = (int64_t)rc.stat_nodes;
+        out->triangle_tests = (int64_t)rc.stat_tris;
+    });
+}
+
+int dl_context_set_kernel_timing(dl_context* ctx, int enabled) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    ctx->kernel_timing = enabled != 0;
+    return DL_OK;
+}
+
+int dl_stats_get(const dl_context* ctx, dl_stats* stats) {
+    if (!ctx || !stats) return DL_ERR_INVALID_ARG;
+    *stats = ctx->stats;
+    return DL_OK;
+}
+
+}  // extern "C"

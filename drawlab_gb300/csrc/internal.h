@@ -1,0 +1,149 @@
+// Host-side internals of libdlgpu: context, scene, device buffers, errors.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/drawlab.h"
+#include "layout.h"
+
+namespace dl {
+
+// Status-carrying exception used inside the library; converted to a status
+// code and dl_last_error() message at the C ABI.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define DL_CUDA(call)                                                                      \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            throw ::dl::Error(DL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Owning device allocation that only grows.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ptr = nullptr;
+            throw Error(e == cudaErrorMemoryAllocation ? DL_ERR_OOM : DL_ERR_CUDA,
+                        std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(ptr); }
+    template <typename T>
+    void upload(const std::vector<T>& v, cudaStream_t s) {
+        ensure(std::max<size_t>(v.size() * sizeof(T), 16));
+        if (!v.empty()) {
+            DL_CUDA(cudaMemcpyAsync(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+        }
+    }
+};
+
+// Pinned host staging buffer that only grows.
+struct HostBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    ~HostBuf() {
+        if (ptr) cudaFreeHost(ptr);
+    }
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        if (ptr) cudaFreeHost(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        DL_CUDA(cudaMallocHost(&ptr, n));
+        bytes = n;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Device counters of one wavefront render (see render.cu).
+struct RenderCounters {
+    int ext[2];
+    int shadow[2];
+    int retire[2];
+    int pad[2];
+    unsigned long long next_path;
+    unsigned long long stat_ext;
+    unsigned long long stat_shadow;
+    unsigned long long stat_camera;
+    unsigned long long stat_invalid;
+    unsigned long long stat_nodes;
+    unsigned long long stat_tris;
+    unsigned int err;
+    unsigned int pad2;
+};
+
+// Wavefront path-state buffers, sized for the pool and reused across renders.
+struct RenderBuffers {
+    int64_t capacity = 0;
+    DevBuf ray_o, ray_d, hit, tp, lacc, meta, rng, pos;
+    DevBuf ext_q[2], retire_q;
+    DevBuf sh_o, sh_d, sh_c;
+    DevBuf counters;
+    DevBuf film;      // internal film when the caller gives no device film
+    DevBuf rgb;       // resolved image
+    DevBuf li_xys, li_out, li_pos;
+    HostBuf host_counters;
+    HostBuf host_stage;
+    void ensure(int64_t cap);
+    size_t device_bytes() const;
+};
+
+struct TraceBuffers {
+    DevBuf rays, hits, occ;
+    HostBuf stage;
+};
+
+}  // namespace dl
+
+struct dl_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string error;
+    dl_stats stats{};
+    dl::RenderBuffers render;
+    dl::TraceBuffers trace;
+    int num_sms = 0;
+    bool kernel_timing = false;
+    std::vector<cudaEvent_t> timing_events;  // created on first timed render
+    ~dl_context() {
+        for (cudaEvent_t e : timing_events) cudaEventDestroy(e);
+    }
+};
+
+struct dl_scene {
+    dl_context* ctx = nullptr;
+    dl::DevScene dev{};
+    dl::DevBuf nodes, tris, tri_vidx, normals, meshes, materials, lights, emit_tris, emit_cdf;
+    std::vector<int32_t> tri_order;   // leaf-order triangle -> original id
+    dl_scene_info info{};
+    dl_render_opts defaults{};
+    float filter_radius[2] = {2.0f, 0.5f};
+};

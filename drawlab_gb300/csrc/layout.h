@@ -1,0 +1,69 @@
+// Device-visible scene layout (plain structs shared by host and device code).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dl {
+
+// ------------------------------------------------------------------ layout
+constexpr int32_t kEmptyChild = 0x7fffffff;
+constexpr int kStackSize = 64;
+constexpr float kRayEps = 1e-4f;   // M_EPSILON, include/core/math/math.h:14
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr float kInvPiF = 0.31830988618379067154f;
+constexpr float kInvTwoPiF = 0.15915494309189533577f;
+
+enum MatType { MAT_DIFFUSE = 0, MAT_MIRROR = 1, MAT_DIELECTRIC = 2, MAT_MICROFACET = 3, MAT_ANISO_GGX = 4 };
+enum LightType { LIGHT_AREA = 0, LIGHT_POINT = 1, LIGHT_ENVMAP = 2 };
+
+struct DevMaterial {
+    int type;
+    float albedo[3];
+    float specular[3];
+    float ax, ay;
+    float int_ior, ext_ior;
+    float ks;          // microfacet: 1 - max(kd)
+};
+
+struct DevMesh {
+    int material;
+    int light;         // emitter index or -1
+    int has_normals;
+    int pad;
+};
+
+struct DevLight {
+    int type;
+    int mesh;
+    int tri_begin;     // area: first entry in emit_tris (6 float4 per triangle)
+    int tri_count;
+    int cdf_begin;     // area: first entry in emit_cdf (tri_count + 1 floats)
+    int has_normals;
+    float pA;          // area: 1 / total area (DiscretePDF normalisation)
+    float radiance[3];
+    float position[3];
+};
+
+struct DevCamera {
+    int w, h;
+    float eye[3], U[3], V[3], W[3];
+    float inv_w, inv_h;
+};
+
+struct DevScene {
+    const float4* __restrict__ nodes;     // 4 float4 per node
+    const float4* __restrict__ tris;      // 3 float4 per triangle (leaf order)
+    const int4* __restrict__ tri_vidx;    // per leaf-order triangle: vertex ids + mesh id
+    const float4* __restrict__ normals;   // per vertex (global index), w unused
+    const DevMesh* __restrict__ meshes;
+    const DevMaterial* __restrict__ materials;
+    const DevLight* __restrict__ lights;
+    const float4* __restrict__ emit_tris;
+    const float* __restrict__ emit_cdf;
+    int num_tris;
+    int num_lights;
+    DevCamera cam;
+};
+
+}  // namespace dl

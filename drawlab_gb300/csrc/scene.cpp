@@ -1,0 +1,274 @@
+// Scene construction from dl_*_desc arrays: validation, BVH build, emitter
+// tables and upload.  Replaces Scene::addChild / Scene::activate /
+// Mesh::activate / OCTree::build of the reference
+// (src/tracer/scene/scene.cpp:19-106, src/tracer/mesh/mesh.cpp:15-45).
+//
+// Compiled with -ffp-contract=off: the per-face areas and the area CDF of
+// every emitting mesh are computed with the reference's float operations
+// (mesh.cpp:102-108, dpdf.h:70-103) so light sampling picks the same faces.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bvh.h"
+#include "internal.h"
+#include "scene.h"
+
+namespace dl {
+namespace {
+
+struct HV {
+    float x, y, z;
+};
+inline HV hsub(HV a, HV b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline HV hcross(HV a, HV b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float hdot(HV a, HV b) {
+    float s = 0;
+    s += a.x * b.x;
+    s += a.y * b.y;
+    s += a.z * b.z;
+    return s;
+}
+inline float hlen(HV a) { return std::sqrt(hdot(a, a)); }
+inline HV hnorm(HV a) {
+    float l = hlen(a);
+    return {a.x / l, a.y / l, a.z / l};
+}
+inline HV hscale(HV a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline HV ld(const float* p) { return {p[0], p[1], p[2]}; }
+
+void check(bool ok, const std::string& msg) {
+    if (!ok) throw Error(DL_ERR_INVALID_ARG, msg);
+}
+
+}  // namespace
+
+// virtual.cpp:16-42
+DevCamera make_camera(const dl_camera_desc& c) {
+    DevCamera cam;
+    cam.w = c.width;
+    cam.h = c.height;
+    cam.inv_w = 1.f / c.width;
+    cam.inv_h = 1.f / c.height;
+    const float pi = 3.14159265358979323846f;
+    float aspect = c.width / (float)c.height;
+    HV eye = ld(c.eye), look = ld(c.lookat), up = ld(c.up);
+    HV W = hsub(look, eye);
+    float wlen = hlen(W);
+    HV U = hnorm(hcross(W, up));
+    HV V = hnorm(hcross(U, W));
+    float vlen = wlen * tanf(0.5f * c.fov * pi / 180.f);
+    V = hscale(V, vlen);
+    U = hscale(U, vlen * aspect);
+    cam.eye[0] = eye.x; cam.eye[1] = eye.y; cam.eye[2] = eye.z;
+    cam.U[0] = U.x; cam.U[1] = U.y; cam.U[2] = U.z;
+    cam.V[0] = V.x; cam.V[1] = V.y; cam.V[2] = V.z;
+    cam.W[0] = W.x; cam.W[1] = W.y; cam.W[2] = W.z;
+    return cam;
+}
+
+void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,
+                    const dl_light_desc* lights, int32_t nl, const dl_camera_desc* cam) {
+    check(nm >= 0 && nmat >= 0 && nl >= 0, "negative count");
+    check(nm == 0 || meshes, "meshes is NULL");
+    check(nmat == 0 || mats, "materials is NULL");
+    check(nl == 0 || lights, "lights is NULL");
+    check(cam != nullptr, "camera is NULL");
+    check(cam->type == DL_CAMERA_VIRTUAL, "unsupported camera type");
+    check(cam->width > 0 && cam->height > 0 && cam->width <= 65536 && cam->height <= 65536,
+          "camera resolution out of range");
+    check(cam->fov > 0.f && cam->fov < 180.f, "camera fov out of range");
+    int64_t total = 0;
+    for (int i = 0; i < nm; i++) {
+        const dl_mesh_desc& m = meshes[i];
+        check(m.num_vertices >= 0 && m.num_triangles >= 0, "mesh " + std::to_string(i) + ": negative size");
+        check(m.num_triangles == 0 || (m.positions && m.indices), "mesh " + std::to_string(i) + ": NULL arrays");
+        check(m.material >= 0 && m.material < nmat, "mesh " + std::to_string(i) + ": material out of range");
+        check(m.light >= -1 && m.light < nl, "mesh " + std::to_string(i) + ": light out of range");
+        if (m.light >= 0)
+            check(lights[m.light].type == DL_LIGHT_AREA && lights[m.light].mesh == i,
+                  "mesh " + std::to_string(i) + ": light is not an area light of this mesh");
+        for (int64_t k = 0; k < 3 * m.num_triangles; k++)
+            check(m.indices[k] < (uint64_t)m.num_vertices, "mesh " + std::to_string(i) + ": vertex index out of range");
+        for (int64_t k = 0; k < 3 * m.num_vertices; k++)
+            check(std::isfinite(m.positions[k]), "mesh " + std::to_string(i) + ": non-finite vertex");
+        total += m.num_triangles;
+    }
+    check(total < (int64_t)1 << 27, "too many triangles (limit 2^27)");
+    for (int i = 0; i < nmat; i++) {
+        const dl_material_desc& m = mats[i];
+        check(m.type >= DL_MAT_DIFFUSE && m.type <= DL_MAT_ANISO_GGX, "material " + std::to_string(i) + ": bad type");
+        if (m.type == DL_MAT_MICROFACET) check(m.alpha[0] > 0.f, "microfacet alpha must be > 0");
+        if (m.type == DL_MAT_ANISO_GGX) check(m.alpha[0] > 0.f && m.alpha[1] > 0.f, "aniso_ggx alpha must be > 0");
+    }
+    for (int l = 0; l < nl; l++) {
+        const dl_light_desc& L = lights[l];
+        if (L.type == DL_LIGHT_AREA) {
+            check(L.mesh >= 0 && L.mesh < nm, "light " + std::to_string(l) + ": mesh out of range");
+            check(meshes[L.mesh].light == l, "light " + std::to_string(l) + ": mesh does not point back to it");
+            check(meshes[L.mesh].num_triangles > 0, "light " + std::to_string(l) + ": emitting mesh is empty");
+        } else if (L.type == DL_LIGHT_POINT) {
+        } else if (L.type == DL_LIGHT_ENVMAP) {
+            throw Error(DL_ERR_UNSUPPORTED, "environment lights are not supported yet");
+        } else {
+            throw Error(DL_ERR_INVALID_ARG, "light " + std::to_string(l) + ": bad type");
+        }
+    }
+}
+
+void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,
+                 const dl_light_desc* lights, int32_t nl, const dl_camera_desc* cam) {
+    validate_scene(meshes, nm, mats, nmat, lights, nl, cam);
+    cudaStream_t st = S->ctx->stream;
+    int64_t ntri = 0, nvert = 0;
+    for (int i = 0; i < nm; i++) {
+        ntri += meshes[i].num_triangles;
+        nvert += meshes[i].num_vertices;
+    }
+    std::vector<float> tri9((size_t)ntri * 9);
+    std::vector<int4> vidx_orig((size_t)ntri);
+    std::vector<float4> normals((size_t)std::max<int64_t>(nvert, 1));
+    std::vector<DevMesh> dmesh(std::max(nm, 1));
+    int64_t t = 0, vo = 0;
+    for (int i = 0; i < nm; i++) {
+        const dl_mesh_desc& m = meshes[i];
+        for (int64_t f = 0; f < m.num_triangles; f++, t++) {
+            for (int k = 0; k < 3; k++) {
+                uint32_t vi = m.indices[3 * f + k];
+                std::memcpy(&tri9[9 * t + 3 * k], m.positions + 3 * vi, 12);
+            }
+            vidx_orig[t] = make_int4((int)(vo + m.indices[3 * f]), (int)(vo + m.indices[3 * f + 1]),
+                                     (int)(vo + m.indices[3 * f + 2]), i);
+        }
+        for (int64_t v = 0; v < m.num_vertices; v++) {
+            if (m.normals)
+                normals[vo + v] = make_float4(m.normals[3 * v], m.normals[3 * v + 1], m.normals[3 * v + 2], 0.f);
+            else
+                normals[vo + v] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        dmesh[i].material = m.material;
+        dmesh[i].light = m.light;
+        dmesh[i].has_normals = m.normals != nullptr;
+        dmesh[i].pad = 0;
+        vo += m.num_vertices;
+    }
+    BvhBuildOptions bo;
+    BvhResult bvh = build_bvh(tri9.data(), ntri, bo);
+    std::vector<int4> vidx((size_t)std::max<int64_t>(ntri, 1));
+    for (size_t k = 0; k < bvh.tri_order.size(); k++) vidx[k] = vidx_orig[bvh.tri_order[k]];
+
+    std::vector<DevMaterial> dmat(std::max(nmat, 1));
+    for (int i = 0; i < nmat; i++) {
+        const dl_material_desc& m = mats[i];
+        DevMaterial& d = dmat[i];
+        d.type = m.type;
+        for (int k = 0; k < 3; k++) {
+            d.albedo[k] = m.albedo[k];
+            d.specular[k] = m.specular[k];
+        }
+        d.ax = m.alpha[0];
+        d.ay = m.alpha[1];
+        d.int_ior = m.int_ior;
+        d.ext_ior = m.ext_ior;
+        d.ks = 1 - std::max(std::max(m.albedo[0], m.albedo[1]), m.albedo[2]);
+    }
+
+    std::vector<DevLight> dlights(std::max(nl, 1));
+    std::vector<float4> etris;
+    std::vector<float> ecdf;
+    for (int l = 0; l < nl; l++) {
+        const dl_light_desc& L = lights[l];
+        DevLight& d = dlights[l];
+        std::memset(&d, 0, sizeof(d));
+        d.type = L.type;
+        d.mesh = L.mesh;
+        for (int k = 0; k < 3; k++) {
+            d.radiance[k] = L.radiance[k];
+            d.position[k] = L.position[k];
+        }
+        if (L.type == DL_LIGHT_AREA) {
+            const dl_mesh_desc& m = meshes[L.mesh];
+            d.tri_begin = (int)(etris.size() / 6);
+            d.tri_count = (int)m.num_triangles;
+            d.cdf_begin = (int)ecdf.size();
+            d.has_normals = m.normals != nullptr;
+            // DiscretePDF over face areas (mesh.cpp:21-28, dpdf.h:70-103)
+            std::vector<float> cdf;
+            cdf.push_back(0.0f);
+            for (int64_t f = 0; f < m.num_triangles; f++) {
+                HV p[3], n[3];
+                for (int k = 0; k < 3; k++) {
+                    uint32_t vi = m.indices[3 * f + k];
+                    p[k] = ld(m.positions + 3 * vi);
+                    n[k] = m.normals ? ld(m.normals + 3 * vi) : HV{0, 0, 0};
+                }
+                float area = 0.5f * hlen(hcross(hsub(p[1], p[0]), hsub(p[2], p[0])));
+                cdf.push_back(cdf.back() + area);
+                for (int k = 0; k < 3; k++) etris.push_back(make_float4(p[k].x, p[k].y, p[k].z, 0.f));
+                for (int k = 0; k < 3; k++) etris.push_back(make_float4(n[k].x, n[k].y, n[k].z, 0.f));
+            }
+            float sum = cdf.back();
+            float norm = 0.0f;
+            if (sum > 0) {
+                norm = 1.0f / sum;
+                for (size_t i = 1; i < cdf.size(); ++i) cdf[i] *= norm;
+                cdf.back() = 1.0f;
+            }
+            d.pA = norm;
+            ecdf.insert(ecdf.end(), cdf.begin(), cdf.end());
+        }
+    }
+
+    S->nodes.upload(bvh.nodes, st);
+    S->tris.upload(bvh.tris, st);
+    S->tri_vidx.upload(vidx, st);
+    S->normals.upload(normals, st);
+    S->meshes.upload(dmesh, st);
+    S->materials.upload(dmat, st);
+    S->lights.upload(dlights, st);
+    if (etris.empty()) etris.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+    if (ecdf.empty()) ecdf.push_back(0.f);
+    S->emit_tris.upload(etris, st);
+    S->emit_cdf.upload(ecdf, st);
+    DL_CUDA(cudaStreamSynchronize(st));
+
+    DevScene& D = S->dev;
+    D.nodes = S->nodes.as<float4>();
+    D.tris = S->tris.as<float4>();
+    D.tri_vidx = S->tri_vidx.as<int4>();
+    D.normals = S->normals.as<float4>();
+    D.meshes = S->meshes.as<DevMesh>();
+    D.materials = S->materials.as<DevMaterial>();
+    D.lights = S->lights.as<DevLight>();
+    D.emit_tris = S->emit_tris.as<float4>();
+    D.emit_cdf = S->emit_cdf.as<float>();
+    D.num_tris = (int)ntri;
+    D.num_lights = nl;
+    D.cam = make_camera(*cam);
+    S->tri_order = bvh.tri_order;
+
+    dl_scene_info& I = S->info;
+    I.num_triangles = ntri;
+    I.num_bvh_nodes = (int64_t)bvh.nodes.size();
+    I.num_meshes = nm;
+    I.num_materials = nmat;
+    I.num_lights = nl;
+    I.width = cam->width;
+    I.height = cam->height;
+    I.bvh_depth = bvh.depth;
+    I.bvh_build_seconds = bvh.seconds;
+    I.bvh_sah_cost = bvh.sah_cost;
+    I.device_bytes = (int64_t)(S->nodes.bytes + S->tris.bytes + S->tri_vidx.bytes + S->normals.bytes +
+                               S->meshes.bytes + S->materials.bytes + S->lights.bytes + S->emit_tris.bytes +
+                               S->emit_cdf.bytes);
+    dl_render_opts& O = S->defaults;
+    std::memset(&O, 0, sizeof(O));
+    O.spp = 1;
+    O.max_depth = 0;
+    O.rr_depth = 3;
+    O.filter = DL_FILTER_GAUSSIAN;
+}
+
+}  // namespace dl

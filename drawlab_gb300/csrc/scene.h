@@ -1,0 +1,26 @@
+// Scene construction (scene.cpp) and the launchers of trace.cu / render.cu.
+#pragma once
+
+#include "internal.h"
+
+namespace dl {
+
+DevCamera make_camera(const dl_camera_desc& c);
+void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,
+                    const dl_light_desc* lights, int32_t nl, const dl_camera_desc* cam);
+void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,
+                 const dl_light_desc* lights, int32_t nl, const dl_camera_desc* cam);
+
+void trace_closest_launch(dl_scene* S, const float* d_rays, int64_t n, float* d_hits, void* scratch, bool count);
+void trace_any_launch(dl_scene* S, const float* d_rays, int64_t n, uint8_t* d_occ, void* scratch, bool count);
+
+int64_t film_floats(int w, int h, int filter);
+void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys, float* d_L,
+                float* d_pos, bool count_traversal, RenderCounters* out_counters);
+void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb);
+
+// XML scene loading (xml.cpp): fills arrays and default render options.
+struct XmlScene;
+int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out);
+
+}  // namespace dl

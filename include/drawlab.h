@@ -257,10 +257,32 @@ typedef struct dl_stats {
     int64_t iterations;        /* wavefront iterations of the last render */
     double render_ms;          /* device time of the last render */
     double trace_ms;           /* device time of the last dl_trace_* call */
+    /* Per-kernel device time of the last render, summed over its launches
+     * (CUDA events on the context stream; filled only while kernel timing is
+     * enabled, see dl_context_set_kernel_timing). */
+    double extend_ms;          /* closest-hit traversal */
+    double shadow_ms;          /* any-hit traversal */
+    double shade_ms;           /* shading, NEE, BSDF sampling, film splat */
+    double retire_ms;          /* deferred path completion */
+    int64_t kernel_launches;   /* kernels launched by the last render */
 } dl_stats;
+
+/* Enable (1) or disable (0) per-kernel event timing on a context. */
+int dl_context_set_kernel_timing(dl_context* ctx, int enabled);
 
 /* Counters of the last dl_render* / dl_li / dl_trace_* call on ctx. */
 int dl_stats_get(const dl_context* ctx, dl_stats* stats);
+
+/* Measurement aid (not for timing): repeats a render with per-ray traversal
+ * counters enabled and reports the BVH node visits and triangle tests of its
+ * extension and shadow rays.  No reference counterpart. */
+typedef struct dl_traversal_counts {
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    int64_t node_visits;
+    int64_t triangle_tests;
+} dl_traversal_counts;
+int dl_render_traversal_counts(dl_scene* scene, const dl_render_opts* opts, dl_traversal_counts* out);
 
 #ifdef __cplusplus
 }

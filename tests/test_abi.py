@@ -1,0 +1,77 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every entry
+point include/drawlab.h declares, and fails cleanly where a device is needed."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from drawlab_gb300 import abi, api
+from drawlab_gb300 import build as gpu_build
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    for fn in os.listdir(os.path.join(REPO, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(REPO, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:int|const char\*)\s+(dl_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    gpu_build.build()
+    return api.lib()
+
+
+def test_library_exports_every_header_function(lib):
+    names = header_functions()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_binding_covers_every_header_function():
+    assert sorted(api.SIGNATURES) == header_functions()
+
+
+def test_abi_version(lib):
+    assert lib.dl_abi_version() == abi.DL_ABI_VERSION
+
+
+def test_struct_sizes_match_header():
+    # sizes of the descriptor structs as laid out by a C compiler (x86-64/aarch64 LP64)
+    assert C.sizeof(abi.dl_mesh_desc) == 4 * 8 + 2 * 8 + 2 * 4
+    assert C.sizeof(abi.dl_material_desc) == 4 * (1 + 3 + 3 + 2 + 2)
+    assert C.sizeof(abi.dl_render_opts) == 4 * 4 + 8 + 4 + 4 + 8
+    assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1)
+
+
+def test_null_handles_are_rejected(lib):
+    assert lib.dl_scene_destroy(None) == abi.DL_ERR_INVALID_ARG
+    assert lib.dl_context_destroy(None) == abi.DL_ERR_INVALID_ARG
+    assert lib.dl_render(None, None, None) == abi.DL_ERR_INVALID_ARG
+    assert lib.dl_stats_get(None, None) == abi.DL_ERR_INVALID_ARG
+    h = C.c_void_p()
+    assert lib.dl_context_create(0, None) == abi.DL_ERR_INVALID_ARG
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a GPU is present")
+def test_context_creation_fails_cleanly_without_gpu(lib):
+    h = C.c_void_p()
+    rc = lib.dl_context_create(0, C.byref(h))
+    assert rc == abi.DL_ERR_CUDA
+    assert b"CUDA" in lib.dl_last_error(None)
+    assert not h.value

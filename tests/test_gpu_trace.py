@@ -1,0 +1,137 @@
+"""First-hit and shadow-ray parity of the GPU traversal (dl_trace_closest /
+dl_trace_any) against the oracle's octree (and the reference's golden
+vectors).
+
+Bar: the same triangle id for every ray, hit t/u/v bit-identical (the device
+runs the reference's Moller-Trumbore with the same float operations),
+except rays whose hit lies within 1e-6 of a triangle edge or ties two
+triangles within 1e-5 in t, where the octree's and the BVH's visiting
+orders may legitimately pick different triangles.  Those rays must stay
+rarer than 0.2 %.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import make_golden as mg
+import pyoracle as po
+from drawlab_gb300 import abi, api, scenes
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+EDGE = 1e-6
+TIE = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return api.Context(0)
+
+
+def near_edge(u, v, hit):
+    w = 1.0 - u - v
+    return hit & (np.minimum(np.minimum(u, v), w) < EDGE)
+
+
+def compare_closest(g, o):
+    gp, gt, gu, gv = g
+    op, ot, ou, ov = o
+    ambiguous = near_edge(gu, gv, gp >= 0) | near_edge(ou, ov, op >= 0)
+    both = (gp >= 0) & (op >= 0) & (gp != op)
+    ambiguous |= both & (np.abs(gt - ot) <= TIE * np.maximum(np.abs(ot), 1e-30))
+    keep = ~ambiguous
+    assert ambiguous.mean() < 2e-3, "too many ambiguous rays: %.5f" % ambiguous.mean()
+    np.testing.assert_array_equal(gp[keep], op[keep])
+    hit = keep & (op >= 0)
+    np.testing.assert_array_equal(gt[hit], ot[hit])
+    np.testing.assert_array_equal(gu[hit], ou[hit])
+    np.testing.assert_array_equal(gv[hit], ov[hit])
+    return keep
+
+
+def scene_cases():
+    return {
+        "cornell": scenes.cornell(),
+        "refspheres": scenes.reference_spheres(),
+        "mis_plates": scenes.mis_plates(width=320, height=180),
+        "spheres16": scenes.material_spheres(width=320, height=180, num_spheres=16, level=3),
+    }
+
+
+CASES = scene_cases()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_first_hit_matches_oracle(ctx, name):
+    sc = CASES[name]
+    gs = api.Scene.from_data(ctx, sc)
+    orc = po.OracleScene(sc)
+    rays = mg.seeded_rays(sc, 60000, seed=17)
+    keep = compare_closest(gs.trace_closest(rays), orc.trace_closest(rays))
+    # any-hit on the same rays with a finite tmax halfway to the closest hit
+    prim, t, _, _ = orc.trace_closest(rays)
+    r2 = rays.copy()
+    hit = prim >= 0
+    r2[hit, 7] = np.where(np.arange(hit.sum()) % 2 == 0, 0.5 * t[hit], 1.5 * t[hit])
+    g_occ = gs.trace_any(r2)
+    o_occ = orc.trace_any(r2)
+    near_tmax = hit & (np.abs(r2[:, 7] - t) <= TIE * np.abs(t))
+    ok = keep & ~near_tmax
+    np.testing.assert_array_equal(g_occ[ok], o_occ[ok])
+
+
+@pytest.mark.parametrize("name", ["cornell", "refspheres"])
+def test_first_hit_matches_reference_golden(ctx, name):
+    sc = mg.fixture_scenes()[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}_trace.npz"))
+    gs = api.Scene.from_data(ctx, sc)
+    compare_closest(gs.trace_closest(g["rays"]), (g["prim"], g["t"], g["u"], g["v"]))
+    np.testing.assert_array_equal(gs.trace_any(g["rays"]), g["occ"])
+
+
+def test_full_material_scene_first_hits(ctx):
+    # the 327,682-triangle scene, 100k seeded rays
+    sc = scenes.material_spheres(width=320, height=180)
+    gs = api.Scene.from_data(ctx, sc)
+    info = gs.info()
+    assert info.num_triangles == 327682
+    assert info.bvh_depth <= 64
+    orc = po.OracleScene(sc)
+    rays = mg.seeded_rays(sc, 100000, seed=23)
+    compare_closest(gs.trace_closest(rays), orc.trace_closest(rays))
+
+
+def test_edge_cases(ctx):
+    sc = scenes.cornell()
+    gs = api.Scene.from_data(ctx, sc)
+    orc = po.OracleScene(sc)
+    rays = np.zeros((6, 8), np.float32)
+    rays[:, 3] = 1e-4
+    rays[:, 7] = np.inf
+    rays[0, 4:7] = (0, 0, 0)                 # zero direction: no hit
+    rays[1, 4:7] = (0, 0, -1)                # straight at the back wall
+    rays[2, 4:7] = (1, 0, 0)                 # axis-aligned, red/green walls
+    rays[3, 4:7] = (0, 0, -1)
+    rays[3, 3], rays[3, 7] = 5.0, 1.0        # tmin > tmax: no hit
+    rays[4, 0:3] = (0, 0, 10)
+    rays[4, 4:7] = (0, 0, 1)                 # pointing away from the scene
+    rays[5, 0:3] = (0.0, 2.0, 0.0)
+    rays[5, 4:7] = (0, -1, 0)                # from above through the ceiling
+    compare_closest(gs.trace_closest(rays), orc.trace_closest(rays))
+    assert gs.trace_closest(rays[:0])[0].shape == (0,)
+    np.testing.assert_array_equal(gs.trace_any(rays), orc.trace_any(rays))
+
+
+def test_empty_scene_misses(ctx):
+    sc = scenes.SceneData("empty")
+    sc.materials.append(scenes.Material())
+    sc.camera = scenes.Camera(width=8, height=8)
+    gs = api.Scene.from_data(ctx, sc)
+    rays = np.zeros((4, 8), np.float32)
+    rays[:, 6] = 1
+    rays[:, 7] = np.inf
+    prim, t, u, v = gs.trace_closest(rays)
+    assert (prim == -1).all()
+    assert (gs.trace_any(rays) == 0).all()
