@@ -39,7 +39,8 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 WORKLOAD = dict(workload="material_spheres", width=1920, height=1080, spp=64, max_depth=16,
-                triangles=327682, spheres=64, sphere_level=4, area_lights=4, point_lights=1)
+                triangles=327690, spheres=64, sphere_level=4, area_lights=4, point_lights=1,
+                triangles_note="64 x 5120 sphere + 2 ground + 8 light-quad triangles")
 METRIC = "samples/s (material-sphere scene 1920x1080, 64 spp, depth 16)"
 
 # algorithmic bytes per closest-hit ray: node = 64 B (both child boxes + refs),

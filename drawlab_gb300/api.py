@@ -6,7 +6,9 @@ missing or no GPU is present, calls raise.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -74,6 +76,20 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
+# Contexts still open at interpreter exit are closed (scenes first) before
+# the CUDA runtime tears itself down.
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    for c in list(_live_contexts):
+        try:
+            c.close()
+        except Exception:
+            pass
+
+
 class Context:
     """A device context: one CUDA stream, device memory owned by the library."""
 
@@ -84,6 +100,9 @@ class Context:
         if rc != abi.DL_OK:
             raise DrawlabError(rc, self.lib.dl_last_error(None).decode())
         self.h = h
+        # scenes must be destroyed before their context: keep track of them
+        self._scenes = weakref.WeakSet()
+        _live_contexts.add(self)
 
     def check(self, rc: int):
         if rc != abi.DL_OK:
@@ -99,6 +118,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            for s in list(getattr(self, "_scenes", ())):
+                s.close()
             self.lib.dl_context_destroy(self.h)
             self.h = None
 
@@ -116,6 +137,7 @@ class Scene:
         self.ctx = ctx
         self.h = handle
         self.data = data
+        ctx._scenes.add(self)
         info = self.info()
         self.width, self.height = info.width, info.height
 
@@ -185,7 +207,8 @@ class Scene:
 
     def close(self):
         if getattr(self, "h", None):
-            self.ctx.lib.dl_scene_destroy(self.h)
+            if getattr(self.ctx, "h", None):   # the context still exists
+                self.ctx.lib.dl_scene_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -1,0 +1,133 @@
+"""Scenes in the reference's XML format (dl_scene_create_from_xml) against the
+same scene built from arrays: identical geometry gives identical hits and
+identical per-path radiance; malformed files fail with DL_ERR_PARSE."""
+import numpy as np
+import pytest
+
+import make_golden as mg
+from drawlab_gb300 import abi, api, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return api.Context(0)
+
+
+def cornell_xml(sc, obj_path):
+    def v(x):
+        return ", ".join("%.9g" % float(c) for c in x)
+
+    quads = [((-1, -1, -1), (0, 0, 2), (2, 0, 0), (0.725, 0.725, 0.725)),
+             ((-1, 1, -1), (2, 0, 0), (0, 0, 2), (0.725, 0.725, 0.725)),
+             ((-1, -1, -1), (2, 0, 0), (0, 2, 0), (0.725, 0.725, 0.725)),
+             ((-1, -1, -1), (0, 2, 0), (0, 0, 2), (0.63, 0.065, 0.05)),
+             ((1, -1, -1), (0, 0, 2), (0, 2, 0), (0.14, 0.45, 0.09))]
+    out = ['<?xml version="1.0"?>', "<!-- Cornell box in the reference's scene format -->", "<scene>",
+           '  <integrator type="path"/>',
+           '  <sampler type="independent"><integer name="sampleCount" value="7"/></sampler>',
+           '  <camera type="virtual">',
+           '    <vector name="eye" value="%s"/>' % v(sc.camera.eye),
+           '    <vector name="lookat" value="%s"/>' % v(sc.camera.lookat),
+           '    <vector name="up" value="%s"/>' % v(sc.camera.up),
+           '    <float name="fov" value="%.9g"/>' % sc.camera.fov,
+           '    <integer name="width" value="%d"/>' % sc.camera.width,
+           '    <integer name="height" value="%d"/>' % sc.camera.height,
+           '    <rfilter type="gaussian"/>',
+           "  </camera>",
+           '  <bsdf type="diffuse" id="white"><color name="albedo" value="0.725, 0.725, 0.725"/></bsdf>']
+    for pos, a, b, alb in quads:
+        out += ['  <mesh type="rectangle">', '    <vector name="pos" value="%s"/>' % v(pos),
+                '    <vector name="v0" value="%s"/>' % v(a), '    <vector name="v1" value="%s"/>' % v(b),
+                '    <bsdf type="diffuse"><color name="albedo" value="%s"/></bsdf>' % v(alb), "  </mesh>"]
+    out += ['  <mesh type="obj">', '    <string name="filename" value="%s"/>' % obj_path,
+            '    <ref id="white"/>', '    <transform name="toWorld">',
+            '      <translate value="0.0, 0.0, 0.0"/>', "    </transform>", "  </mesh>",
+            '  <mesh type="rectangle">', '    <vector name="pos" value="-0.25, 0.999, -0.2"/>',
+            '    <vector name="v0" value="0.5, 0, 0"/>', '    <vector name="v1" value="0, 0, 0.4"/>',
+            '    <bsdf type="diffuse"><color name="albedo" value="0, 0, 0"/></bsdf>',
+            '    <emitter type="area"><color name="radiance" value="17, 12, 4"/></emitter>', "  </mesh>",
+            "</scene>"]
+    return "\n".join(out)
+
+
+def write_obj(path, P, F, N):
+    with open(path, "w") as f:
+        f.write("# cuboid\n")
+        for p in P:
+            f.write("v %.9g %.9g %.9g\n" % tuple(p))
+        for n in N:
+            f.write("vn %.9g %.9g %.9g\n" % tuple(n))
+        for t in F:
+            f.write("f %d//%d %d//%d %d//%d\n" % (t[0] + 1, t[0] + 1, t[1] + 1, t[1] + 1, t[2] + 1, t[2] + 1))
+
+
+def arrays_equivalent():
+    """The XML scene as arrays: 5 quads, one cuboid mesh, the light quad."""
+    s = scenes.SceneData("cornell_xml")
+    base = scenes.cornell(width=40, height=32)
+    s.camera = base.camera
+    for m in base.meshes[:5]:
+        s.meshes.append(m)
+    s.materials = list(base.materials)
+    white = s.add_material(scenes.Material(albedo=(0.725, 0.725, 0.725)))
+    P, F, N = scenes.cuboid((0.34, -1 + 0.3 + 1e-3, 0.32), (0.6, 0.6, 0.6), -17.0)
+    s.add_mesh(scenes.Mesh(P, F, N, material=white))
+    p, f, n = scenes.rectangle((-0.25, 0.999, -0.2), (0.5, 0, 0), (0, 0, 0.4))
+    li = s.add_mesh(scenes.Mesh(p, f, n, material=3))
+    s.add_area_light(li, (17.0, 12.0, 4.0))
+    return s, (P, F, N)
+
+
+def test_xml_scene_matches_arrays(ctx, tmp_path):
+    arr, (P, F, N) = arrays_equivalent()
+    # the OBJ round-trips through text: write with 9 significant digits (exact for float32)
+    write_obj(tmp_path / "cuboid.obj", P, F, N)
+    (tmp_path / "scene.xml").write_text(cornell_xml(arr, "cuboid.obj"))
+    gx = api.Scene.from_xml(ctx, str(tmp_path / "scene.xml"))
+    ga = api.Scene.from_data(ctx, arr)
+    ix, ia = gx.info(), ga.info()
+    assert (ix.num_triangles, ix.num_lights, ix.width, ix.height) == (ia.num_triangles, ia.num_lights, 40, 32)
+    d = gx.default_opts()
+    assert d.spp == 7 and d.filter == abi.DL_FILTER_GAUSSIAN and d.rr_depth == 3 and d.max_depth == 0
+    rays = mg.seeded_rays(arr, 20000, seed=5)
+    a, b = gx.trace_closest(rays), ga.trace_closest(rays)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    xys = np.array([(x, y, s) for y in range(32) for x in range(40) for s in range(2)], np.int32)
+    opts = abi.make_opts(seed=3, max_depth=6)
+    La, _ = gx.li(opts, xys)
+    Lb, _ = ga.li(opts, xys)
+    np.testing.assert_array_equal(La, Lb)
+
+
+@pytest.mark.parametrize("text,needle", [
+    ("<scene><integrator type='path'/>", "unterminated"),
+    ("<scene><foo/></scene>", "unexpected tag"),
+    ("<scene><integrator type='path'/></scene>", "No camera"),
+    ("<scene><camera type='virtual'><vector name='eye' value='0,0'/></camera></scene>", "expected 3 values"),
+    ("<scene><integrator type='path' bogus='1'/></scene>", "unexpected attribute"),
+    ("<scene><mesh type='rectangle'><ref id='nothere'/></mesh></scene>", "can't find"),
+])
+def test_malformed_xml_is_reported(ctx, tmp_path, text, needle):
+    p = tmp_path / "bad.xml"
+    p.write_text(text)
+    with pytest.raises(api.DrawlabError) as e:
+        api.Scene.from_xml(ctx, str(p))
+    assert e.value.status == abi.DL_ERR_PARSE
+    assert needle in str(e.value)
+
+
+def test_missing_file_is_io_error(ctx, tmp_path):
+    with pytest.raises(api.DrawlabError) as e:
+        api.Scene.from_xml(ctx, str(tmp_path / "none.xml"))
+    assert e.value.status == abi.DL_ERR_IO
+
+
+def test_unsupported_plugin_is_reported(ctx, tmp_path):
+    p = tmp_path / "u.xml"
+    p.write_text("<scene><integrator type='normals'/></scene>")
+    with pytest.raises(api.DrawlabError) as e:
+        api.Scene.from_xml(ctx, str(p))
+    assert e.value.status == abi.DL_ERR_UNSUPPORTED
