@@ -148,8 +148,10 @@ class dl_traversal_counts(C.Structure):
     _fields_ = [
         ("extension_rays", C.c_int64),
         ("shadow_rays", C.c_int64),
-        ("node_visits", C.c_int64),
-        ("triangle_tests", C.c_int64),
+        ("extension_node_visits", C.c_int64),
+        ("extension_triangle_tests", C.c_int64),
+        ("shadow_node_visits", C.c_int64),
+        ("shadow_triangle_tests", C.c_int64),
     ]
 
 

@@ -311,8 +311,10 @@ int dl_render_traversal_counts(dl_scene* S, const dl_render_opts* opts, dl_trave
         dl::render_run(S, *opts, ctx->render.film.as<float>(), 0, nullptr, nullptr, nullptr, true, &rc);
         out->extension_rays = (int64_t)rc.stat_ext;
         out->shadow_rays = (int64_t)rc.stat_shadow;
-        out->node_visits = (int64_t)rc.stat_nodes;
-        out->triangle_tests = (int64_t)rc.stat_tris;
+        out->extension_node_visits = (int64_t)rc.stat_nodes_ext;
+        out->extension_triangle_tests = (int64_t)rc.stat_tris_ext;
+        out->shadow_node_visits = (int64_t)rc.stat_nodes_sh;
+        out->shadow_triangle_tests = (int64_t)rc.stat_tris_sh;
     });
 }
 

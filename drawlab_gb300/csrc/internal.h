@@ -93,8 +93,10 @@ struct RenderCounters {
     unsigned long long stat_shadow;
     unsigned long long stat_camera;
     unsigned long long stat_invalid;
-    unsigned long long stat_nodes;
-    unsigned long long stat_tris;
+    unsigned long long stat_nodes_ext;
+    unsigned long long stat_tris_ext;
+    unsigned long long stat_nodes_sh;
+    unsigned long long stat_tris_sh;
     unsigned int err;
     unsigned int pad2;
 };

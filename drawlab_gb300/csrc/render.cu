@@ -212,8 +212,8 @@ __global__ void __launch_bounds__(128) k_extend(RenderParams P, int p) {
     }
     if (err) atomicOr(&P.cnt->err, err);
     if (kCount) {
-        atomicAdd(&P.cnt->stat_nodes, (unsigned long long)nn);
-        atomicAdd(&P.cnt->stat_tris, (unsigned long long)nt);
+        atomicAdd(&P.cnt->stat_nodes_ext, (unsigned long long)nn);
+        atomicAdd(&P.cnt->stat_tris_ext, (unsigned long long)nt);
     }
 }
 
@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(128) k_shadow(RenderParams P, int p) {
     }
     if (err) atomicOr(&P.cnt->err, err);
     if (kCount) {
-        atomicAdd(&P.cnt->stat_nodes, (unsigned long long)nn);
-        atomicAdd(&P.cnt->stat_tris, (unsigned long long)nt);
+        atomicAdd(&P.cnt->stat_nodes_sh, (unsigned long long)nn);
+        atomicAdd(&P.cnt->stat_tris_sh, (unsigned long long)nt);
     }
 }
 

@@ -279,8 +279,10 @@ int dl_stats_get(const dl_context* ctx, dl_stats* stats);
 typedef struct dl_traversal_counts {
     int64_t extension_rays;
     int64_t shadow_rays;
-    int64_t node_visits;
-    int64_t triangle_tests;
+    int64_t extension_node_visits;     /* BVH nodes fetched by closest-hit rays */
+    int64_t extension_triangle_tests;  /* triangles tested by closest-hit rays */
+    int64_t shadow_node_visits;
+    int64_t shadow_triangle_tests;
 } dl_traversal_counts;
 int dl_render_traversal_counts(dl_scene* scene, const dl_render_opts* opts, dl_traversal_counts* out);
 
