@@ -44,6 +44,7 @@ SIGNATURES = {
     "dl_stats_get": (C.c_int, [_vp, _vp]),
     "dl_render_traversal_counts": (C.c_int, [_vp, _vp, _vp]),
     "dl_context_set_kernel_timing": (C.c_int, [_vp, C.c_int]),
+    "dl_li_static": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
 }
 
 

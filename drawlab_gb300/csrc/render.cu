@@ -688,6 +688,79 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
     if (out_counters) *out_counters = *hc;
 }
 
+// Li of explicit paths with every piece of path state in caller-provided
+// device memory (`pool`, laid out by fixed_pool_layout) and no allocation of
+// any kind: no cudaMalloc, no pinned staging (the counters are read back into
+// a stack copy), no exceptions.  Used by the allocation-free entry point.
+size_t fixed_pool_bytes(int64_t slots) {
+    size_t c = (size_t)slots;
+    return 7 * 16 * c + 8 * c + 3 * 4 * c + 3 * 16 * c + 256;
+}
+
+cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
+                            const int* d_xys, float* d_L, float* d_pos) {
+    dl_context* ctx = S->ctx;
+    cudaStream_t st = ctx->stream;
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.sc = S->dev;
+    P.mode = 1;
+    size_t c = (size_t)slots;
+    char* b = static_cast<char*>(pool);
+    P.cnt = reinterpret_cast<RenderCounters*>(b);
+    b += 256;
+    P.ray_o = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.ray_d = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.hit = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.tp = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.lacc = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.meta = reinterpret_cast<int4*>(b); b += 16 * c;
+    P.rng = reinterpret_cast<uint4*>(b); b += 16 * c;
+    P.sh_o = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.sh_d = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.sh_c = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.pos = reinterpret_cast<float2*>(b); b += 8 * c;
+    P.ext_q[0] = reinterpret_cast<int*>(b); b += 4 * c;
+    P.ext_q[1] = reinterpret_cast<int*>(b); b += 4 * c;
+    P.retire_q = reinterpret_cast<int*>(b);
+    filter_setup(o.filter, P.radius, P.border, P.lookup, P.filter);
+    P.film_cols = S->dev.cam.w + 2 * P.border;
+    P.film_rows = S->dev.cam.h + 2 * P.border;
+    P.xys = d_xys;
+    P.li_L = d_L;
+    P.li_pos = d_pos;
+    P.total_paths = (unsigned long long)li_n;
+    P.max_depth = o.max_depth;
+    P.rr_depth = o.rr_depth;
+    P.flags = o.flags;
+    P.seed_mix = splitmix64(o.seed);
+    int64_t cap = std::min<int64_t>(slots, ((li_n + 31) / 32) * 32);
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
+    cudaError_t e = cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st);
+    if (e != cudaSuccess) return e;
+    k_init<<<sms * 16, 128, 0, st>>>(P, (int)cap);
+    RenderCounters hc;
+    int64_t iters = 0;
+    for (;;) {
+        for (int k = 0; k < 4; k++) {
+            int p = (int)(iters & 1);
+            k_extend<false><<<sms * 16, 128, 0, st>>>(P, p);
+            k_shadow<false><<<sms * 16, 128, 0, st>>>(P, p);
+            k_retire<<<sms * 16, 128, 0, st>>>(P, p);
+            k_shade<<<sms * 16, 128, 0, st>>>(P, p);
+            iters++;
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        int p = (int)(iters & 1);
+        if (hc.err) return cudaErrorUnknown;
+        if (hc.ext[p] == 0 && hc.shadow[p] == 0 && hc.retire[p] == 0 && hc.next_path >= (unsigned long long)li_n) break;
+        if (iters > 1000000) return cudaErrorLaunchTimeout;
+    }
+    return cudaSuccess;
+}
+
 void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb) {
     const DevCamera& cam = S->dev.cam;
     int b = filter == DL_FILTER_BOX ? 0 : 2;

@@ -247,6 +247,20 @@ int dl_render_film_device(dl_scene* scene, const dl_render_opts* opts, float* d_
 int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
           const int32_t* xys, float* L_out, float* pos_out);
 
+/* Allocation-free form of dl_li, with no counterpart in the reference.  For
+ * callers that may not allocate device memory while rendering (a frame loop
+ * recorded into a CUDA graph, an engine that owns all device memory after
+ * start-up): the path state lives in one fixed array of 16384 path slots
+ * (2.9 MiB) compiled into the library, present on every GPU that loads it.
+ * d_xys (n x 3 int32), d_L (n x 3 float) and d_pos (n x 2 float) are device
+ * pointers supplied by the caller.  opts->max_paths_in_flight must be 0
+ * (whole pool) or at most 16384, else DL_ERR_INVALID_ARG.  The first call on
+ * a device resolves the array's address, so make it before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race.  Runs on the context stream and returns after the paths finish. */
+int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t n,
+                 const int32_t* d_xys, float* d_L, float* d_pos);
+
 /* --------------------------------------------------------------- statistics */
 
 typedef struct dl_stats {
