@@ -276,6 +276,7 @@ int dl_li(dl_scene* S, const dl_render_opts* opts, int64_t n, const int32_t* xys
     return guard(ctx, [&] {
         need(opts != nullptr, "opts is NULL");
         need(n >= 0 && (n == 0 || (xys && L_out)), "bad path buffers");
+        need(n < ((int64_t)1 << 31), "at most 2^31 - 1 paths per call");
         if (n == 0) return;
         const dl::DevCamera& cam = S->dev.cam;
         for (int64_t i = 0; i < n; i++)

@@ -409,8 +409,11 @@ __device__ __forceinline__ float3 square_to_ggx(float2 s, float ax, float ay) {
     return normalize(f3(-x, -y, 1.f));
 }
 
+// BSDF evaluation / density / sampling, specialised per material type T so
+// each material kernel carries only its own code.
+template <int T>
 __device__ __forceinline__ float3 bsdf_eval(const DevMaterial& m, const BRec& r) {
-    switch (m.type) {
+    switch (T) {
         case MAT_DIFFUSE:
             if (r.measure != M_SOLID || r.wi.z <= 0.f || r.wo.z <= 0.f) return f3(0.f, 0.f, 0.f);
             return scale(ld3(m.albedo), kInvPiF);
@@ -442,8 +445,9 @@ __device__ __forceinline__ float3 bsdf_eval(const DevMaterial& m, const BRec& r)
     }
 }
 
+template <int T>
 __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const BRec& r) {
-    switch (m.type) {
+    switch (T) {
         case MAT_DIFFUSE:
             if (r.measure != M_SOLID || r.wi.z <= 0.f || r.wo.z <= 0.f) return 0.f;
             return __fmul_rn(kInvPiF, r.wo.z);
@@ -467,9 +471,10 @@ __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const BRec& r) {
     }
 }
 
+template <int T>
 __device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, float2 s) {
     const float3 zero = f3(0.f, 0.f, 0.f);
-    switch (m.type) {
+    switch (T) {
         case MAT_DIFFUSE:
             if (r.wi.z <= 0.f) return zero;
             r.measure = M_SOLID;
@@ -509,7 +514,7 @@ __device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, flo
                 r.wo = reflect(r.wi, square_to_beckmann(ss, m.ax));
             }
             if (r.wo.z <= 0.f) return zero;
-            return divs(scale(bsdf_eval(m, r), r.wo.z), bsdf_pdf(m, r));
+            return divs(scale(bsdf_eval<T>(m, r), r.wo.z), bsdf_pdf<T>(m, r));
         }
         case MAT_ANISO_GGX: {
             if (r.wi.z <= 0.f) return zero;
@@ -523,7 +528,7 @@ __device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, flo
                 r.wo = reflect(r.wi, square_to_ggx(ss, m.ax, m.ay));
             }
             if (r.wo.z <= 0.f) return zero;
-            return divs(scale(bsdf_eval(m, r), r.wo.z), bsdf_pdf(m, r));
+            return divs(scale(bsdf_eval<T>(m, r), r.wo.z), bsdf_pdf<T>(m, r));
         }
         default:
             return zero;

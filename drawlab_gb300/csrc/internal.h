@@ -82,12 +82,15 @@ struct HostBuf {
     T* as() const { return static_cast<T*>(ptr); }
 };
 
+constexpr int kNumMaterialTypes = 5;
+
 // Device counters of one wavefront render (see render.cu).
 struct RenderCounters {
-    int ext[2];
-    int shadow[2];
-    int retire[2];
-    int pad[2];
+    int ext[2];       // extension-ray queue lengths (ping-pong)
+    int shadow[2];    // shadow-ray queue lengths
+    int mat[2][kNumMaterialTypes + 1];  // material-sorted hit queues + miss queue (ping-pong)
+    unsigned int work_ext;       // dynamic-fetch cursors of the traversal kernels
+    unsigned int work_sh;
     unsigned long long next_path;
     unsigned long long stat_ext;
     unsigned long long stat_shadow;
@@ -104,10 +107,11 @@ struct RenderCounters {
 // Wavefront path-state buffers, sized for the pool and reused across renders.
 struct RenderBuffers {
     int64_t capacity = 0;
-    DevBuf ray_o, ray_d, hit, tp, lacc, meta, rng, pos;
-    DevBuf ext_q[2], retire_q;
+    DevBuf ray, path, meta, hit, pos;   // 32-byte path records per slot (pos: Li mode)
+    DevBuf ext_q[2], mat_q[kNumMaterialTypes + 1];
     DevBuf sh_o, sh_d, sh_c;
-    DevBuf counters;
+    DevBuf counters, invalid;
+    DevBuf samples;   // per-path radiance of the current sample chunk (film gather input)
     DevBuf film;      // internal film when the caller gives no device film
     DevBuf rgb;       // resolved image
     DevBuf li_xys, li_out, li_pos;
@@ -135,8 +139,13 @@ struct dl_context {
     int num_sms = 0;
     bool kernel_timing = false;
     std::vector<cudaEvent_t> timing_events;  // created on first timed render
+    // CUDA graph of one batch of wavefront iterations, reused while the
+    // kernel parameters stay byte-identical.
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<unsigned char> graph_key;
     ~dl_context() {
         for (cudaEvent_t e : timing_events) cudaEventDestroy(e);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
     }
 };
 

@@ -9,8 +9,8 @@
 // fixed, file-scope device array.
 //
 // Limits and sharing:
-//  * the array holds kStaticPathSlots = 16384 path slots (180 bytes each,
-//    2.9 MiB in all) and lives on every GPU that loads the library until the
+//  * the array holds kStaticPathSlots = 16384 path slots (240 bytes each,
+//    3.75 MiB in all) and lives on every GPU that loads the library until the
 //    process exits;
 //  * requests with max_paths_in_flight above 16384 are rejected with
 //    DL_ERR_INVALID_ARG (0 means "use the whole pool"); the number of paths n
@@ -33,7 +33,7 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
                             const int* d_xys, float* d_L, float* d_pos);
 
 constexpr int64_t kStaticPathSlots = 16384;
-constexpr size_t kStaticPoolBytes = 180 * (size_t)kStaticPathSlots + 256;
+constexpr size_t kStaticPoolBytes = 240 * (size_t)kStaticPathSlots + 256;
 
 // The pool.  Host code must not use this name as an address: it is a host
 // stand-in for the device symbol.  Its device address comes from
@@ -70,7 +70,7 @@ extern "C" int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t
     if (!scene) return DL_ERR_INVALID_ARG;
     dl_context* ctx = scene->ctx;
     ctx->error.clear();
-    if (!opts || n < 0 || (n > 0 && (!d_xys || !d_L || !d_pos))) {
+    if (!opts || n < 0 || n >= ((int64_t)1 << 31) || (n > 0 && (!d_xys || !d_L || !d_pos))) {
         ctx->error = "dl_li_static: bad arguments";
         return DL_ERR_INVALID_ARG;
     }

@@ -3,23 +3,33 @@
 // The reference runs one path per thread/loop iteration (CPU:
 // PathIntegrator::Li, src/tracer/integrator/path.cpp:13-100; OptiX:
 // __raygen__path, src/optix/cuda/integrator/path.cu:28-97).  Here a fixed
-// pool of path slots advances one segment per iteration through four kernels:
+// pool of path slots advances one segment per iteration through:
 //
-//   extend  (queue E[p])  closest hit of every pending ray          -> hit[slot]
-//   shadow  (queue S)     any hit of last iteration's NEE rays      -> L[slot] += c
-//   retire  (queue R)     paths that ended with a shadow ray in flight: splat,
-//                         then start a new camera path in the slot  -> E[q]
-//   shade   (queue E[p])  emitter hit + MIS, Russian roulette, NEE (emits a
-//                         shadow ray), BSDF sample (emits the next ray) or
-//                         finish: splat + new camera path           -> E[q], S, R
+//   extend    persistent closest-hit traversal of queue E[p]; lanes whose ray
+//             finishes fetch the next one (per-lane replacement); each hit
+//             joins the queue of its material type, misses the miss queue
+//   shadow    same, any hit, for last iteration's NEE rays: the contribution
+//             goes to the path (or, if the path has ended, to its sample)
+//   miss      paths whose ray missed: store the sample, start a new camera
+//             path in the slot                                     -> E[q]
+//   material  one kernel per BSDF type (diffuse, mirror, dielectric,
+//             Beckmann microfacet, GGX): emitter hit + MIS, Russian roulette,
+//             NEE (emits a shadow ray), BSDF sampling (emits the next ray);
+//             a path that ends stores its sample and its slot starts a new
+//             camera path                                          -> E[q], S
+//   film      after the last path: gather every sample into the film
 //
-// Queues are compacted with warp ballots (one atomic per warp).  Every path
-// (x, y, s) owns a pcg32 stream and draws its numbers in the reference's order
-// (pixel 2D, aperture 2D, then per bounce NEE 2D, BSDF 2D, RR 1D), so each path
-// reproduces the oracle's path of the same (x, y, s).
+// Path state lives in 32-byte records (ray, path, meta+rng, hit), each read
+// and written whole: a full DRAM sector, no read-modify-write of partial
+// sectors.  Queues are compacted with warp ballots (one atomic per warp).  A
+// batch of iterations is captured once as a CUDA graph and replayed.  Every
+// path (x, y, s) owns a pcg32 stream and draws its numbers in the reference's
+// order (pixel 2D, aperture 2D, then per bounce NEE 2D, BSDF 2D, RR 1D), so
+// each path reproduces the oracle's path of the same (x, y, s).
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "device.cuh"
@@ -29,26 +39,42 @@ namespace dl {
 
 enum PathFlags { PF_CAMERA = 1, PF_PREV_DIFFUSE = 2 };
 
+struct __align__(32) RayRec {
+    float4 o;   // origin, tmin
+    float4 d;   // direction, tmax
+};
+struct __align__(32) PathRec {
+    float4 tp;  // throughput.rgb, eta
+    float4 L;   // radiance.rgb, pdf of the last BSDF sample
+};
+struct __align__(32) MetaRec {
+    int4 m;     // depth, flags, path index lo, path index hi
+    uint4 rng;  // pcg32 state lo/hi, inc lo/hi
+};
+struct __align__(32) HitRec {
+    float4 h;   // t, u, v, leaf-order triangle (int bits; -1 = miss)
+    float4 pad;
+};
+static_assert(sizeof(RayRec) == 32 && sizeof(PathRec) == 32 && sizeof(MetaRec) == 32 && sizeof(HitRec) == 32,
+              "path records are one 32-byte sector each");
+constexpr size_t kSlotBytes = 4 * 32 + 8 + 3 * 16 + 4 * (2 + kNumMaterialTypes + 1);  // records, pos, shadow, queues
+
+constexpr int kMissQueue = kNumMaterialTypes;  // queue index of rays that hit nothing
+
 struct RenderParams {
     DevScene sc;
-    float4* ray_o;   // o.xyz, tmin
-    float4* ray_d;   // d.xyz, tmax
-    float4* hit;     // t, u, v, leaf-order triangle (int bits; -1 = miss)
-    float4* tp;      // throughput.rgb, eta
-    float4* lacc;    // radiance.rgb, pdf of the last BSDF sample
-    int4* meta;      // depth, flags, path index lo, path index hi
-    uint4* rng;      // pcg32 state lo/hi, inc lo/hi
-    float2* pos;     // film position of the camera sample
+    RayRec* ray;
+    PathRec* path;
+    MetaRec* meta;
+    HitRec* hit;
+    float2* pos;     // film position of the camera sample (Li mode only)
     int* ext_q[2];
-    int* retire_q;
+    int* mat_q[kNumMaterialTypes + 1];  // per material type, then the miss queue
     float4* sh_o;
     float4* sh_d;
-    float4* sh_c;    // contribution.rgb, slot (int bits)
+    float4* sh_c;    // contribution.rgb, target: slot >= 0 (live path) or -1 - path index (ended path)
     RenderCounters* cnt;
-    float4* film;
-    int film_cols, film_rows, border;
-    float radius, lookup;
-    float filter[33];
+    float4* samples; // radiance.rgb + presence flag per path index of this chunk
     int mode;        // 0: film, 1: Li of explicit paths
     const int* xys;
     float* li_L;
@@ -94,6 +120,9 @@ __device__ __forceinline__ Pcg32 load_rng(const uint4& r) {
 __device__ __forceinline__ uint4 store_rng(const Pcg32& g) {
     return make_uint4((uint32_t)g.state, (uint32_t)(g.state >> 32), (uint32_t)g.inc, (uint32_t)(g.inc >> 32));
 }
+__device__ __forceinline__ unsigned long long path_index(const int4& m) {
+    return (unsigned long long)(unsigned)m.z | ((unsigned long long)(unsigned)m.w << 32);
+}
 
 // Start path `pid` in `slot`: camera sample and ray (cpu_renderer.cpp:36-44).
 __device__ void start_path(const RenderParams& P, int slot, unsigned long long pid) {
@@ -118,46 +147,25 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     (void)g.next2d();  // aperture sample: drawn, unused by the "virtual" camera
     float3 o, d;
     camera_ray(cam, ps, o, d);
-    P.ray_o[slot] = make_float4(o.x, o.y, o.z, kRayEps);
-    P.ray_d[slot] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
-    P.tp[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
-    P.lacc[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.meta[slot] = make_int4(0, PF_CAMERA, (int)(pid & 0xffffffffu), (int)(pid >> 32));
-    P.rng[slot] = store_rng(g);
-    P.pos[slot] = ps;
+    RayRec r;
+    r.o = make_float4(o.x, o.y, o.z, kRayEps);
+    r.d = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    P.ray[slot] = r;
+    PathRec pr;
+    pr.tp = make_float4(1.f, 1.f, 1.f, 1.f);
+    pr.L = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.path[slot] = pr;
+    MetaRec mr;
+    mr.m = make_int4(0, PF_CAMERA, (int)(pid & 0xffffffffu), (int)(pid >> 32));
+    mr.rng = store_rng(g);
+    P.meta[slot] = mr;
+    if (P.mode == 1) P.pos[slot] = ps;
 }
 
-// Film splat (ImageBlock::put, src/core/bitmap/block.cpp:81-113) with float
-// atomics into the whole-image film; invalid samples are dropped and counted.
-__device__ void splat(const RenderParams& P, float2 pos, float3 v) {
-    bool ok = v.x >= 0.f && v.y >= 0.f && v.z >= 0.f && isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
-    if (!ok) {
-        atomicAdd(&P.cnt->stat_invalid, 1ull);
-        return;
-    }
-    float px = __fsub_rn(__fsub_rn(pos.x, 0.5f), (float)(-P.border));
-    float py = __fsub_rn(__fsub_rn(pos.y, 0.5f), (float)(-P.border));
-    int x0 = max((int)ceilf(__fsub_rn(px, P.radius)), 0);
-    int y0 = max((int)ceilf(__fsub_rn(py, P.radius)), 0);
-    int x1 = min((int)floorf(__fadd_rn(px, P.radius)), P.film_cols - 1);
-    int y1 = min((int)floorf(__fadd_rn(py, P.radius)), P.film_rows - 1);
-    for (int y = y0; y <= y1; y++) {
-        float wy = P.filter[min((int)__fmul_rn(fabsf(__fsub_rn((float)y, py)), P.lookup), 32)];
-        for (int x = x0; x <= x1; x++) {
-            float wx = P.filter[min((int)__fmul_rn(fabsf(__fsub_rn((float)x, px)), P.lookup), 32)];
-            float4 c = make_float4(__fmul_rn(__fmul_rn(v.x, wx), wy), __fmul_rn(__fmul_rn(v.y, wx), wy),
-                                   __fmul_rn(__fmul_rn(v.z, wx), wy), __fmul_rn(wx, wy));
-            atomicAdd(&P.film[(size_t)y * P.film_cols + x], c);
-        }
-    }
-}
-
-// Path `slot` is complete: splat (or write its Li).
-__device__ void finish_path(const RenderParams& P, int slot) {
-    float4 L = P.lacc[slot];
+// Radiance of ended path `pid` (slot `slot`): into the sample buffer at its
+// path index (the film kernel gathers it), or as its Li.
+__device__ __forceinline__ void store_sample(const RenderParams& P, unsigned long long pid, float3 L, int slot) {
     if (P.mode == 1) {
-        int4 m = P.meta[slot];
-        unsigned long long pid = (unsigned long long)(unsigned)m.z | ((unsigned long long)(unsigned)m.w << 32);
         P.li_L[3 * pid] = L.x;
         P.li_L[3 * pid + 1] = L.y;
         P.li_L[3 * pid + 2] = L.z;
@@ -165,7 +173,20 @@ __device__ void finish_path(const RenderParams& P, int slot) {
         P.li_pos[2 * pid] = ps.x;
         P.li_pos[2 * pid + 1] = ps.y;
     } else {
-        splat(P, P.pos[slot], f3(L.x, L.y, L.z));
+        P.samples[pid] = make_float4(L.x, L.y, L.z, 1.f);
+    }
+}
+
+// A shadow ray of an ended path was unoccluded: add its contribution to the
+// stored sample.  One shadow ray per path at a time, so no atomics.
+__device__ __forceinline__ void add_to_sample(const RenderParams& P, unsigned long long pid, float4 c) {
+    if (P.mode == 1) {
+        P.li_L[3 * pid] = __fadd_rn(P.li_L[3 * pid], c.x);
+        P.li_L[3 * pid + 1] = __fadd_rn(P.li_L[3 * pid + 1], c.y);
+        P.li_L[3 * pid + 2] = __fadd_rn(P.li_L[3 * pid + 2], c.z);
+    } else {
+        float4 s = P.samples[pid];
+        P.samples[pid] = make_float4(__fadd_rn(s.x, c.x), __fadd_rn(s.y, c.y), __fadd_rn(s.z, c.z), s.w);
     }
 }
 
@@ -178,80 +199,6 @@ __device__ __forceinline__ bool regenerate(const RenderParams& P, int slot, bool
     unsigned mask = __ballot_sync(0xffffffffu, ok);
     if (mask && lane_id() == __ffs(mask) - 1) atomicAdd(&P.cnt->stat_camera, (unsigned long long)__popc(mask));
     return ok;
-}
-
-// ---------------------------------------------------------------- kernels
-__global__ void k_init(RenderParams P, int capacity) {
-    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < capacity;
-         i0 += gridDim.x * blockDim.x) {
-        int slot = i0 + lane_id();
-        bool active = slot < capacity;
-        bool ok = regenerate(P, slot, active);
-        int e = warp_push(&P.cnt->ext[0], ok);
-        if (ok) P.ext_q[0][e] = slot;
-    }
-}
-
-template <bool kCount>
-__global__ void __launch_bounds__(128) k_extend(RenderParams P, int p) {
-    int q = p ^ 1;
-    int n = P.cnt->ext[p];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        P.cnt->ext[q] = 0;
-        P.cnt->shadow[q] = 0;
-        P.cnt->retire[q] = 0;
-        P.cnt->stat_ext += (unsigned long long)n;
-    }
-    uint32_t err = 0, nn = 0, nt = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int slot = P.ext_q[p][i];
-        float4 o = P.ray_o[slot], d = P.ray_d[slot];
-        float t = 0.f, u = 0.f, v = 0.f;
-        int tri = trace_closest<kCount>(P.sc, xyz(o), xyz(d), o.w, d.w, t, u, v, err, nn, nt);
-        P.hit[slot] = make_float4(t, u, v, __int_as_float(tri));
-    }
-    if (err) atomicOr(&P.cnt->err, err);
-    if (kCount) {
-        atomicAdd(&P.cnt->stat_nodes_ext, (unsigned long long)nn);
-        atomicAdd(&P.cnt->stat_tris_ext, (unsigned long long)nt);
-    }
-}
-
-template <bool kCount>
-__global__ void __launch_bounds__(128) k_shadow(RenderParams P, int p) {
-    int n = P.cnt->shadow[p];
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->stat_shadow += (unsigned long long)n;
-    uint32_t err = 0, nn = 0, nt = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 o = P.sh_o[i], d = P.sh_d[i], c = P.sh_c[i];
-        if (!trace_any<kCount>(P.sc, xyz(o), xyz(d), o.w, d.w, err, nn, nt)) {
-            int slot = __float_as_int(c.w);
-            float4 L = P.lacc[slot];
-            L.x = __fadd_rn(L.x, c.x);
-            L.y = __fadd_rn(L.y, c.y);
-            L.z = __fadd_rn(L.z, c.z);
-            P.lacc[slot] = L;
-        }
-    }
-    if (err) atomicOr(&P.cnt->err, err);
-    if (kCount) {
-        atomicAdd(&P.cnt->stat_nodes_sh, (unsigned long long)nn);
-        atomicAdd(&P.cnt->stat_tris_sh, (unsigned long long)nt);
-    }
-}
-
-__global__ void k_retire(RenderParams P, int p) {
-    int q = p ^ 1;
-    int n = P.cnt->retire[p];
-    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
-        int i = i0 + lane_id();
-        bool active = i < n;
-        int slot = active ? P.retire_q[i] : 0;
-        if (active) finish_path(P, slot);
-        bool ok = regenerate(P, slot, active);
-        int e = warp_push(&P.cnt->ext[q], ok);
-        if (ok) P.ext_q[q][e] = slot;
-    }
 }
 
 struct HitInfo {
@@ -361,139 +308,478 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     return spec;
 }
 
-__global__ void __launch_bounds__(128) k_shade(RenderParams P, int p) {
+// ---------------------------------------------------------------- kernels
+__global__ void k_init(RenderParams P, int capacity) {
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < capacity;
+         i0 += gridDim.x * blockDim.x) {
+        int slot = i0 + lane_id();
+        bool active = slot < capacity;
+        bool ok = regenerate(P, slot, active);
+        int e = warp_push(&P.cnt->ext[0], ok);
+        if (ok) P.ext_q[0][e] = slot;
+    }
+}
+
+constexpr int kDone = kEmptyChild;  // traversal state: ray finished
+
+// Persistent traversal over a ray queue.  Each lane holds one ray's
+// traversal state (node, stack); a lane whose ray finishes takes the next ray
+// of the queue (one atomic per warp for all lanes that need one), so lanes do
+// not idle while the warp's longest ray finishes.
+//   kAny = false: closest hit of extension rays E[p] (slots) -> hit[slot], and
+//                 the slot joins the queue of its hit's material type (or the
+//                 miss queue): lanes with the same destination share one atomic
+//   kAny = true:  any hit of shadow rays S (queue positions); unoccluded ones
+//                 add their contribution to the path or the ended path's sample
+template <bool kCount, bool kAny>
+__global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     const int q = p ^ 1;
     const DevScene& sc = P.sc;
-    int n = P.cnt->ext[p];
+    const int n = kAny ? P.cnt->shadow[p] : P.cnt->ext[p];
+    unsigned int* work = kAny ? &P.cnt->work_sh : &P.cnt->work_ext;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!kAny) {
+            // this iteration's output queues start empty
+            P.cnt->ext[q] = 0;
+            P.cnt->shadow[q] = 0;
+            P.cnt->stat_ext += (unsigned long long)n;
+        } else {
+            // next iteration's material queues and extend cursor start empty
+            for (int k = 0; k <= kNumMaterialTypes; k++) P.cnt->mat[q][k] = 0;
+            P.cnt->work_ext = 0;
+            P.cnt->stat_shadow += (unsigned long long)n;
+        }
+    }
+    uint32_t err = 0, nn = 0, nt = 0;
+    bool has = false, exhausted = false;
+    int idx = 0, slot = 0, node = kDone, sp = 0, hit_tri = -1;
+    float3 o = f3(0.f, 0.f, 0.f), d = o;
+    float tmin = 0.f, tmax = 0.f, ht = 0.f, hu = 0.f, hv = 0.f;
+    RayBox rb;
+    rb.idir = o;
+    rb.ood = o;
+    int stack[kStackSize];
+    for (;;) {
+        bool need = !has && !exhausted;
+        unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            int leader = __ffs(m) - 1;
+            unsigned base = 0;
+            if (lane_id() == leader) base = atomicAdd(work, (unsigned)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                idx = (int)(base + __popc(m & ((1u << lane_id()) - 1u)));
+                if (idx < n) {
+                    float4 ro, rd;
+                    if (kAny) {
+                        ro = P.sh_o[idx];
+                        rd = P.sh_d[idx];
+                    } else {
+                        slot = P.ext_q[p][idx];
+                        RayRec r = P.ray[slot];
+                        ro = r.o;
+                        rd = r.d;
+                    }
+                    o = xyz(ro);
+                    d = xyz(rd);
+                    tmin = ro.w;
+                    tmax = rd.w;
+                    rb = make_raybox(o, d);
+                    node = sc.num_tris > 0 ? 0 : kDone;
+                    sp = 0;
+                    hit_tri = -1;
+                    has = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, has) == 0) break;
+        bool finished = false;
+        int dest = 0;
+        if (has) {
+            // descend inner nodes until a leaf (or the end of the traversal)
+            while (node >= 0 && node != kDone) {
+                const float4* np = sc.nodes + 4 * node;
+                float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+                int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
+                if (kCount) nn++;
+                bool h0, h1;
+                float t0, t1;
+                box2(rb, tmin, tmax, a, b, c, h0, h1, t0, t1);
+                h0 = h0 && ch.x != kEmptyChild;
+                h1 = h1 && ch.y != kEmptyChild;
+                if (h0 && h1) {
+                    int near = ch.x, far = ch.y;
+                    if (t1 < t0) { near = ch.y; far = ch.x; }
+                    if (sp < kStackSize) stack[sp++] = far; else err |= 1u;
+                    node = near;
+                } else if (h0) {
+                    node = ch.x;
+                } else if (h1) {
+                    node = ch.y;
+                } else {
+                    node = sp > 0 ? stack[--sp] : kDone;
+                }
+            }
+            finished = node == kDone;
+            if (!finished) {
+                // leaf: test its triangles (the reference's Moller-Trumbore)
+                int ref = ~node;
+                int first = ref >> 4, count = (ref & 15) + 1;
+                bool any = false;
+                for (int k = 0; k < count; k++) {
+                    const float4* tp = sc.tris + 3 * (first + k);
+                    float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                    if (kCount) nt++;
+                    float t, u, v;
+                    if (intersect_tri(xyz(p0), xyz(p1), xyz(p2), o, d, tmin, tmax, t, u, v)) {
+                        if (kAny) {
+                            any = true;
+                            break;
+                        }
+                        tmax = t;
+                        ht = t;
+                        hu = u;
+                        hv = v;
+                        hit_tri = first + k;
+                    }
+                }
+                if (kAny && any) {
+                    finished = true;
+                    hit_tri = 0;
+                } else {
+                    node = sp > 0 ? stack[--sp] : kDone;
+                    finished = node == kDone;
+                }
+            }
+            if (finished) {
+                if (kAny) {
+                    if (hit_tri < 0) {  // unoccluded: add the NEE contribution
+                        float4 c = P.sh_c[idx];
+                        int target = __float_as_int(c.w);
+                        if (target >= 0) {
+                            PathRec pr = P.path[target];
+                            pr.L = make_float4(__fadd_rn(pr.L.x, c.x), __fadd_rn(pr.L.y, c.y),
+                                               __fadd_rn(pr.L.z, c.z), pr.L.w);
+                            P.path[target] = pr;
+                        } else {
+                            add_to_sample(P, (unsigned long long)(unsigned)(-1 - target), c);
+                        }
+                    }
+                } else {
+                    HitRec hr;
+                    hr.pad = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (hit_tri >= 0) {
+                        hr.h = make_float4(ht, hu, hv, __int_as_float(hit_tri));
+                        int mesh = __ldg(sc.tri_vidx + hit_tri).w;
+                        dest = sc.materials[sc.meshes[mesh].material].type;
+                    } else {
+                        hr.h = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+                        dest = kMissQueue;
+                    }
+                    P.hit[slot] = hr;
+                }
+                has = false;
+            }
+        }
+        if (!kAny) {
+            unsigned fm = __ballot_sync(0xffffffffu, finished);
+            if (finished) {
+                unsigned peers = __match_any_sync(fm, dest);
+                int leader = __ffs(peers) - 1;
+                int base = 0;
+                if (lane_id() == leader) base = atomicAdd(&P.cnt->mat[p][dest], __popc(peers));
+                base = __shfl_sync(peers, base, leader);
+                P.mat_q[dest][base + __popc(peers & ((1u << lane_id()) - 1u))] = slot;
+            }
+        }
+    }
+    if (err) atomicOr(&P.cnt->err, err);
+    if (kCount) {
+        if (kAny) {
+            atomicAdd(&P.cnt->stat_nodes_sh, (unsigned long long)nn);
+            atomicAdd(&P.cnt->stat_tris_sh, (unsigned long long)nt);
+        } else {
+            atomicAdd(&P.cnt->stat_nodes_ext, (unsigned long long)nn);
+            atomicAdd(&P.cnt->stat_tris_ext, (unsigned long long)nt);
+        }
+    }
+}
+
+// Rays that hit nothing (path.cpp:23-25, 85-87): store the sample, then start
+// new camera paths in the freed slots.
+__global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
+    const int q = p ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
+    const int n = P.cnt->mat[p][kMissQueue];
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
         int i = i0 + lane_id();
         bool active = i < n;
-        int slot = active ? P.ext_q[p][i] : 0;
-        bool cont = false, emit_shadow = false, finish = false;
+        int slot = active ? P.mat_q[kMissQueue][i] : 0;
+        if (active) {
+            float4 L = P.path[slot].L;
+            unsigned long long pid = path_index(P.meta[slot].m);
+            store_sample(P, pid, make_float3(L.x, L.y, L.z), slot);
+        }
+        bool ok = regenerate(P, slot, active);
+        int e = warp_push(&P.cnt->ext[q], ok);
+        if (ok) P.ext_q[q][e] = slot;
+    }
+}
+
+// One BSDF type, the whole rest of the path iteration for hits on it:
+// emitter hit + MIS (path.cpp:72-84) or first-hit emission (27-29), Russian
+// roulette (89-97), depth limit, next-event estimation (36-56) and BSDF
+// sampling (60-69).  A path that ends here stores its sample and its slot
+// starts a new camera path at once; a shadow ray it emitted on the way adds
+// to the stored sample when traced.  Mirror and dielectric still draw the NEE
+// sample (their eval and pdf are zero: no contribution, no shadow ray).
+template <int T>
+__global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
+    const int q = p ^ 1;
+    const DevScene& sc = P.sc;
+    const int n = P.cnt->mat[p][T];
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
+        int i = i0 + lane_id();
+        bool active = i < n;
+        int slot = active ? P.mat_q[T][i] : 0;
+        bool cont = false, emit = false, done = false;
         float4 sh_o = make_float4(0.f, 0.f, 0.f, 0.f), sh_d = sh_o, sh_c = sh_o;
         if (active) {
-            float4 hit = P.hit[slot];
-            int tri = __float_as_int(hit.w);
-            float4 ro = P.ray_o[slot], rd = P.ray_d[slot];
-            float4 tpe = P.tp[slot];
-            float4 L = P.lacc[slot];
-            int4 meta = P.meta[slot];
-            float3 tp = f3(tpe.x, tpe.y, tpe.z);
-            float eta = tpe.w;
-            float3 Lr = f3(L.x, L.y, L.z);
-            float prev_pdf = L.w;
-            int depth = meta.x;
-            int flags = meta.y;
-            Pcg32 g = load_rng(P.rng[slot]);
-            bool done = false;
-            HitInfo h;
-            float3 dir = xyz(rd);
-            if (tri < 0) {
-                done = true;  // miss: path.cpp:23-25 / 85-87
+            float4 hit = P.hit[slot].h;
+            RayRec ray = P.ray[slot];
+            PathRec pr = P.path[slot];
+            MetaRec mr = P.meta[slot];
+            Pcg32 g = load_rng(mr.rng);
+            unsigned long long pid = path_index(mr.m);
+            float3 tp = f3(pr.tp.x, pr.tp.y, pr.tp.z);
+            float eta = pr.tp.w;
+            float3 Lr = f3(pr.L.x, pr.L.y, pr.L.z);
+            float3 dir = xyz(ray.d);
+            int depth = mr.m.x, flags = mr.m.y;
+            HitInfo h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
+            int light = sc.meshes[h.mesh].light;
+            if (flags & PF_CAMERA) {
+                if (light >= 0 && dot(h.sh.n, neg(dir)) > 0.f) Lr = add(Lr, mul(tp, ld3(sc.lights[light].radiance)));
+                depth = 0;
             } else {
-                h = hit_info(sc, tri, hit.y, hit.z);
-                int light = sc.meshes[h.mesh].light;
-                if (flags & PF_CAMERA) {
-                    if (light >= 0) {
-                        // first hit: emission without MIS (path.cpp:27-29)
-                        const DevLight& Lt = sc.lights[light];
-                        if (dot(h.sh.n, neg(dir)) > 0.f) Lr = add(Lr, mul(tp, ld3(Lt.radiance)));
-                    }
-                    depth = 0;
-                } else {
-                    if (light >= 0) {
-                        // BSDF-sampled ray hit an emitter (path.cpp:72-84)
-                        const DevLight& Lt = sc.lights[light];
-                        float3 le = dot(h.sh.n, neg(dir)) > 0.f ? ld3(Lt.radiance) : f3(0.f, 0.f, 0.f);
-                        float3 vec = sub(h.p, xyz(ro));
-                        float3 dd = normalize(vec);
-                        float dist = length(vec);
-                        float dp = fmaxf(dot(h.sh.n, neg(dd)), 0.f);
-                        float ep = dp != 0.f ? __fdiv_rn(__fmul_rn(__fmul_rn(Lt.pA, dist), dist), dp) : 0.f;
-                        if (sc.num_lights != 1) ep = __fdiv_rn(ep, (float)sc.num_lights);
-                        float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(prev_pdf, ep) : 1.f;
-                        Lr = add(Lr, mul(scale(tp, w), le));
-                    }
-                    // Russian roulette (path.cpp:89-97)
-                    if (depth > P.rr_depth) {
-                        float pr = fminf(maxc(scale(scale(tp, eta), eta)), 0.99f);
-                        if (g.next_float() > pr) done = true;
-                        else tp = divs(tp, pr);
-                    }
-                    depth += 1;
+                if (light >= 0) {
+                    const DevLight& Lt = sc.lights[light];
+                    float3 le = dot(h.sh.n, neg(dir)) > 0.f ? ld3(Lt.radiance) : f3(0.f, 0.f, 0.f);
+                    float3 vec = sub(h.p, xyz(ray.o));
+                    float3 dd = normalize(vec);
+                    float dist = length(vec);
+                    float dp = fmaxf(dot(h.sh.n, neg(dd)), 0.f);
+                    float ep = dp != 0.f ? __fdiv_rn(__fmul_rn(__fmul_rn(Lt.pA, dist), dist), dp) : 0.f;
+                    if (sc.num_lights != 1) ep = __fdiv_rn(ep, (float)sc.num_lights);
+                    float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(pr.L.w, ep) : 1.f;
+                    Lr = add(Lr, mul(scale(tp, w), le));
                 }
-                if (!done && P.max_depth > 0 && depth >= P.max_depth) done = true;
+                if (depth > P.rr_depth) {
+                    float pq = fminf(maxc(scale(scale(tp, eta), eta)), 0.99f);
+                    if (g.next_float() > pq) done = true;
+                    else tp = divs(tp, pq);
+                }
+                depth += 1;
             }
+            if (!done && P.max_depth > 0 && depth >= P.max_depth) done = true;
+            float prev_pdf = pr.L.w;
+            int target = slot;
             if (!done) {
                 const DevMaterial& m = sc.materials[sc.meshes[h.mesh].material];
-                bool aniso = m.type == MAT_ANISO_GGX;
-                Frame fr = aniso ? make_onb(normalize(h.sh.n)) : h.sh;
-                // ---- emitter sampling (path.cpp:36-56)
-                float2 s_nee = g.next2d();
-                float3 ld;
-                float ldist, lpdf;
-                bool delta;
-                float3 espec = sample_emitter(P, h.p, h.sh.n, s_nee, ld, ldist, lpdf, delta);
+                Frame fr = T == MAT_ANISO_GGX ? make_onb(normalize(h.sh.n)) : h.sh;
                 float3 wi = to_local(fr, neg(normalize(dir)));
-                if (aniso) wi = normalize(wi);
-                if (__fadd_rn(__fadd_rn(espec.x, espec.y), espec.z) > 0.f && lpdf > 0.f) {
-                    BRec q1;
-                    q1.wi = wi;
-                    q1.wo = to_local(fr, ld);
-                    q1.measure = M_SOLID;
-                    q1.eta = 1.f;
-                    float3 bv = bsdf_eval(m, q1);
-                    float bp = bsdf_pdf(m, q1);
-                    float w = (delta && (P.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
-                    float3 c = mul(mul(scale(tp, w), bv), espec);
-                    if (c.x != 0.f || c.y != 0.f || c.z != 0.f) {
-                        emit_shadow = true;
-                        sh_o = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
-                        sh_d = make_float4(ld.x, ld.y, ld.z, __fsub_rn(ldist, kRayEps));
-                        sh_c = make_float4(c.x, c.y, c.z, __int_as_float(slot));
+                if (T == MAT_ANISO_GGX) wi = normalize(wi);
+                float2 s_nee = g.next2d();
+                float3 c = f3(0.f, 0.f, 0.f);
+                float3 ld = c;
+                float ldist = 0.f;
+                if (T != MAT_MIRROR && T != MAT_DIELECTRIC) {
+                    float lpdf;
+                    bool delta;
+                    float3 espec = sample_emitter(P, h.p, h.sh.n, s_nee, ld, ldist, lpdf, delta);
+                    if (__fadd_rn(__fadd_rn(espec.x, espec.y), espec.z) > 0.f && lpdf > 0.f) {
+                        BRec q1;
+                        q1.wi = wi;
+                        q1.wo = to_local(fr, ld);
+                        q1.measure = M_SOLID;
+                        q1.eta = 1.f;
+                        float3 bv = bsdf_eval<T>(m, q1);
+                        float bp = bsdf_pdf<T>(m, q1);
+                        float w = (delta && (P.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
+                        c = mul(mul(scale(tp, w), bv), espec);
+                        emit = c.x != 0.f || c.y != 0.f || c.z != 0.f;
                     }
                 }
-                // ---- BSDF sampling (path.cpp:60-69)
                 BRec q2;
                 q2.wi = wi;
                 q2.wo = f3(0.f, 0.f, 0.f);
                 q2.eta = 1.f;
                 q2.measure = M_UNKNOWN;
-                float3 f = bsdf_sample(m, q2, g.next2d());
+                float3 f = bsdf_sample<T>(m, q2, g.next2d());
                 tp = mul(tp, f);
                 eta = __fmul_rn(eta, q2.eta);
-                prev_pdf = bsdf_pdf(m, q2);
-                flags = is_diffuse(m.type) ? PF_PREV_DIFFUSE : 0;
+                prev_pdf = bsdf_pdf<T>(m, q2);
+                flags = is_diffuse(T) ? PF_PREV_DIFFUSE : 0;
                 float3 nd = to_world(fr, q2.wo);
-                if (aniso) nd = normalize(nd);
+                if (T == MAT_ANISO_GGX) nd = normalize(nd);
                 if (tp.x == 0.f && tp.y == 0.f && tp.z == 0.f) {
                     done = true;  // every later contribution is zero
                 } else {
-                    P.ray_o[slot] = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
-                    P.ray_d[slot] = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
+                    RayRec nr;
+                    nr.o = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
+                    nr.d = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
+                    P.ray[slot] = nr;
                     cont = true;
                 }
+                if (emit) {
+                    if (done) target = -1 - (int)pid;  // lands in the stored sample
+                    sh_o = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
+                    sh_d = make_float4(ld.x, ld.y, ld.z, __fsub_rn(ldist, kRayEps));
+                    sh_c = make_float4(c.x, c.y, c.z, __int_as_float(target));
+                }
             }
-            P.tp[slot] = make_float4(tp.x, tp.y, tp.z, eta);
-            P.lacc[slot] = make_float4(Lr.x, Lr.y, Lr.z, prev_pdf);
-            P.meta[slot] = make_int4(depth, flags, meta.z, meta.w);
-            P.rng[slot] = store_rng(g);
-            finish = done && !emit_shadow;
+            if (done) {
+                store_sample(P, pid, Lr, slot);
+            } else {
+                PathRec npr;
+                npr.tp = make_float4(tp.x, tp.y, tp.z, eta);
+                npr.L = make_float4(Lr.x, Lr.y, Lr.z, prev_pdf);
+                P.path[slot] = npr;
+                MetaRec nmr;
+                nmr.m = make_int4(depth, flags, mr.m.z, mr.m.w);
+                nmr.rng = store_rng(g);
+                P.meta[slot] = nmr;
+            }
         }
-        bool retire = active && !cont && emit_shadow;
-        int sp = warp_push(&P.cnt->shadow[q], emit_shadow);
-        if (emit_shadow) {
+        int sp = warp_push(&P.cnt->shadow[q], emit);
+        if (emit) {
             P.sh_o[sp] = sh_o;
             P.sh_d[sp] = sh_d;
             P.sh_c[sp] = sh_c;
         }
-        int rp = warp_push(&P.cnt->retire[q], retire);
-        if (retire) P.retire_q[rp] = slot;
-        if (finish) finish_path(P, slot);
-        bool fresh = regenerate(P, slot, finish);
+        bool fresh = regenerate(P, slot, done);
         bool push = cont || fresh;
         int e = warp_push(&P.cnt->ext[q], push);
         if (push) P.ext_q[q][e] = slot;
+    }
+}
+
+// Film accumulation as a gather (the reference splats each sample with
+// ImageBlock::put, src/core/bitmap/block.cpp:81-113).  One block owns a
+// 16x16 tile of film pixels; it stages the samples of the 20x20 image pixels
+// around it (radiance from the sample buffer, film position recomputed from
+// the path's pcg32 stream: its first 2D draw) in shared memory together with
+// their 5 x and 5 y filter weights (the reference's table lookup), then every
+// thread sums the weighted samples of its 5x5 neighbourhood in a fixed order:
+// no atomics, bit-reproducible films.  Samples the film rejects (NaN, Inf or
+// negative: ImageBlock::put block.cpp:82-88) get zero weight and are counted.
+constexpr int kFilmTile = 16, kFilmApron = 2, kFilmRegion = kFilmTile + 2 * kFilmApron, kFilmStage = 2;
+constexpr int kFilmCells = kFilmRegion * kFilmRegion;
+
+struct FilmParams {
+    float4* film;
+    const float4* samples;
+    unsigned long long* invalid;
+    int w, h, cols, rows, border;
+    float lookup;
+    float table[33];
+    int nspp;             // samples per pixel in the sample buffer
+    int s_first;          // sample index of the buffer's first sample
+    unsigned long long seed_mix;
+    int accumulate;       // add to the film instead of overwriting it
+};
+
+__global__ void __launch_bounds__(256) k_film_gather(FilmParams F) {
+    constexpr int kTaps = 2 * kFilmApron + 1;  // 5 film pixels per axis around a sample
+    constexpr int kN = kFilmStage * kFilmCells;
+    __shared__ float s_r[kN], s_g[kN], s_b[kN];
+    __shared__ float s_wx[kTaps][kN], s_wy[kTaps][kN];
+    __shared__ float s_table[33];
+    __shared__ unsigned int s_invalid;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int X0 = blockIdx.x * kFilmTile, Y0 = blockIdx.y * kFilmTile;
+    const int X = X0 + tx, Y = Y0 + ty;
+    const int IX0 = X0 - F.border - kFilmApron, IY0 = Y0 - F.border - kFilmApron;
+    const size_t npix = (size_t)F.w * F.h;
+    if (threadIdx.x < 33) s_table[threadIdx.x] = F.table[threadIdx.x];
+    if (threadIdx.x == 0) s_invalid = 0;
+    __syncthreads();
+    float ar = 0.f, ag = 0.f, ab = 0.f, aw = 0.f;
+    for (int k0 = 0; k0 < F.nspp; k0 += kFilmStage) {
+        for (int e = threadIdx.x; e < kN; e += blockDim.x) {
+            int kk = e / kFilmCells, r = e - kk * kFilmCells;
+            int rx = r % kFilmRegion, ry = r / kFilmRegion;
+            int sx = IX0 + rx, sy = IY0 + ry;
+            float L0 = 0.f, L1 = 0.f, L2 = 0.f;
+            bool ok = false;
+            float px = 0.f, py = 0.f;
+            if (k0 + kk < F.nspp && sx >= 0 && sx < F.w && sy >= 0 && sy < F.h) {
+                float4 L = F.samples[(size_t)(k0 + kk) * npix + (size_t)sy * F.w + sx];
+                ok = L.w != 0.f && L.x >= 0.f && L.y >= 0.f && L.z >= 0.f && isfinite(L.x) && isfinite(L.y) &&
+                     isfinite(L.z);
+                // each sample is counted by the tile that owns its pixel
+                if (!ok && L.w != 0.f && rx >= kFilmApron && rx < kFilmApron + kFilmTile && ry >= kFilmApron &&
+                    ry < kFilmApron + kFilmTile)
+                    atomicAdd(&s_invalid, 1u);
+                if (ok) {
+                    Pcg32 g;
+                    seed_path(g, F.seed_mix, F.w, F.h, sx, sy, F.s_first + k0 + kk);
+                    float2 ps = g.next2d();
+                    float fx = __fadd_rn((float)sx, ps.x), fy = __fadd_rn((float)sy, ps.y);
+                    px = __fsub_rn(__fsub_rn(fx, 0.5f), (float)(-F.border));
+                    py = __fsub_rn(__fsub_rn(fy, 0.5f), (float)(-F.border));
+                    L0 = L.x;
+                    L1 = L.y;
+                    L2 = L.z;
+                }
+            }
+            s_r[e] = L0;
+            s_g[e] = L1;
+            s_b[e] = L2;
+            // weights of this sample for film columns X0 + rx - d and rows Y0 + ry - d
+#pragma unroll
+            for (int d = 0; d < kTaps; d++) {
+                int cx = X0 + rx - d, cy = Y0 + ry - d;
+                float wx = 0.f, wy = 0.f;
+                if (ok && cx >= 0 && cx < F.cols)
+                    wx = s_table[min((int)__fmul_rn(fabsf(__fsub_rn((float)cx, px)), F.lookup), 32)];
+                if (ok && cy >= 0 && cy < F.rows)
+                    wy = s_table[min((int)__fmul_rn(fabsf(__fsub_rn((float)cy, py)), F.lookup), 32)];
+                s_wx[d][e] = wx;
+                s_wy[d][e] = wy;
+            }
+        }
+        __syncthreads();
+        if (X < F.cols && Y < F.rows) {
+            for (int kk = 0; kk < kFilmStage; kk++) {
+                const int base = kk * kFilmCells;
+#pragma unroll
+                for (int dy = 0; dy < kTaps; dy++) {
+#pragma unroll
+                    for (int dx = 0; dx < kTaps; dx++) {
+                        int c = base + (ty + dy) * kFilmRegion + (tx + dx);
+                        float wx = s_wx[dx][c], wy = s_wy[dy][c];
+                        ar = __fadd_rn(ar, __fmul_rn(__fmul_rn(s_r[c], wx), wy));
+                        ag = __fadd_rn(ag, __fmul_rn(__fmul_rn(s_g[c], wx), wy));
+                        ab = __fadd_rn(ab, __fmul_rn(__fmul_rn(s_b[c], wx), wy));
+                        aw = __fadd_rn(aw, __fmul_rn(wx, wy));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && s_invalid) atomicAdd(F.invalid, (unsigned long long)s_invalid);
+    if (X < F.cols && Y < F.rows) {
+        float4* o = F.film + (size_t)Y * F.cols + X;
+        if (F.accumulate) {
+            float4 c = *o;
+            *o = make_float4(__fadd_rn(c.x, ar), __fadd_rn(c.y, ag), __fadd_rn(c.z, ab), __fadd_rn(c.w, aw));
+        } else {
+            *o = make_float4(ar, ag, ab, aw);
+        }
     }
 }
 
@@ -518,29 +804,61 @@ __global__ void k_resolve(const float4* film, int cols, int border, int w, int h
 void RenderBuffers::ensure(int64_t cap) {
     if (cap <= capacity) return;
     size_t c = (size_t)cap;
-    ray_o.ensure(16 * c);
-    ray_d.ensure(16 * c);
-    hit.ensure(16 * c);
-    tp.ensure(16 * c);
-    lacc.ensure(16 * c);
-    meta.ensure(16 * c);
-    rng.ensure(16 * c);
+    for (DevBuf* b : {&ray, &path, &meta, &hit}) b->ensure(32 * c);
     pos.ensure(8 * c);
-    ext_q[0].ensure(4 * c);
-    ext_q[1].ensure(4 * c);
-    retire_q.ensure(4 * c);
-    sh_o.ensure(16 * c);
-    sh_d.ensure(16 * c);
-    sh_c.ensure(16 * c);
+    for (DevBuf* b : {&sh_o, &sh_d, &sh_c}) b->ensure(16 * c);
+    for (DevBuf* b : {&ext_q[0], &ext_q[1]}) b->ensure(4 * c);
+    for (int k = 0; k <= kNumMaterialTypes; k++) mat_q[k].ensure(4 * c);
     counters.ensure(sizeof(RenderCounters));
-    host_counters.ensure(sizeof(RenderCounters));
+    invalid.ensure(sizeof(unsigned long long));
+    host_counters.ensure(sizeof(RenderCounters) + sizeof(unsigned long long));
     capacity = cap;
 }
 
 size_t RenderBuffers::device_bytes() const {
-    return ray_o.bytes + ray_d.bytes + hit.bytes + tp.bytes + lacc.bytes + meta.bytes + rng.bytes +
-           pos.bytes + ext_q[0].bytes + ext_q[1].bytes + retire_q.bytes + sh_o.bytes + sh_d.bytes +
-           sh_c.bytes + counters.bytes + film.bytes + rgb.bytes;
+    size_t s = ray.bytes + path.bytes + meta.bytes + hit.bytes + pos.bytes + ext_q[0].bytes + ext_q[1].bytes +
+               sh_o.bytes + sh_d.bytes + sh_c.bytes + counters.bytes + film.bytes + rgb.bytes + samples.bytes;
+    for (int k = 0; k <= kNumMaterialTypes; k++) s += mat_q[k].bytes;
+    return s;
+}
+
+constexpr int kBatch = 4;  // iterations per counter check and per captured graph (even)
+constexpr int kKernelsPerIteration = 8;
+
+// Launches one wavefront iteration (8 kernels).  `ev`, when given, holds 8
+// events bracketing extend, shadow, the material kernels, miss.
+static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, bool count, cudaEvent_t* ev) {
+    const int tb = sms * 8, wb = sms * 16, th = 128;
+    if (ev) cudaEventRecord(ev[0], st);
+    if (count) k_traverse<true, false><<<tb, th, 0, st>>>(P, p);
+    else k_traverse<false, false><<<tb, th, 0, st>>>(P, p);
+    if (ev) { cudaEventRecord(ev[1], st); cudaEventRecord(ev[2], st); }
+    if (count) k_traverse<true, true><<<tb, th, 0, st>>>(P, p);
+    else k_traverse<false, true><<<tb, th, 0, st>>>(P, p);
+    if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[6], st); }
+    k_miss<<<wb, th, 0, st>>>(P, p);
+    if (ev) { cudaEventRecord(ev[7], st); cudaEventRecord(ev[4], st); }
+    k_material<MAT_DIFFUSE><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_MIRROR><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_DIELECTRIC><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_MICROFACET><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_ANISO_GGX><<<wb, th, 0, st>>>(P, p);
+    if (ev) cudaEventRecord(ev[5], st);
+}
+
+static void bind_pool(RenderParams& P, const RenderBuffers& B) {
+    P.ray = B.ray.as<RayRec>();
+    P.path = B.path.as<PathRec>();
+    P.meta = B.meta.as<MetaRec>();
+    P.hit = B.hit.as<HitRec>();
+    P.pos = B.pos.as<float2>();
+    P.ext_q[0] = B.ext_q[0].as<int>();
+    P.ext_q[1] = B.ext_q[1].as<int>();
+    for (int k = 0; k <= kNumMaterialTypes; k++) P.mat_q[k] = B.mat_q[k].as<int>();
+    P.sh_o = B.sh_o.as<float4>();
+    P.sh_d = B.sh_d.as<float4>();
+    P.sh_c = B.sh_c.as<float4>();
+    P.cnt = B.counters.as<RenderCounters>();
 }
 
 void filter_setup(int filter, float& radius, int& border, float& lookup, float* table) {
@@ -566,98 +884,71 @@ int64_t film_floats(int w, int h, int filter) {
     return (int64_t)(w + 2 * b) * (h + 2 * b) * 4;
 }
 
-// Runs one render.  mode 0: splat into d_film (zeroed here); mode 1: Li of
-// li_n explicit paths (d_xys -> d_L, d_pos).
-void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys,
-                float* d_L, float* d_pos, bool count_traversal, RenderCounters* out_counters) {
-    dl_context* ctx = S->ctx;
-    cudaStream_t st = ctx->stream;
-    const DevCamera& cam = S->dev.cam;
-    RenderParams P;
-    std::memset(&P, 0, sizeof(P));
+static void common_params(RenderParams& P, dl_scene* S, const dl_render_opts& o) {
     P.sc = S->dev;
-    P.mode = li_n > 0 ? 1 : 0;
-    unsigned long long total =
-        P.mode == 1 ? (unsigned long long)li_n : (unsigned long long)cam.w * cam.h * (unsigned long long)std::max(o.spp, 0);
-    int64_t cap = o.max_paths_in_flight > 0 ? o.max_paths_in_flight : (int64_t)1 << 22;
-    cap = std::min<int64_t>(cap, (int64_t)std::max<unsigned long long>(total, 1ull));
-    cap = ((cap + 31) / 32) * 32;
-    RenderBuffers& B = ctx->render;
-    B.ensure(cap);
-    P.ray_o = B.ray_o.as<float4>();
-    P.ray_d = B.ray_d.as<float4>();
-    P.hit = B.hit.as<float4>();
-    P.tp = B.tp.as<float4>();
-    P.lacc = B.lacc.as<float4>();
-    P.meta = B.meta.as<int4>();
-    P.rng = B.rng.as<uint4>();
-    P.pos = B.pos.as<float2>();
-    P.ext_q[0] = B.ext_q[0].as<int>();
-    P.ext_q[1] = B.ext_q[1].as<int>();
-    P.retire_q = B.retire_q.as<int>();
-    P.sh_o = B.sh_o.as<float4>();
-    P.sh_d = B.sh_d.as<float4>();
-    P.sh_c = B.sh_c.as<float4>();
-    P.cnt = B.counters.as<RenderCounters>();
-    filter_setup(o.filter, P.radius, P.border, P.lookup, P.filter);
-    P.film_cols = cam.w + 2 * P.border;
-    P.film_rows = cam.h + 2 * P.border;
-    P.film = reinterpret_cast<float4*>(d_film);
-    P.xys = d_xys;
-    P.li_L = d_L;
-    P.li_pos = d_pos;
-    P.total_paths = total;
     P.spp_offset = o.spp_offset;
     P.max_depth = o.max_depth;
     P.rr_depth = o.rr_depth;
     P.flags = o.flags;
     P.seed_mix = splitmix64(o.seed);
+}
 
-    if (P.mode == 0) DL_CUDA(cudaMemsetAsync(d_film, 0, sizeof(float) * film_floats(cam.w, cam.h, o.filter), st));
+// Wavefront loop over the paths [0, P.total_paths) of one chunk, until every
+// path and every shadow ray has finished.  Adds the chunk's counters into
+// `acc` and per-kernel times into kms.
+static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool count_traversal, double* kms,
+                          int64_t& launches, int64_t& iters, RenderCounters& acc) {
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& B = ctx->render;
+    const unsigned long long total = P.total_paths;
     DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
-    const int trace_blocks = sms * 16, trace_threads = 128;
-    const int work_blocks = sms * 16, work_threads = 128;
-    // Optional per-kernel timing: one event pair per launch, four kernels per
-    // iteration, read back at every counter check.
-    const int check_every = 4;
     const bool timing = ctx->kernel_timing;
+    const bool use_graph = !timing && !count_traversal;
     if (timing && ctx->timing_events.empty()) {
-        ctx->timing_events.resize(2 * 4 * check_every);
+        ctx->timing_events.resize(8 * kBatch);
         for (auto& e : ctx->timing_events) DL_CUDA(cudaEventCreate(&e));
     }
-    double kms[4] = {0, 0, 0, 0};
-    int64_t launches = 1;
-    DL_CUDA(cudaEventRecord(ctx->ev0, st));
-    k_init<<<work_blocks, work_threads, 0, st>>>(P, (int)cap);
-    RenderCounters* hc = B.host_counters.as<RenderCounters>();
-    int64_t iters = 0;
-    for (;;) {
-        for (int k = 0; k < check_every; k++) {
-            int p = (int)(iters & 1);
-            cudaEvent_t* ev = timing ? &ctx->timing_events[8 * k] : nullptr;
-            if (timing) DL_CUDA(cudaEventRecord(ev[0], st));
-            if (count_traversal) k_extend<true><<<trace_blocks, trace_threads, 0, st>>>(P, p);
-            else k_extend<false><<<trace_blocks, trace_threads, 0, st>>>(P, p);
-            if (timing) DL_CUDA(cudaEventRecord(ev[1], st));
-            if (timing) DL_CUDA(cudaEventRecord(ev[2], st));
-            if (count_traversal) k_shadow<true><<<trace_blocks, trace_threads, 0, st>>>(P, p);
-            else k_shadow<false><<<trace_blocks, trace_threads, 0, st>>>(P, p);
-            if (timing) DL_CUDA(cudaEventRecord(ev[3], st));
-            if (timing) DL_CUDA(cudaEventRecord(ev[4], st));
-            k_retire<<<work_blocks, work_threads, 0, st>>>(P, p);
-            if (timing) DL_CUDA(cudaEventRecord(ev[5], st));
-            if (timing) DL_CUDA(cudaEventRecord(ev[6], st));
-            k_shade<<<work_blocks, work_threads, 0, st>>>(P, p);
-            if (timing) DL_CUDA(cudaEventRecord(ev[7], st));
-            iters++;
-            launches += 4;
+    if (use_graph) {
+        std::vector<unsigned char> key(sizeof(P) + sizeof(int) + sizeof(cudaStream_t));
+        std::memcpy(key.data(), &P, sizeof(P));
+        std::memcpy(key.data() + sizeof(P), &sms, sizeof(int));
+        std::memcpy(key.data() + sizeof(P) + sizeof(int), &st, sizeof(cudaStream_t));
+        if (!ctx->graph_exec || key != ctx->graph_key) {
+            if (ctx->graph_exec) {
+                cudaGraphExecDestroy(ctx->graph_exec);
+                ctx->graph_exec = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            DL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr);
+            DL_CUDA(cudaStreamEndCapture(st, &g));
+            cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                ctx->graph_exec = nullptr;
+                throw Error(DL_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+            }
+            ctx->graph_key = key;
         }
+    }
+    k_init<<<sms * 16, 128, 0, st>>>(P, (int)cap);
+    launches += 1;
+    RenderCounters* hc = B.host_counters.as<RenderCounters>();
+    for (;;) {
+        if (use_graph) {
+            DL_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
+        } else {
+            for (int k = 0; k < kBatch; k++)
+                launch_iteration(P, k & 1, st, sms, count_traversal, timing ? &ctx->timing_events[8 * k] : nullptr);
+        }
+        iters += kBatch;
+        launches += kBatch * kKernelsPerIteration;
         DL_CUDA(cudaGetLastError());
         DL_CUDA(cudaMemcpyAsync(hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st));
         DL_CUDA(cudaStreamSynchronize(st));
         if (timing) {
-            for (int k = 0; k < check_every; k++)
+            for (int k = 0; k < kBatch; k++)
                 for (int j = 0; j < 4; j++) {
                     float ms = 0.f;
                     DL_CUDA(cudaEventElapsedTime(&ms, ctx->timing_events[8 * k + 2 * j],
@@ -665,37 +956,117 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
                     kms[j] += ms;
                 }
         }
-        int p = (int)(iters & 1);
         if (hc->err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
-        if (hc->ext[p] == 0 && hc->shadow[p] == 0 && hc->retire[p] == 0 && hc->next_path >= total) break;
+        if (hc->ext[0] == 0 && hc->shadow[0] == 0 && hc->next_path >= total) break;
         if (iters > 1000000) throw Error(DL_ERR_TIMEOUT, "render did not converge");
     }
-    ctx->stats.extend_ms = kms[0];
-    ctx->stats.shadow_ms = kms[1];
-    ctx->stats.retire_ms = kms[2];
-    ctx->stats.shade_ms = kms[3];
-    ctx->stats.kernel_launches = launches;
+    acc.stat_camera += hc->stat_camera;
+    acc.stat_ext += hc->stat_ext;
+    acc.stat_shadow += hc->stat_shadow;
+    acc.stat_nodes_ext += hc->stat_nodes_ext;
+    acc.stat_tris_ext += hc->stat_tris_ext;
+    acc.stat_nodes_sh += hc->stat_nodes_sh;
+    acc.stat_tris_sh += hc->stat_tris_sh;
+}
+
+// Budget of the per-path sample buffer; larger frames render in chunks of
+// whole samples per pixel.
+constexpr size_t kSampleBufferBytes = (size_t)4 << 30;
+
+// Runs one render.  mode 0: the film (d_film) receives every sample through
+// the gather kernel; mode 1: Li of li_n explicit paths (d_xys -> d_L, d_pos).
+void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys,
+                float* d_L, float* d_pos, bool count_traversal, RenderCounters* out_counters) {
+    dl_context* ctx = S->ctx;
+    cudaStream_t st = ctx->stream;
+    const DevCamera& cam = S->dev.cam;
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    common_params(P, S, o);
+    P.mode = li_n > 0 ? 1 : 0;
+    const unsigned long long npix = (unsigned long long)cam.w * cam.h;
+    const int spp = std::max(o.spp, 1);
+    int chunk_spp = P.mode == 1 ? 1 : (int)std::max<size_t>(1, std::min<size_t>(spp, kSampleBufferBytes / (npix * 16)));
+    unsigned long long chunk_total = P.mode == 1 ? (unsigned long long)li_n : npix * (unsigned long long)chunk_spp;
+    int64_t cap = o.max_paths_in_flight > 0 ? o.max_paths_in_flight : (int64_t)1 << 22;
+    cap = std::min<int64_t>(cap, (int64_t)std::max<unsigned long long>(chunk_total, 1ull));
+    cap = ((cap + 31) / 32) * 32;
+    RenderBuffers& B = ctx->render;
+    B.ensure(cap);
+    bind_pool(P, B);
+    P.xys = d_xys;
+    P.li_L = d_L;
+    P.li_pos = d_pos;
+    if (P.mode == 0) {
+        B.samples.ensure((size_t)chunk_total * 16);
+        P.samples = B.samples.as<float4>();
+    }
+    double kms[4] = {0, 0, 0, 0};
+    int64_t launches = 0, iters = 0;
+    RenderCounters acc;
+    std::memset(&acc, 0, sizeof(acc));
+    DL_CUDA(cudaEventRecord(ctx->ev0, st));
+    unsigned long long invalid = 0;
+    if (P.mode == 1) {
+        P.total_paths = (unsigned long long)li_n;
+        run_wavefront(ctx, P, cap, count_traversal, kms, launches, iters, acc);
+    } else {
+        FilmParams F;
+        std::memset(&F, 0, sizeof(F));
+        float radius;
+        filter_setup(o.filter, radius, F.border, F.lookup, F.table);
+        F.film = reinterpret_cast<float4*>(d_film);
+        F.samples = P.samples;
+        F.invalid = B.invalid.as<unsigned long long>();
+        F.w = cam.w;
+        F.h = cam.h;
+        F.cols = cam.w + 2 * F.border;
+        F.rows = cam.h + 2 * F.border;
+        F.seed_mix = P.seed_mix;
+        DL_CUDA(cudaMemsetAsync(F.invalid, 0, sizeof(unsigned long long), st));
+        dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
+        for (int s0 = 0; s0 < spp; s0 += chunk_spp) {
+            int ns = std::min(chunk_spp, spp - s0);
+            P.spp_offset = o.spp_offset + s0;
+            P.total_paths = npix * (unsigned long long)ns;
+            run_wavefront(ctx, P, cap, count_traversal, kms, launches, iters, acc);
+            F.nspp = ns;
+            F.s_first = o.spp_offset + s0;
+            F.accumulate = s0 > 0;
+            k_film_gather<<<fgrid, 256, 0, st>>>(F);
+            launches += 1;
+            DL_CUDA(cudaGetLastError());
+        }
+        unsigned long long* hinv =
+            reinterpret_cast<unsigned long long*>(B.host_counters.as<char>() + sizeof(RenderCounters));
+        DL_CUDA(cudaMemcpyAsync(hinv, F.invalid, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        DL_CUDA(cudaStreamSynchronize(st));
+        invalid = *hinv;
+    }
     DL_CUDA(cudaEventRecord(ctx->ev1, st));
     DL_CUDA(cudaEventSynchronize(ctx->ev1));
     float ms = 0.f;
     DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->stats.camera_rays = (int64_t)hc->stat_camera;
-    ctx->stats.extension_rays = (int64_t)hc->stat_ext;
-    ctx->stats.shadow_rays = (int64_t)hc->stat_shadow;
-    ctx->stats.invalid_samples = (int64_t)hc->stat_invalid;
+    acc.stat_invalid = invalid;
+    ctx->stats.camera_rays = (int64_t)acc.stat_camera;
+    ctx->stats.extension_rays = (int64_t)acc.stat_ext;
+    ctx->stats.shadow_rays = (int64_t)acc.stat_shadow;
+    ctx->stats.invalid_samples = (int64_t)invalid;
     ctx->stats.iterations = iters;
     ctx->stats.render_ms = ms;
-    if (out_counters) *out_counters = *hc;
+    ctx->stats.extend_ms = kms[0];
+    ctx->stats.shadow_ms = kms[1];
+    ctx->stats.shade_ms = kms[2];
+    ctx->stats.retire_ms = kms[3];
+    ctx->stats.kernel_launches = launches;
+    if (out_counters) *out_counters = acc;
 }
 
 // Li of explicit paths with every piece of path state in caller-provided
-// device memory (`pool`, laid out by fixed_pool_layout) and no allocation of
-// any kind: no cudaMalloc, no pinned staging (the counters are read back into
-// a stack copy), no exceptions.  Used by the allocation-free entry point.
-size_t fixed_pool_bytes(int64_t slots) {
-    size_t c = (size_t)slots;
-    return 7 * 16 * c + 8 * c + 3 * 4 * c + 3 * 16 * c + 256;
-}
+// device memory (`pool`, laid out below) and no allocation of any kind: no
+// cudaMalloc, no pinned staging (the counters are read back into a stack
+// copy), no exceptions, no graph.  Used by the allocation-free entry point.
+size_t fixed_pool_bytes(int64_t slots) { return kSlotBytes * (size_t)slots + 256; }
 
 cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
                             const int* d_xys, float* d_L, float* d_pos) {
@@ -703,37 +1074,32 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     cudaStream_t st = ctx->stream;
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
-    P.sc = S->dev;
+    common_params(P, S, o);
     P.mode = 1;
     size_t c = (size_t)slots;
     char* b = static_cast<char*>(pool);
     P.cnt = reinterpret_cast<RenderCounters*>(b);
     b += 256;
-    P.ray_o = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.ray_d = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.hit = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.tp = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.lacc = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.meta = reinterpret_cast<int4*>(b); b += 16 * c;
-    P.rng = reinterpret_cast<uint4*>(b); b += 16 * c;
-    P.sh_o = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.sh_d = reinterpret_cast<float4*>(b); b += 16 * c;
-    P.sh_c = reinterpret_cast<float4*>(b); b += 16 * c;
+    P.ray = reinterpret_cast<RayRec*>(b); b += 32 * c;
+    P.path = reinterpret_cast<PathRec*>(b); b += 32 * c;
+    P.meta = reinterpret_cast<MetaRec*>(b); b += 32 * c;
+    P.hit = reinterpret_cast<HitRec*>(b); b += 32 * c;
+    float4** f4[] = {&P.sh_o, &P.sh_d, &P.sh_c};
+    for (float4** f : f4) {
+        *f = reinterpret_cast<float4*>(b);
+        b += 16 * c;
+    }
     P.pos = reinterpret_cast<float2*>(b); b += 8 * c;
-    P.ext_q[0] = reinterpret_cast<int*>(b); b += 4 * c;
-    P.ext_q[1] = reinterpret_cast<int*>(b); b += 4 * c;
-    P.retire_q = reinterpret_cast<int*>(b);
-    filter_setup(o.filter, P.radius, P.border, P.lookup, P.filter);
-    P.film_cols = S->dev.cam.w + 2 * P.border;
-    P.film_rows = S->dev.cam.h + 2 * P.border;
+    int** iq[] = {&P.ext_q[0], &P.ext_q[1], &P.mat_q[0], &P.mat_q[1], &P.mat_q[2], &P.mat_q[3], &P.mat_q[4],
+                  &P.mat_q[5]};
+    for (int** q : iq) {
+        *q = reinterpret_cast<int*>(b);
+        b += 4 * c;
+    }
     P.xys = d_xys;
     P.li_L = d_L;
     P.li_pos = d_pos;
     P.total_paths = (unsigned long long)li_n;
-    P.max_depth = o.max_depth;
-    P.rr_depth = o.rr_depth;
-    P.flags = o.flags;
-    P.seed_mix = splitmix64(o.seed);
     int64_t cap = std::min<int64_t>(slots, ((li_n + 31) / 32) * 32);
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     cudaError_t e = cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st);
@@ -742,20 +1108,13 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     RenderCounters hc;
     int64_t iters = 0;
     for (;;) {
-        for (int k = 0; k < 4; k++) {
-            int p = (int)(iters & 1);
-            k_extend<false><<<sms * 16, 128, 0, st>>>(P, p);
-            k_shadow<false><<<sms * 16, 128, 0, st>>>(P, p);
-            k_retire<<<sms * 16, 128, 0, st>>>(P, p);
-            k_shade<<<sms * 16, 128, 0, st>>>(P, p);
-            iters++;
-        }
+        for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr);
+        iters += kBatch;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-        int p = (int)(iters & 1);
         if (hc.err) return cudaErrorUnknown;
-        if (hc.ext[p] == 0 && hc.shadow[p] == 0 && hc.retire[p] == 0 && hc.next_path >= (unsigned long long)li_n) break;
+        if (hc.ext[0] == 0 && hc.shadow[0] == 0 && hc.next_path >= (unsigned long long)li_n) break;
         if (iters > 1000000) return cudaErrorLaunchTimeout;
     }
     return cudaSuccess;

@@ -251,7 +251,7 @@ int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
  * callers that may not allocate device memory while rendering (a frame loop
  * recorded into a CUDA graph, an engine that owns all device memory after
  * start-up): the path state lives in one fixed array of 16384 path slots
- * (2.9 MiB) compiled into the library, present on every GPU that loads it.
+ * (3.75 MiB) compiled into the library, present on every GPU that loads it.
  * d_xys (n x 3 int32), d_L (n x 3 float) and d_pos (n x 2 float) are device
  * pointers supplied by the caller.  opts->max_paths_in_flight must be 0
  * (whole pool) or at most 16384, else DL_ERR_INVALID_ARG.  The first call on
