@@ -217,11 +217,12 @@ def main():
     ctx.set_kernel_timing(False)
     for _ in range(args.warmup):
         step()
-    ctx.set_kernel_timing(True)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    dev_ms, ext_ms, sh_ms, shade_ms, ret_ms = 0.0, 0.0, 0.0, 0.0, 0.0
+    # timed frames: the production path (graph replay, concurrent material
+    # kernels); device time from CUDA events on the library stream
+    dev_ms = 0.0
     ext_rays = sh_rays = cam_rays = launches = 0
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
@@ -231,10 +232,6 @@ def main():
             step()
             st = ctx.stats()
             dev_ms += st.render_ms
-            ext_ms += st.extend_ms
-            sh_ms += st.shadow_ms
-            shade_ms += st.shade_ms
-            ret_ms += st.retire_ms
             ext_rays += st.extension_rays
             sh_rays += st.shadow_rays
             cam_rays += st.camera_rays
@@ -242,7 +239,17 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     ck = clocks.summary()
+    # one more frame with per-kernel events (kernels serialised) for the
+    # kernel split and the traversal roofline
+    ctx.set_kernel_timing(True)
+    flush.zero_()
+    torch.cuda.synchronize()
+    step()
+    st = ctx.stats()
     ctx.set_kernel_timing(False)
+    ext_ms, sh_ms, shade_ms, ret_ms = st.extend_ms, st.shadow_ms, st.shade_ms, st.retire_ms
+    timed_frame_ms = st.render_ms
+    t_ext_rays, t_sh_rays = st.extension_rays, st.shadow_rays
     t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -268,11 +275,11 @@ def main():
     n_node = counts.extension_node_visits / max(1, counts.extension_rays)
     n_tri = counts.extension_triangle_tests / max(1, counts.extension_rays)
     bytes_per_ray = n_node * NODE_BYTES + n_tri * TRI_BYTES + RAY_IN + HIT_OUT
-    achieved = ext_rays * bytes_per_ray / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else 0.0
+    achieved = t_ext_rays * bytes_per_ray / (ext_ms / 1000.0) / 1e9 if ext_ms > 0 else 0.0
     sh_node = counts.shadow_node_visits / max(1, counts.shadow_rays)
     sh_tri = counts.shadow_triangle_tests / max(1, counts.shadow_rays)
     sh_bytes = sh_node * NODE_BYTES + sh_tri * TRI_BYTES + 48 + 1
-    sh_achieved = sh_rays * sh_bytes / (sh_ms / 1000.0) / 1e9 if sh_ms > 0 else 0.0
+    sh_achieved = t_sh_rays * sh_bytes / (sh_ms / 1000.0) / 1e9 if sh_ms > 0 else 0.0
 
     if rank == 0:
         base = None
@@ -288,8 +295,9 @@ def main():
             "mrays_per_s": mrays,
             "rays": {"camera": cam_rays, "extension": ext_rays, "shadow": sh_rays},
             "wall_s": wall,
-            "kernel_ms": {"extend": ext_ms, "shadow": sh_ms, "shade": shade_ms, "retire": ret_ms,
-                          "total_device": dev_ms},
+            "kernel_ms": {"frame": "one extra frame with per-kernel events (serialised kernels)",
+                          "extend": ext_ms, "shadow": sh_ms, "materials": shade_ms, "miss": ret_ms,
+                          "frame_total": timed_frame_ms, "timed_steps_device": dev_ms},
             "gpu_launches": launches,
             "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4,

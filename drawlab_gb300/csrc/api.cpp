@@ -79,6 +79,11 @@ int dl_context_create(int device, dl_context** out) {
         DL_CUDA(cudaEventCreate(&ctx->ev0));
         DL_CUDA(cudaEventCreate(&ctx->ev1));
         DL_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+        for (int i = 0; i < dl_context::kAux; i++) {
+            DL_CUDA(cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking));
+            DL_CUDA(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming));
+        }
+        DL_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
     });
     if (rc != DL_OK) {
         delete ctx;

@@ -143,9 +143,20 @@ struct dl_context {
     // kernel parameters stay byte-identical.
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<unsigned char> graph_key;
+    // Side streams and fork/join events: the miss kernel and the material
+    // kernels of an iteration run as parallel graph branches.
+    static constexpr int kAux = 5;
+    cudaStream_t aux[kAux] = {nullptr};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kAux] = {nullptr};
     ~dl_context() {
         for (cudaEvent_t e : timing_events) cudaEventDestroy(e);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        for (int i = 0; i < kAux; i++) {
+            if (aux[i]) cudaStreamDestroy(aux[i]);
+            if (join_ev[i]) cudaEventDestroy(join_ev[i]);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
     }
 };
 

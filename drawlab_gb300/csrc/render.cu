@@ -826,8 +826,12 @@ constexpr int kBatch = 4;  // iterations per counter check and per captured grap
 constexpr int kKernelsPerIteration = 8;
 
 // Launches one wavefront iteration (8 kernels).  `ev`, when given, holds 8
-// events bracketing extend, shadow, the material kernels, miss.
-static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, bool count, cudaEvent_t* ev) {
+// events bracketing extend, shadow, the material kernels, miss (kernels then
+// run one after another).  Otherwise, with `fj` given, the miss kernel and
+// the five material kernels (disjoint slots and queues) run concurrently on
+// the context's side streams, joined before the next iteration.
+static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, bool count, cudaEvent_t* ev,
+                             const dl_context* fj) {
     const int tb = sms * 8, wb = sms * 16, th = 128;
     if (ev) cudaEventRecord(ev[0], st);
     if (count) k_traverse<true, false><<<tb, th, 0, st>>>(P, p);
@@ -836,6 +840,21 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
     if (count) k_traverse<true, true><<<tb, th, 0, st>>>(P, p);
     else k_traverse<false, true><<<tb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[6], st); }
+    if (!ev && fj) {
+        cudaEventRecord(fj->fork_ev, st);
+        for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
+        k_miss<<<wb, th, 0, st>>>(P, p);
+        k_material<MAT_DIFFUSE><<<wb, th, 0, fj->aux[0]>>>(P, p);
+        k_material<MAT_MIRROR><<<wb, th, 0, fj->aux[1]>>>(P, p);
+        k_material<MAT_DIELECTRIC><<<wb, th, 0, fj->aux[2]>>>(P, p);
+        k_material<MAT_MICROFACET><<<wb, th, 0, fj->aux[3]>>>(P, p);
+        k_material<MAT_ANISO_GGX><<<wb, th, 0, fj->aux[4]>>>(P, p);
+        for (int i = 0; i < dl_context::kAux; i++) {
+            cudaEventRecord(fj->join_ev[i], fj->aux[i]);
+            cudaStreamWaitEvent(st, fj->join_ev[i], 0);
+        }
+        return;
+    }
     k_miss<<<wb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[7], st); cudaEventRecord(ev[4], st); }
     k_material<MAT_DIFFUSE><<<wb, th, 0, st>>>(P, p);
@@ -921,7 +940,7 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
             }
             cudaGraph_t g = nullptr;
             DL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr);
+            for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr, ctx);
             DL_CUDA(cudaStreamEndCapture(st, &g));
             cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
             cudaGraphDestroy(g);
@@ -940,7 +959,8 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
             DL_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
         } else {
             for (int k = 0; k < kBatch; k++)
-                launch_iteration(P, k & 1, st, sms, count_traversal, timing ? &ctx->timing_events[8 * k] : nullptr);
+                launch_iteration(P, k & 1, st, sms, count_traversal, timing ? &ctx->timing_events[8 * k] : nullptr,
+                                 ctx);
         }
         iters += kBatch;
         launches += kBatch * kKernelsPerIteration;
@@ -1108,7 +1128,7 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     RenderCounters hc;
     int64_t iters = 0;
     for (;;) {
-        for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr);
+        for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr, nullptr);
         iters += kBatch;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
