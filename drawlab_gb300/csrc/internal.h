@@ -84,17 +84,24 @@ struct HostBuf {
 
 constexpr int kNumMaterialTypes = 5;
 
+// A queue length that kernels bump with atomics, alone in its 128-byte line:
+// atomics on one line serialise in one L2 slice, so the hot counters are
+// spread over separate lines (and so over slices).
+struct alignas(128) QueueCount {
+    int n;
+};
+
 // Device counters of one wavefront render (see render.cu).
 struct RenderCounters {
-    int ext[2];       // extension-ray queue lengths (ping-pong)
-    int shadow[2];    // shadow-ray queue lengths
-    int mat[2][kNumMaterialTypes + 1];  // material-sorted hit queues + miss queue (ping-pong)
-    unsigned int work_ext;       // dynamic-fetch cursors of the traversal kernels
-    unsigned int work_sh;
-    unsigned long long next_path;
-    unsigned long long stat_ext;
+    alignas(128) int ext[2];     // extension-ray queue lengths (ping-pong)
+    alignas(128) int shadow[2];  // shadow-ray queue lengths
+    QueueCount mat[2][kNumMaterialTypes + 1];  // material-sorted hit queues + miss queue (ping-pong)
+    alignas(128) unsigned int work_ext;        // chunk cursors of the traversal kernels
+    alignas(128) unsigned int work_sh;
+    alignas(128) unsigned long long next_path;
+    alignas(128) unsigned long long stat_ext;
     unsigned long long stat_shadow;
-    unsigned long long stat_camera;
+    unsigned long long stat_camera;   // filled on the host: paths started = min(next_path, paths)
     unsigned long long stat_invalid;
     unsigned long long stat_nodes_ext;
     unsigned long long stat_tris_ext;

@@ -21,7 +21,9 @@
 //
 // Path state lives in 32-byte records (ray, path, meta+rng, hit), each read
 // and written whole: a full DRAM sector, no read-modify-write of partial
-// sectors.  Queues are compacted with warp ballots (one atomic per warp).  A
+// sectors.  Queues are compacted with warp ballots: one atomic per warp, or
+// per 32 entries where a warp stages them in shared memory; the hot counters
+// sit in separate 128-byte lines.  A
 // batch of iterations is captured once as a CUDA graph and replayed.  Every
 // path (x, y, s) owns a pcg32 stream and draws its numbers in the reference's
 // order (pixel 2D, aperture 2D, then per bounce NEE 2D, BSDF 2D, RR 1D), so
@@ -196,8 +198,6 @@ __device__ __forceinline__ bool regenerate(const RenderParams& P, int slot, bool
     unsigned long long pid = warp_claim(&P.cnt->next_path, want);
     bool ok = want && pid < P.total_paths;
     if (ok) start_path(P, slot, pid);
-    unsigned mask = __ballot_sync(0xffffffffu, ok);
-    if (mask && lane_id() == __ffs(mask) - 1) atomicAdd(&P.cnt->stat_camera, (unsigned long long)__popc(mask));
     return ok;
 }
 
@@ -324,19 +324,33 @@ constexpr int kDone = kEmptyChild;  // traversal state: ray finished
 
 // Persistent traversal over a ray queue.  Each lane holds one ray's
 // traversal state (node, stack); a lane whose ray finishes takes the next ray
-// of the queue (one atomic per warp for all lanes that need one), so lanes do
-// not idle while the warp's longest ray finishes.
+// of the queue, so lanes do not idle while the warp's longest ray finishes.
+// A warp reserves queue entries kFetchChunk at a time (one atomic per chunk)
+// and hands them to its lanes as they free up.
 //   kAny = false: closest hit of extension rays E[p] (slots) -> hit[slot], and
 //                 the slot joins the queue of its hit's material type (or the
-//                 miss queue): lanes with the same destination share one atomic
+//                 miss queue).  Each warp stages those entries per destination
+//                 in shared memory and appends them 32 at a time: one atomic
+//                 and one coalesced 128-byte store per 32 entries.
 //   kAny = true:  any hit of shadow rays S (queue positions); unoccluded ones
 //                 add their contribution to the path or the ended path's sample
+constexpr unsigned kFetchChunk = 32;
+constexpr int kTraverseWarps = 4;  // 128 threads
+constexpr int kStage = 64;         // staged entries per warp and destination (flushed at 32)
+
 template <bool kCount, bool kAny>
 __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     const int q = p ^ 1;
     const DevScene& sc = P.sc;
     const int n = kAny ? P.cnt->shadow[p] : P.cnt->ext[p];
     unsigned int* work = kAny ? &P.cnt->work_sh : &P.cnt->work_ext;
+    constexpr int kDests = kAny ? 1 : kNumMaterialTypes + 1;
+    __shared__ int s_qbuf[kTraverseWarps][kDests][kStage];
+    __shared__ int s_qcnt[kTraverseWarps][kDests];
+    const int warp = threadIdx.x >> 5, lane = lane_id();
+    const unsigned lt = (1u << lane) - 1u;
+    if (lane < kDests) s_qcnt[warp][lane] = 0;
+    __syncwarp();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!kAny) {
             // this iteration's output queues start empty
@@ -345,7 +359,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
             P.cnt->stat_ext += (unsigned long long)n;
         } else {
             // next iteration's material queues and extend cursor start empty
-            for (int k = 0; k <= kNumMaterialTypes; k++) P.cnt->mat[q][k] = 0;
+            for (int k = 0; k <= kNumMaterialTypes; k++) P.cnt->mat[q][k].n = 0;
             P.cnt->work_ext = 0;
             P.cnt->stat_shadow += (unsigned long long)n;
         }
@@ -359,17 +373,27 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     rb.idir = o;
     rb.ood = o;
     int stack[kStackSize];
+    unsigned c_next = 0, c_end = 0;  // the warp's reserved queue entries [c_next, c_end)
     for (;;) {
         bool need = !has && !exhausted;
         unsigned m = __ballot_sync(0xffffffffu, need);
         if (m) {
-            int leader = __ffs(m) - 1;
-            unsigned base = 0;
-            if (lane_id() == leader) base = atomicAdd(work, (unsigned)__popc(m));
-            base = __shfl_sync(0xffffffffu, base, leader);
+            const unsigned k = __popc(m), rank = __popc(m & lt), avail = c_end - c_next;
+            unsigned mine;
+            if (k > avail) {  // warp-uniform: reserve the next chunk
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(work, kFetchChunk);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                mine = rank < avail ? c_next + rank : base + (rank - avail);
+                c_next = base + (k - avail);
+                c_end = base + kFetchChunk;
+            } else {
+                mine = c_next + rank;
+                c_next += k;
+            }
             if (need) {
-                idx = (int)(base + __popc(m & ((1u << lane_id()) - 1u)));
-                if (idx < n) {
+                idx = (int)min(mine, (unsigned)n);
+                if (mine < (unsigned)n) {
                     float4 ro, rd;
                     if (kAny) {
                         ro = P.sh_o[idx];
@@ -485,14 +509,40 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
         }
         if (!kAny) {
             unsigned fm = __ballot_sync(0xffffffffu, finished);
-            if (finished) {
-                unsigned peers = __match_any_sync(fm, dest);
-                int leader = __ffs(peers) - 1;
-                int base = 0;
-                if (lane_id() == leader) base = atomicAdd(&P.cnt->mat[p][dest], __popc(peers));
-                base = __shfl_sync(peers, base, leader);
-                P.mat_q[dest][base + __popc(peers & ((1u << lane_id()) - 1u))] = slot;
+            while (fm) {  // warp-uniform loop over the destinations present
+                const int dd = __shfl_sync(0xffffffffu, dest, __ffs(fm) - 1);
+                const unsigned g = __ballot_sync(0xffffffffu, finished && dest == dd);
+                fm &= ~g;
+                int* buf = s_qbuf[warp][dd];
+                int c = s_qcnt[warp][dd];
+                if ((g >> lane) & 1u) buf[c + __popc(g & lt)] = slot;
+                c += __popc(g);
+                __syncwarp();
+                if (c >= 32) {
+                    int base = 0;
+                    if (lane == 0) base = atomicAdd(&P.cnt->mat[p][dd].n, 32);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    P.mat_q[dd][base + lane] = buf[lane];
+                    const int rest = c - 32;
+                    const int v = lane < rest ? buf[32 + lane] : 0;
+                    __syncwarp();
+                    if (lane < rest) buf[lane] = v;
+                    c = rest;
+                }
+                __syncwarp();
+                if (lane == 0) s_qcnt[warp][dd] = c;
+                __syncwarp();
             }
+        }
+    }
+    if (!kAny) {  // flush the staged remainders
+        for (int dd = 0; dd < kDests; dd++) {
+            const int c = s_qcnt[warp][dd];
+            if (c == 0) continue;
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&P.cnt->mat[p][dd].n, c);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (lane < c) P.mat_q[dd][base + lane] = s_qbuf[warp][dd][lane];
         }
     }
     if (err) atomicOr(&P.cnt->err, err);
@@ -512,7 +562,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
 __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
-    const int n = P.cnt->mat[p][kMissQueue];
+    const int n = P.cnt->mat[p][kMissQueue].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
         int i = i0 + lane_id();
         bool active = i < n;
@@ -539,7 +589,7 @@ template <int T>
 __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
     const int q = p ^ 1;
     const DevScene& sc = P.sc;
-    const int n = P.cnt->mat[p][T];
+    const int n = P.cnt->mat[p][T].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
         int i = i0 + lane_id();
         bool active = i < n;
@@ -980,7 +1030,7 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
         if (hc->ext[0] == 0 && hc->shadow[0] == 0 && hc->next_path >= total) break;
         if (iters > 1000000) throw Error(DL_ERR_TIMEOUT, "render did not converge");
     }
-    acc.stat_camera += hc->stat_camera;
+    acc.stat_camera += std::min<unsigned long long>(hc->next_path, total);
     acc.stat_ext += hc->stat_ext;
     acc.stat_shadow += hc->stat_shadow;
     acc.stat_nodes_ext += hc->stat_nodes_ext;
@@ -1086,7 +1136,8 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
 // device memory (`pool`, laid out below) and no allocation of any kind: no
 // cudaMalloc, no pinned staging (the counters are read back into a stack
 // copy), no exceptions, no graph.  Used by the allocation-free entry point.
-size_t fixed_pool_bytes(int64_t slots) { return kSlotBytes * (size_t)slots + 256; }
+constexpr size_t kCounterBytes = (sizeof(RenderCounters) + 255) / 256 * 256;
+size_t fixed_pool_bytes(int64_t slots) { return kSlotBytes * (size_t)slots + kCounterBytes; }
 
 cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
                             const int* d_xys, float* d_L, float* d_pos) {
@@ -1099,7 +1150,7 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     size_t c = (size_t)slots;
     char* b = static_cast<char*>(pool);
     P.cnt = reinterpret_cast<RenderCounters*>(b);
-    b += 256;
+    b += kCounterBytes;
     P.ray = reinterpret_cast<RayRec*>(b); b += 32 * c;
     P.path = reinterpret_cast<PathRec*>(b); b += 32 * c;
     P.meta = reinterpret_cast<MetaRec*>(b); b += 32 * c;
