@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 1
+DL_ABI_VERSION = 2
 
 # status
 DL_OK = 0
@@ -83,6 +83,7 @@ class dl_light_desc(C.Structure):
         ("env_height", C.c_int32),
         ("env_scale", C.c_float),
         ("env_visual", C.c_int32),
+        ("env_background", C.c_float * 3),
     ]
 
 

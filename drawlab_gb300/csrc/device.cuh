@@ -541,6 +541,94 @@ __device__ __forceinline__ float mis_weight(float a, float b) {
     return __fdiv_rn(a, __fadd_rn(a, b));
 }
 
+// ----------------------------------------------------------- environment
+// The envmap emitter of include/optix/light/envmap.h:25-94: direction <->
+// (u, v), alias-table pick of a texel followed by a uniform sample of its
+// solid angle, and the radiance lookup.  The reference looks radiance up in a
+// linear-filtered, wrap-addressed float texture (src/tracer/texture/
+// bitmap.cpp:95-99); here the same bilinear filter runs on plain loads with
+// fp32 weights.
+constexpr float kHalfInvPiF = (float)(0.5 / (double)kPiF);  // (float)(0.5 / M_PIf)
+
+__device__ __forceinline__ float3 env_lookup(const DevScene& sc, float u, float v) {
+    const int W = sc.env_w, H = sc.env_h;
+    u = __fsub_rn(u, floorf(u));
+    v = __fsub_rn(v, floorf(v));
+    float x = __fsub_rn(__fmul_rn(u, (float)W), 0.5f);
+    float y = __fsub_rn(__fmul_rn(v, (float)H), 0.5f);
+    float fx = floorf(x), fy = floorf(y);
+    float ax = __fsub_rn(x, fx), ay = __fsub_rn(y, fy);
+    int x0 = (int)fx, y0 = (int)fy;
+    int x1 = x0 + 1, y1 = y0 + 1;
+    x0 = x0 < 0 ? x0 + W : x0;
+    y0 = y0 < 0 ? y0 + H : y0;
+    x1 = x1 >= W ? x1 - W : x1;
+    y1 = y1 >= H ? y1 - H : y1;
+    float3 t00 = xyz(__ldg(sc.env_tex + (size_t)y0 * W + x0));
+    float3 t10 = xyz(__ldg(sc.env_tex + (size_t)y0 * W + x1));
+    float3 t01 = xyz(__ldg(sc.env_tex + (size_t)y1 * W + x0));
+    float3 t11 = xyz(__ldg(sc.env_tex + (size_t)y1 * W + x1));
+    float bx = __fsub_rn(1.f, ax), by = __fsub_rn(1.f, ay);
+    float3 r = add(add(add(scale(t00, __fmul_rn(bx, by)), scale(t10, __fmul_rn(ax, by))),
+                       scale(t01, __fmul_rn(bx, ay))),
+                   scale(t11, __fmul_rn(ax, ay)));
+    return scale(r, sc.env_scale);
+}
+
+// Envmap::environment_coords (envmap.h:26-30)
+__device__ __forceinline__ float2 env_coords(float3 d) {
+    float u = __fadd_rn(__fmul_rn(atan2f(d.z, d.x), kHalfInvPiF), 0.5f);
+    float v = __fmul_rn(acosf(fmaxf(fminf(d.y, 1.0f), -1.0f)), kInvPiF);
+    return make_float2(u, v);
+}
+
+// Envmap::eval (envmap.h:86-91)
+__device__ __forceinline__ float3 env_lookup_dir(const DevScene& sc, float3 d) {
+    float2 uv = env_coords(d);
+    return env_lookup(sc, uv.x, uv.y);
+}
+
+// Envmap::pdfDirection (envmap.h:78-84): solid-angle density of the texel.
+__device__ __forceinline__ float env_pdf(const DevScene& sc, float3 d) {
+    float2 uv = env_coords(d);
+    int x = min((int)__fmul_rn(uv.x, (float)sc.env_w), sc.env_w - 1);
+    int y = min((int)__fmul_rn(uv.y, (float)sc.env_h), sc.env_h - 1);
+    return __ldg(sc.env_accel + (size_t)y * sc.env_w + x).z;
+}
+
+// Envmap::sampleDirection (envmap.h:33-76) with three uniform numbers:
+// texel pick, alias coin (reused for the position in the texel's phi range),
+// position in its cos(theta) range.  Returns radiance * cos / pdf.
+__device__ __forceinline__ float3 env_sample(const DevScene& sc, float3 sh_n, float3 xi, float3& d, float& pdf) {
+    const unsigned W = (unsigned)sc.env_w, H = (unsigned)sc.env_h, size = W * H;
+    unsigned idx = min((unsigned)__fmul_rn(xi.x, (float)size), size - 1u);
+    float4 a = __ldg(sc.env_accel + idx);
+    unsigned env_idx;
+    float xy = xi.y;
+    if (xy < a.x) {
+        env_idx = idx;
+        xy = __fdiv_rn(xy, a.x);
+    } else {
+        env_idx = __float_as_uint(a.y);
+        xy = __fdiv_rn(__fsub_rn(xy, a.x), __fsub_rn(1.0f, a.x));
+    }
+    const unsigned py = env_idx / W, px = env_idx % W;
+    pdf = __ldg(sc.env_accel + env_idx).z;
+    float u = __fdiv_rn(__fadd_rn((float)px, xy), (float)W);
+    float phi = (float)__dsub_rn(__dmul_rn(__dmul_rn((double)u, 2.0), (double)kPiF), (double)kPiF);
+    float step_theta = __fdiv_rn(kPiF, (float)H);
+    float theta0 = __fmul_rn((float)py, step_theta);
+    float cos_theta = __fadd_rn(__fmul_rn(cosf(theta0), __fsub_rn(1.0f, xi.z)),
+                                __fmul_rn(cosf(__fadd_rn(theta0, step_theta)), xi.z));
+    float theta = acosf(cos_theta);
+    float sin_theta = sinf(theta);
+    d = f3(__fmul_rn(cosf(phi), sin_theta), cos_theta, __fmul_rn(sinf(phi), sin_theta));
+    if (!(pdf > 0.f)) return f3(0.f, 0.f, 0.f);
+    float3 val = env_lookup(sc, u, __fmul_rn(theta, kInvPiF));
+    float c = fmaxf(dot(sh_n, d), 0.f);
+    return c > 0.f ? divs(scale(val, c), pdf) : f3(0.f, 0.f, 0.f);
+}
+
 // ---------------------------------------------------------------- camera
 __device__ __forceinline__ void camera_ray(const DevCamera& c, float2 s, float3& o, float3& d) {
     float lx = s.x;

@@ -64,6 +64,15 @@ struct DevScene {
     int num_tris;
     int num_lights;
     DevCamera cam;
+    // environment light (env_light < 0: none).  Texels rgb+pad, row 0 at the
+    // +y pole; per texel {alias probability q, alias index, pdf, 0}.
+    const float4* __restrict__ env_tex;
+    const float4* __restrict__ env_accel;
+    int env_light;
+    int env_w, env_h;
+    int env_visual;
+    float env_scale;
+    float env_bg[3];
 };
 
 }  // namespace dl

@@ -255,10 +255,26 @@ __device__ __forceinline__ void sample_area(const DevScene& sc, const DevLight& 
     n = normalize(n);
 }
 
+// Index of the emitter that the NEE sample `s` picks (scene.cpp:148-163).
+__device__ __forceinline__ int picked_light(const DevScene& sc, float sx) {
+    const int N = sc.num_lights;
+    return N > 1 ? min((int)__fmul_rn(sx, (float)N), N - 1) : 0;
+}
+
+// Three fresh numbers for an envmap NEE sample, drawn after the NEE 2D sample.
+__device__ __forceinline__ float3 env_xi(Pcg32& g) {
+    float3 xi;
+    xi.x = g.next_float();
+    xi.y = g.next_float();
+    xi.z = g.next_float();
+    return xi;
+}
+
 // Scene::sampleEmitterDirection without the visibility test (the caller
-// traces the shadow ray).  Returns the unoccluded spectrum.
+// traces the shadow ray).  Returns the unoccluded spectrum.  An envmap pick
+// draws three more numbers from `g`.
 __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 its_p, float3 sh_n, float2 s,
-                                                 float3& d, float& dist, float& pdf, bool& delta) {
+                                                 Pcg32& g, float3& d, float& dist, float& pdf, bool& delta) {
     const DevScene& sc = P.sc;
     int N = sc.num_lights;
     float3 zero = f3(0.f, 0.f, 0.f);
@@ -267,12 +283,8 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     dist = 0.f;
     d = zero;
     if (N == 0) return zero;
-    int idx = 0;
-    if (N > 1) {
-        float fn = (float)N;
-        idx = min((int)__fmul_rn(s.x, fn), N - 1);
-        s.x = __fsub_rn(__fmul_rn(s.x, fn), (float)idx);
-    }
+    int idx = picked_light(sc, s.x);
+    if (N > 1) s.x = __fsub_rn(__fmul_rn(s.x, (float)N), (float)idx);
     const DevLight& L = sc.lights[idx];
     float3 spec;
     if (L.type == LIGHT_AREA) {
@@ -298,6 +310,9 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
         } else {
             spec = scale(scale(ld3(L.radiance), inv), inv);
         }
+    } else if (L.type == LIGHT_ENVMAP) {
+        spec = env_sample(sc, sh_n, env_xi(g), d, pdf);
+        dist = 1e16f;  // envmap.h:67
     } else {
         spec = zero;
     }
@@ -557,10 +572,14 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     }
 }
 
-// Rays that hit nothing (path.cpp:23-25, 85-87): store the sample, then start
-// new camera paths in the freed slots.
+// Rays that hit nothing (path.cpp:23-25, 85-87): with an envmap, add its
+// radiance first (miss.cu:11-49: camera rays see it if "visual", else the
+// background colour; later rays weight it by MIS against the BSDF pdf after
+// a diffuse bounce).  Store the sample, then start new camera paths in the
+// freed slots.
 __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
+    const DevScene& sc = P.sc;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
     const int n = P.cnt->mat[p][kMissQueue].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -568,9 +587,25 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
         bool active = i < n;
         int slot = active ? P.mat_q[kMissQueue][i] : 0;
         if (active) {
-            float4 L = P.path[slot].L;
-            unsigned long long pid = path_index(P.meta[slot].m);
-            store_sample(P, pid, make_float3(L.x, L.y, L.z), slot);
+            PathRec pr = P.path[slot];
+            int4 m = P.meta[slot].m;
+            float3 L = f3(pr.L.x, pr.L.y, pr.L.z);
+            if (sc.env_light >= 0) {
+                float3 dir = xyz(P.ray[slot].d);
+                if (m.y & PF_CAMERA) {
+                    L = add(L, sc.env_visual ? env_lookup_dir(sc, dir) : ld3(sc.env_bg));
+                } else {
+                    float3 le = env_lookup_dir(sc, dir);
+                    float w = 1.f;
+                    if (m.y & PF_PREV_DIFFUSE) {
+                        float ep = env_pdf(sc, dir);
+                        if (sc.num_lights != 1) ep = __fdiv_rn(ep, (float)sc.num_lights);
+                        w = mis_weight(pr.L.w, ep);
+                    }
+                    L = add(L, mul(scale(f3(pr.tp.x, pr.tp.y, pr.tp.z), w), le));
+                }
+            }
+            store_sample(P, path_index(m), L, slot);
         }
         bool ok = regenerate(P, slot, active);
         int e = warp_push(&P.cnt->ext[q], ok);
@@ -645,10 +680,13 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 float3 c = f3(0.f, 0.f, 0.f);
                 float3 ld = c;
                 float ldist = 0.f;
-                if (T != MAT_MIRROR && T != MAT_DIELECTRIC) {
+                if (T == MAT_MIRROR || T == MAT_DIELECTRIC) {
+                    // no NEE contribution, but an envmap pick still draws its numbers
+                    if (sc.env_light >= 0 && picked_light(sc, s_nee.x) == sc.env_light) (void)env_xi(g);
+                } else {
                     float lpdf;
                     bool delta;
-                    float3 espec = sample_emitter(P, h.p, h.sh.n, s_nee, ld, ldist, lpdf, delta);
+                    float3 espec = sample_emitter(P, h.p, h.sh.n, s_nee, g, ld, ldist, lpdf, delta);
                     if (__fadd_rn(__fadd_rn(espec.x, espec.y), espec.z) > 0.f && lpdf > 0.f) {
                         BRec q1;
                         q1.wi = wi;

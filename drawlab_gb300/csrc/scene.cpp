@@ -39,6 +39,64 @@ inline HV hnorm(HV a) {
 inline HV hscale(HV a, float s) { return {a.x * s, a.y * s, a.z * s}; }
 inline HV ld(const float* p) { return {p[0], p[1], p[2]}; }
 
+// EnvironmentMap::activate + build_alias_map (src/tracer/emitter/envmap.cpp:
+// 59-141): the importance of a texel is its solid angle times max(r, g, b)
+// (float, as the reference computes it; its unqualified cos of a float is the
+// double cos); an alias table (Walker/Vose, one partition array, the
+// reference's steps) picks texels in proportion to it; pdf = max(r, g, b) /
+// sum(importance) is the solid-angle density of a direction in the texel.
+// The sum and the table's residual chain (q[k] += q[j] - 1) run in double:
+// in the reference's float they misstate a texel's pick probability by up to
+// tens of percent on maps with a bright sun, and the pick would no longer
+// follow the pdf.  A map with zero importance everywhere gets pdf 0.
+void build_env_tables(const dl_light_desc& L, std::vector<float4>& tex, std::vector<float4>& accel) {
+    const unsigned rx = (unsigned)L.env_width, ry = (unsigned)L.env_height, size = rx * ry;
+    const float* px = L.env_rgb;
+    const float pi = 3.14159265358979323846f;
+    tex.resize(size);
+    accel.resize(size);
+    std::vector<float> imp(size);
+    std::vector<double> q(size);
+    std::vector<unsigned> alias(size);
+    auto maxc = [&](unsigned i) { return std::max(px[3 * i], std::max(px[3 * i + 1], px[3 * i + 2])); };
+    float cos_theta0 = 1.0f;
+    const float step_phi = (float)(2.0 * (double)pi) / (float)rx;
+    const float step_theta = pi / (float)ry;
+    for (unsigned y = 0; y < ry; ++y) {
+        const float theta1 = (float)(y + 1) * step_theta;
+        const float cos_theta1 = (float)std::cos((double)theta1);
+        const float area = (cos_theta0 - cos_theta1) * step_phi;
+        cos_theta0 = cos_theta1;
+        for (unsigned x = 0; x < rx; ++x) imp[y * rx + x] = area * maxc(y * rx + x);
+    }
+    double sum = 0.0;
+    for (unsigned i = 0; i < size; ++i) sum += imp[i];
+    if (sum > 0.0) {
+        for (unsigned i = 0; i < size; ++i) q[i] = (double)size * imp[i] / sum;
+        std::vector<unsigned> part(size);
+        unsigned s = 0u, large = size;
+        for (unsigned i = 0; i < size; ++i) part[(q[i] < 1.0) ? (s++) : (--large)] = alias[i] = i;
+        for (s = 0; s < large && large < size; ++s) {
+            const unsigned j = part[s], k = part[large];
+            alias[j] = k;
+            q[k] += q[j] - 1.0;
+            large = (q[k] < 1.0) ? (large + 1u) : large;
+        }
+    } else {
+        for (unsigned i = 0; i < size; ++i) {
+            q[i] = 1.0;
+            alias[i] = i;
+        }
+    }
+    for (unsigned i = 0; i < size; ++i) {
+        float a;
+        std::memcpy(&a, &alias[i], 4);
+        float pdf = sum > 0.0 ? (float)((double)maxc(i) / sum) : 0.0f;
+        accel[i] = make_float4((float)q[i], a, pdf, 0.f);
+        tex[i] = make_float4(px[3 * i], px[3 * i + 1], px[3 * i + 2], 0.f);
+    }
+}
+
 void check(bool ok, const std::string& msg) {
     if (!ok) throw Error(DL_ERR_INVALID_ARG, msg);
 }
@@ -103,6 +161,7 @@ void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_de
         if (m.type == DL_MAT_MICROFACET) check(m.alpha[0] > 0.f, "microfacet alpha must be > 0");
         if (m.type == DL_MAT_ANISO_GGX) check(m.alpha[0] > 0.f && m.alpha[1] > 0.f, "aniso_ggx alpha must be > 0");
     }
+    int num_env = 0;
     for (int l = 0; l < nl; l++) {
         const dl_light_desc& L = lights[l];
         if (L.type == DL_LIGHT_AREA) {
@@ -111,7 +170,15 @@ void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_de
             check(meshes[L.mesh].num_triangles > 0, "light " + std::to_string(l) + ": emitting mesh is empty");
         } else if (L.type == DL_LIGHT_POINT) {
         } else if (L.type == DL_LIGHT_ENVMAP) {
-            throw Error(DL_ERR_UNSUPPORTED, "environment lights are not supported yet");
+            std::string who = "light " + std::to_string(l) + ": ";
+            check(++num_env == 1, who + "more than one envmap in the scene");
+            check(L.env_rgb != nullptr, who + "env_rgb is NULL");
+            check(L.env_width > 0 && L.env_height > 0 && (int64_t)L.env_width * L.env_height <= ((int64_t)1 << 26),
+                  who + "envmap size out of range");
+            check(std::isfinite(L.env_scale), who + "envmap scale is not finite");
+            for (int64_t k = 0; k < 3 * (int64_t)L.env_width * L.env_height; k++)
+                check(std::isfinite(L.env_rgb[k]) && L.env_rgb[k] >= 0.f,
+                      who + "envmap texels must be finite and non-negative");
         } else {
             throw Error(DL_ERR_INVALID_ARG, "light " + std::to_string(l) + ": bad type");
         }
@@ -220,6 +287,19 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
             ecdf.insert(ecdf.end(), cdf.begin(), cdf.end());
         }
     }
+    int env_light = -1;
+    std::vector<float4> env_tex, env_accel;
+    for (int l = 0; l < nl; l++) {
+        if (lights[l].type != DL_LIGHT_ENVMAP) continue;
+        env_light = l;
+        build_env_tables(lights[l], env_tex, env_accel);
+    }
+    if (env_tex.empty()) {
+        env_tex.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+        env_accel.push_back(make_float4(1.f, 0.f, 0.f, 0.f));
+    }
+    S->env_tex.upload(env_tex, st);
+    S->env_accel.upload(env_accel, st);
 
     S->nodes.upload(bvh.nodes, st);
     S->tris.upload(bvh.tris, st);
@@ -247,6 +327,14 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     D.num_tris = (int)ntri;
     D.num_lights = nl;
     D.cam = make_camera(*cam);
+    D.env_tex = S->env_tex.as<float4>();
+    D.env_accel = S->env_accel.as<float4>();
+    D.env_light = env_light;
+    D.env_w = env_light >= 0 ? lights[env_light].env_width : 1;
+    D.env_h = env_light >= 0 ? lights[env_light].env_height : 1;
+    D.env_visual = env_light >= 0 ? (lights[env_light].env_visual != 0) : 0;
+    D.env_scale = env_light >= 0 ? lights[env_light].env_scale : 0.f;
+    for (int k = 0; k < 3; k++) D.env_bg[k] = env_light >= 0 ? lights[env_light].env_background[k] : 0.f;
     S->tri_order = bvh.tri_order;
 
     dl_scene_info& I = S->info;
@@ -262,7 +350,7 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     I.bvh_sah_cost = bvh.sah_cost;
     I.device_bytes = (int64_t)(S->nodes.bytes + S->tris.bytes + S->tri_vidx.bytes + S->normals.bytes +
                                S->meshes.bytes + S->materials.bytes + S->lights.bytes + S->emit_tris.bytes +
-                               S->emit_cdf.bytes);
+                               S->emit_cdf.bytes + S->env_tex.bytes + S->env_accel.bytes);
     dl_render_opts& O = S->defaults;
     std::memset(&O, 0, sizeof(O));
     O.spp = 1;

@@ -8,7 +8,8 @@
 // them (src/tracer/scene/scene.cpp:36-81).
 //
 // Supported plugins: mesh rectangle|obj, bsdf diffuse|mirror|dielectric|
-// microfacet|aniso_ggx, emitter area|point, camera virtual, integrator path,
+// microfacet|aniso_ggx, emitter area|point|envmap (PFM images), camera
+// virtual, integrator path,
 // sampler independent, rfilter gaussian|box.  Anything else is reported as
 // DL_ERR_UNSUPPORTED with its location.
 #include <cctype>
@@ -16,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <list>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -505,6 +507,41 @@ void apply_transform(MeshData& m, const M4& T) {
     }
 }
 
+// Portable float map (PF: RGB, Pf: grey), rows stored bottom to top, scale
+// sign = byte order.  Returns rows top to bottom, RGB.  The reference reads
+// envmaps through its Bitmap class (EXR via OpenEXR, LDR/HDR via stb_image,
+// src/core/bitmap/bitmap.cpp:30-140); this build reads PFM.
+std::vector<float> load_pfm(const std::string& path, int& w, int& h) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw Error(DL_ERR_IO, "cannot open image \"" + path + "\"");
+    std::string magic;
+    double scale = 0;
+    in >> magic >> w >> h >> scale;
+    if (!in || (magic != "PF" && magic != "Pf") || w <= 0 || h <= 0 || (int64_t)w * h > ((int64_t)1 << 26) ||
+        scale == 0)
+        throw Error(DL_ERR_PARSE, "\"" + path + "\": not a PFM image");
+    in.get();  // the single whitespace byte before the raster
+    const int ch = magic == "PF" ? 3 : 1;
+    std::vector<float> raw((size_t)w * h * ch);
+    in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * 4));
+    if (!in) throw Error(DL_ERR_PARSE, "\"" + path + "\": truncated PFM raster");
+    const uint16_t probe = 1;
+    const bool host_le = *reinterpret_cast<const uint8_t*>(&probe) == 1;
+    if ((scale < 0) != host_le) {
+        for (float& v : raw) {
+            uint8_t* b = reinterpret_cast<uint8_t*>(&v);
+            std::swap(b[0], b[3]);
+            std::swap(b[1], b[2]);
+        }
+    }
+    std::vector<float> rgb((size_t)w * h * 3);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            for (int c = 0; c < 3; c++)
+                rgb[3 * ((size_t)y * w + x) + c] = raw[ch * ((size_t)(h - 1 - y) * w + x) + (ch == 3 ? c : 0)];
+    return rgb;
+}
+
 // Wavefront OBJ: one vertex per distinct (position, texcoord, normal) index
 // triple in order of first use, faces fan-triangulated (the layout
 // tinyobjloader gives src/tracer/mesh/obj.cpp).
@@ -682,6 +719,7 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
     std::vector<dl_material_desc> mats;
     std::map<const Obj*, int> mat_index;
     std::vector<dl_light_desc> lights;
+    std::list<std::vector<float>> env_images;  // stable storage for envmap texels
     dl_camera_desc cam;
     std::memset(&cam, 0, sizeof(cam));
     bool have_cam = false, have_integrator = false, have_sampler = false;
@@ -750,6 +788,25 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
                     L.mesh = -1;
                     c->props.vec("intensity", P_COLOR, L.radiance, nullptr);
                     c->props.vec("position", P_POINT, L.position, nullptr);
+                } else if (c->type == "envmap") {
+                    // src/tracer/emitter/envmap.cpp:13-19
+                    std::string fn = c->props.s("filename");
+                    if (!fn.empty() && fn[0] != '/') fn = it.dir + "/" + fn;
+                    std::string ext = fn.size() >= 4 ? fn.substr(fn.size() - 4) : "";
+                    for (char& ch : ext) ch = (char)std::tolower((unsigned char)ch);
+                    if (ext != ".pfm")
+                        throw Error(DL_ERR_UNSUPPORTED, "envmap \"" + fn + "\": only PFM images are read");
+                    int w = 0, h = 0;
+                    env_images.push_back(load_pfm(fn, w, h));
+                    L.type = DL_LIGHT_ENVMAP;
+                    L.mesh = -1;
+                    L.env_rgb = env_images.back().data();
+                    L.env_width = w;
+                    L.env_height = h;
+                    L.env_scale = c->props.f("scale", 1.0f);
+                    L.env_visual = c->props.b("visual", true) ? 1 : 0;
+                    const float zero[3] = {0.f, 0.f, 0.f};
+                    scene->props.vec("bg_color", P_COLOR, L.env_background, zero);
                 } else {
                     throw Error(DL_ERR_UNSUPPORTED, "emitter type \"" + c->type + "\" is not supported at scene level");
                 }

@@ -59,6 +59,7 @@ class Light:
     env_rgb: np.ndarray | None = None   # (H, W, 3) float32
     env_scale: float = 1.0
     env_visual: int = 1
+    env_background: tuple = (0.0, 0.0, 0.0)
 
 
 @dataclass
@@ -152,6 +153,7 @@ class SceneData:
                 ld[i].env_width = x.env_rgb.shape[1]
             ld[i].env_scale = x.env_scale
             ld[i].env_visual = x.env_visual
+            ld[i].env_background[:] = [float(v) for v in x.env_background]
         cam = abi.dl_camera_desc()
         c = self.camera
         cam.type = abi.DL_CAMERA_VIRTUAL
@@ -428,3 +430,68 @@ SCENES = {
     "mis_plates": mis_plates,
     "reference_spheres": reference_spheres,
 }
+
+
+# ----------------------------------------------------------------- envmaps
+
+def sky_envmap(width: int = 2048, height: int = 1024, sun_dir=(0.35, 0.6, -0.72), sun_peak: float = 1.0e4,
+               sun_radius_deg: float = 0.5, sky_scale: float = 1.0) -> np.ndarray:
+    """Procedural latitude-longitude sky, (height, width, 3) float32: a
+    zenith-to-horizon gradient above a dim ground, plus a sun lobe of peak
+    radiance `sun_peak` and angular radius `sun_radius_deg` (smooth falloff
+    over the outer fifth).  Row 0 is the +y pole; texel centres map to
+    directions as the envmap emitter's lookup does."""
+    y, x = np.mgrid[0:height, 0:width].astype(np.float64)
+    u = (x + 0.5) / width
+    v = (y + 0.5) / height
+    phi = 2.0 * np.pi * u - np.pi
+    theta = np.pi * v
+    d = np.stack([np.cos(phi) * np.sin(theta), np.cos(theta), np.sin(phi) * np.sin(theta)], axis=-1)
+    up = np.clip(d[..., 1], 0.0, 1.0)[..., None]
+    zenith = np.array([0.15, 0.3, 0.8])
+    horizon = np.array([0.8, 0.85, 0.9])
+    ground = np.array([0.25, 0.22, 0.2])
+    sky = np.where(d[..., 1:2] >= 0.0, horizon + (zenith - horizon) * np.sqrt(up), ground * 0.5)
+    s = np.asarray(sun_dir, np.float64)
+    s = s / np.linalg.norm(s)
+    ang = np.degrees(np.arccos(np.clip(d @ s, -1.0, 1.0)))
+    r = float(sun_radius_deg)
+    lobe = np.clip((r - ang) / (0.2 * r), 0.0, 1.0)
+    rgb = sky * sky_scale + (sun_peak * lobe)[..., None] * np.array([1.0, 0.95, 0.85])
+    return np.ascontiguousarray(rgb, dtype=np.float32)
+
+
+def env_spheres(width: int = 96, height: int = 64, spp: int = 4, max_depth: int = 8, env_width: int = 64,
+                env_height: int = 32, sun_radius_deg: float = 6.0, sun_peak: float = 200.0,
+                with_area_light: bool = True, visual: int = 1) -> SceneData:
+    """Spheres of every material type on a ground quad under a procedural sky
+    envmap (optionally plus one quad area light): the envmap NEE, MIS and miss
+    paths.  The default map is small, with a wide sun, so the oracle stays
+    fast; the 2048x1024 form with a 0.5-degree sun is sky_envmap()."""
+    s = SceneData("env_spheres", spp=spp, max_depth=max_depth, rr_depth=3)
+    ground = s.add_material(Material(albedo=(0.5, 0.45, 0.4)))
+    p, f, n = rectangle((-8, 0, -8), (0, 0, 16), (16, 0, 0))
+    s.add_mesh(Mesh(p, f, n, material=ground))
+    kinds = [
+        Material(type=abi.DL_MAT_DIFFUSE, albedo=(0.8, 0.3, 0.2)),
+        Material(type=abi.DL_MAT_MIRROR),
+        Material(type=abi.DL_MAT_DIELECTRIC, int_ior=1.5, ext_ior=1.000277),
+        Material(type=abi.DL_MAT_MICROFACET, albedo=(0.2, 0.2, 0.4), alpha=(0.2, 0.2), int_ior=1.7),
+        Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1), alpha=(0.15, 0.15)),
+        Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0.2, 0.2, 0.2), specular=(0.8, 0.8, 0.8), alpha=(0.05, 0.3)),
+    ]
+    for k, m in enumerate(kinds):
+        mi = s.add_material(m)
+        p, f, n = sphere_mesh(2, (-3.75 + 1.5 * k, 0.601, 0.3 * (k % 2)), 0.6)
+        s.add_mesh(Mesh(p, f, n, material=mi))
+    if with_area_light:
+        black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+        p, f, n = rectangle((-1.0, 4.0, -1.0), (2.0, 0, 0), (0, 0, 1.5))
+        li = s.add_mesh(Mesh(p, f, n, material=black))
+        s.add_area_light(li, (6.0, 6.0, 6.0))
+    env = sky_envmap(env_width, env_height, sun_peak=sun_peak, sun_radius_deg=sun_radius_deg)
+    s.lights.append(Light(type=abi.DL_LIGHT_ENVMAP, env_rgb=env, env_scale=1.0, env_visual=visual,
+                          env_background=(0.1, 0.2, 0.3)))
+    s.camera = Camera(width=width, height=height, eye=(0.0, 2.5, 9.0), lookat=(0.0, 0.5, 0.0),
+                      up=(0.0, 1.0, 0.0), fov=40.0)
+    return s

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 1
+#define DL_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -91,11 +91,17 @@ typedef struct dl_light_desc {
     int32_t mesh;          /* area: index of the emitting mesh */
     float radiance[3];     /* area radiance | point intensity */
     float position[3];     /* point position */
-    const float* env_rgb;  /* envmap: env_height x env_width x 3 floats, lat-long */
+    /* envmap: env_height x env_width x 3 floats, latitude-longitude.  Row 0
+     * is the +y pole (theta = 0), the last row the -y pole; column u covers
+     * phi = atan2(z, x) = 2 pi u - pi (include/optix/light/envmap.h:26-30).
+     * At most one envmap per scene (src/tracer/scene/scene.cpp:72-78). */
+    const float* env_rgb;
     int32_t env_width;
     int32_t env_height;
     float env_scale;       /* envmap "scale" (default 1) */
     int32_t env_visual;    /* envmap "visual": seen by camera rays (default 1) */
+    float env_background[3]; /* what camera rays that miss see when visual = 0:
+                                the scene's "bg_color" (scene.cpp:7, miss.cu:20-27) */
 } dl_light_desc;
 
 enum dl_camera_type {

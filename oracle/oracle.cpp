@@ -389,6 +389,14 @@ struct Light {
     int type;
     int mesh;
     V3 radiance, position;
+    // envmap (include/optix/light/envmap.h, src/tracer/emitter/envmap.cpp)
+    int env_w = 0, env_h = 0;
+    float env_scale = 1.f;
+    bool env_visual = true;
+    V3 env_bg;
+    std::vector<float> env_rgb;      // rows from the +y pole down
+    std::vector<float> env_q, env_pdf;
+    std::vector<uint32_t> env_alias;
 };
 
 struct Node {
@@ -423,6 +431,7 @@ struct Scene {
     std::vector<Mesh> meshes;
     std::vector<Material> mats;
     std::vector<Light> lights;
+    int env_light = -1;
     std::vector<Node> nodes;
     int root = -1;
     Camera cam;
@@ -783,30 +792,172 @@ V3 emitter_sample_direction(const Scene& sc, const Light& L, P2 s, const Hit& it
     return V3();
 }
 
+// ---------------------------------------------------------------- envmap
+// The envmap emitter exists only in the reference's OptiX backend
+// (include/optix/light/envmap.h:25-94, tables from src/tracer/emitter/
+// envmap.cpp:59-141; miss shading src/optix/cuda/miss.cu:11-49).  Restated
+// here with the C float functions for CUDA's atan2f/acosf/cosf/sinf, a
+// bilinear, wrap-addressed lookup for the reference's linear-filtered float
+// texture, and the pcg32 ordering of this renderer: an envmap pick in NEE
+// draws three fresh numbers after the NEE 2D sample.
+
+// envmap.cpp:59-141 (importance, alias table, pdf)
+void env_build(Light& L) {
+    const uint32_t rx = L.env_w, ry = L.env_h, size = rx * ry;
+    const float* px = L.env_rgb.data();
+    std::vector<float> imp(size);
+    L.env_q.assign(size, 0.f);
+    L.env_pdf.assign(size, 0.f);
+    L.env_alias.assign(size, 0u);
+    auto maxc3 = [&](uint32_t i) { return std::max(px[3 * i], std::max(px[3 * i + 1], px[3 * i + 2])); };
+    float cos_theta0 = 1.0f;
+    const float step_phi = (float)(2.0 * (double)kPi) / (float)rx;
+    const float step_theta = kPi / (float)ry;
+    for (uint32_t y = 0; y < ry; ++y) {
+        const float theta1 = (float)(y + 1) * step_theta;
+        const float cos_theta1 = (float)std::cos((double)theta1);
+        const float area = (cos_theta0 - cos_theta1) * step_phi;
+        cos_theta0 = cos_theta1;
+        for (uint32_t x = 0; x < rx; ++x) imp[y * rx + x] = area * maxc3(y * rx + x);
+    }
+    // sum and residual chain in double (the renderer's choice: the
+    // reference's float chain misstates pick probabilities on bright suns)
+    double sum = 0.0;
+    for (uint32_t i = 0; i < size; ++i) sum += imp[i];
+    if (!(sum > 0.0)) {
+        for (uint32_t i = 0; i < size; ++i) {
+            L.env_q[i] = 1.0f;
+            L.env_alias[i] = i;
+        }
+        return;
+    }
+    std::vector<double> q(size);
+    for (uint32_t i = 0; i < size; ++i) q[i] = (double)size * imp[i] / sum;
+    std::vector<uint32_t> part(size);
+    uint32_t s = 0u, large = size;
+    for (uint32_t i = 0; i < size; ++i) part[(q[i] < 1.0) ? (s++) : (--large)] = L.env_alias[i] = i;
+    for (s = 0; s < large && large < size; ++s) {
+        const uint32_t j = part[s], k = part[large];
+        L.env_alias[j] = k;
+        q[k] += q[j] - 1.0;
+        large = (q[k] < 1.0) ? (large + 1u) : large;
+    }
+    for (uint32_t i = 0; i < size; ++i) {
+        L.env_q[i] = (float)q[i];
+        L.env_pdf[i] = (float)((double)maxc3(i) / sum);
+    }
+}
+
+// linear filter, wrap addressing, normalised coordinates
+V3 env_lookup(const Light& L, float u, float v) {
+    const int W = L.env_w, H = L.env_h;
+    u = u - std::floor(u);
+    v = v - std::floor(v);
+    float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy, x1 = x0 + 1, y1 = y0 + 1;
+    if (x0 < 0) x0 += W;
+    if (y0 < 0) y0 += H;
+    if (x1 >= W) x1 -= W;
+    if (y1 >= H) y1 -= H;
+    auto tx = [&](int yy, int xx) { return ld3(&L.env_rgb[3 * ((size_t)yy * W + xx)]); };
+    float bx = 1.f - ax, by = 1.f - ay;
+    V3 r = tx(y0, x0) * (bx * by) + tx(y0, x1) * (ax * by) + tx(y1, x0) * (bx * ay) + tx(y1, x1) * (ax * ay);
+    return r * L.env_scale;
+}
+
+// envmap.h:26-30
+P2 env_coords(V3 d) {
+    float u = std::atan2(d.z, d.x) * (float)(0.5 / (double)kPi) + 0.5f;
+    float v = std::acos(std::fmax(std::fmin(d.y, 1.0f), -1.0f)) * kInvPi;
+    return P2{u, v};
+}
+
+V3 env_eval(const Light& L, V3 d) {
+    P2 uv = env_coords(d);
+    return env_lookup(L, uv.x, uv.y);
+}
+
+// envmap.h:78-84
+float env_pdf(const Light& L, V3 d) {
+    P2 uv = env_coords(d);
+    int x = std::min((int)(uv.x * (float)L.env_w), L.env_w - 1);
+    int y = std::min((int)(uv.y * (float)L.env_h), L.env_h - 1);
+    return L.env_pdf[(size_t)y * L.env_w + x];
+}
+
+// envmap.h:33-76
+V3 env_sample(const Light& L, const Hit& its, V3 xi, DirSample& ds) {
+    const uint32_t W = L.env_w, H = L.env_h, size = W * H;
+    uint32_t idx = std::min((uint32_t)(xi.x * (float)size), size - 1);
+    uint32_t env_idx;
+    float xy = xi.y;
+    if (xy < L.env_q[idx]) {
+        env_idx = idx;
+        xy /= L.env_q[idx];
+    } else {
+        env_idx = L.env_alias[idx];
+        xy = (xy - L.env_q[idx]) / (1.0f - L.env_q[idx]);
+    }
+    const uint32_t py = env_idx / W, px = env_idx % W;
+    float pdf = L.env_pdf[env_idx];
+    float u = ((float)px + xy) / (float)W;
+    float phi = (float)((double)u * 2.0 * (double)kPi - (double)kPi);
+    float step_theta = kPi / (float)H;
+    float theta0 = (float)py * step_theta;
+    float cos_theta = std::cos(theta0) * (1.0f - xi.z) + std::cos(theta0 + step_theta) * xi.z;
+    float theta = std::acos(cos_theta);
+    float sin_theta = std::sin(theta);
+    ds.o = its.p;
+    ds.d = V3(std::cos(phi) * sin_theta, cos_theta, std::sin(phi) * sin_theta);
+    ds.n = -ds.d;
+    ds.dist = 1e16f;
+    ds.pdf = pdf;
+    if (!(pdf > 0.f)) return V3();
+    V3 val = env_lookup(L, u, theta * kInvPi);
+    float c = std::max(dot(its.sh.n, ds.d), 0.f);
+    return c > 0.f ? val * c / pdf : V3();
+}
+
 float emitter_pdf_direction(const Scene& sc, const Light& L, const DirSample& ds) {
     if (L.type == DL_LIGHT_AREA) {
         float pA = sc.meshes[L.mesh].dpdf.norm;
         float dp = std::max(dot(ds.n, -ds.d), 0.0f);
         return dp != 0 ? pA * ds.dist * ds.dist / dp : 0;
     }
+    if (L.type == DL_LIGHT_ENVMAP) return env_pdf(L, ds.d);
     return 0;
 }
 
-// scene.cpp:139-170; `delta` reports a point light (for the fix flag).
+// scene.cpp:139-170; `delta` reports a point light (for the fix flag).  An
+// envmap pick draws three numbers from `rng` (none given: no sample).
 void sample_emitter(const Scene& sc, const Hit& its, P2 s, DirSample& ds, V3& spec, bool& delta,
-                    uint32_t flags) {
+                    uint32_t flags, Pcg32* rng) {
     size_t N = sc.lights.size();
     delta = false;
+    auto one = [&](const Light& L, P2 ss) {
+        if (L.type != DL_LIGHT_ENVMAP) return emitter_sample_direction(sc, L, ss, its, ds, flags);
+        if (!rng) {
+            ds.pdf = 0;
+            return V3();
+        }
+        V3 xi;
+        xi.x = rng->next1d();
+        xi.y = rng->next1d();
+        xi.z = rng->next1d();
+        return env_sample(L, its, xi, ds);
+    };
     if (N == 0) {
         spec = V3();
     } else if (N == 1) {
-        spec = emitter_sample_direction(sc, sc.lights[0], s, its, ds, flags);
+        spec = one(sc.lights[0], s);
         delta = sc.lights[0].type == DL_LIGHT_POINT;
     } else {
         float epdf = 1.f / N;
         size_t idx = std::min((size_t)(s.x * N), N - 1);
         s.x = s.x * N - idx;
-        spec = emitter_sample_direction(sc, sc.lights[idx], s, its, ds, flags);
+        spec = one(sc.lights[idx], s);
         delta = sc.lights[idx].type == DL_LIGHT_POINT;
         spec = spec * (float)N;
         ds.pdf *= epdf;
@@ -854,7 +1005,14 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
     float eta = 1.f;
     V3 result, tp(1.f, 1.f, 1.f);
     Hit its;
-    if (!ray_intersect(sc, ray, its)) return result;
+    if (!ray_intersect(sc, ray, its)) {
+        // miss.cu:20-27: the camera sees the envmap if "visual", else bg_color
+        if (sc.env_light >= 0) {
+            const Light& E = sc.lights[sc.env_light];
+            result = E.env_visual ? env_eval(E, ray.d) : E.env_bg;
+        }
+        return result;
+    }
     int light = sc.meshes[its.mesh].light;
     if (light >= 0) result = result + mul(tp, emitter_eval(sc.lights[light], its, -ray.d));
     for (int depth = 0;; ++depth) {
@@ -864,7 +1022,7 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
         DirSample ds;
         V3 ev;
         bool delta = false;
-        sample_emitter(sc, its, rng.next2d(), ds, ev, delta, o.flags);
+        sample_emitter(sc, its, rng.next2d(), ds, ev, delta, o.flags, &rng);
         V3 wi = to_local(fr, -normalized(ray.d));
         if (bsdf.type == DL_MAT_ANISO_GGX) wi = normalized(wi);
         V3 wo = to_local(fr, ds.d);
@@ -897,6 +1055,17 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
                 result = result + mul(w * tp, le);
             }
         } else {
+            // miss.cu:28-44: envmap radiance, MIS-weighted after a diffuse bounce
+            if (sc.env_light >= 0) {
+                V3 le = env_eval(sc.lights[sc.env_light], ray.d);
+                float w = 1.f;
+                if (is_diffuse(bsdf)) {
+                    DirSample hs;
+                    hs.d = ray.d;
+                    w = mis(bsdf_pdf(bsdf, bq), pdf_emitter(sc, sc.env_light, hs));
+                }
+                result = result + mul(w * tp, le);
+            }
             break;
         }
         if (depth > o.rr_depth) {
@@ -1147,8 +1316,23 @@ void* orc_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
                 return nullptr;
             }
             sc->meshes[L.mesh].light = l;
+        } else if (L.type == DL_LIGHT_ENVMAP) {
+            const dl_light_desc& d = lights[l];
+            if (sc->env_light >= 0 || !d.env_rgb || d.env_width <= 0 || d.env_height <= 0) {
+                g_error = "bad envmap (at most one, with texels)";
+                delete sc;
+                return nullptr;
+            }
+            L.env_w = d.env_width;
+            L.env_h = d.env_height;
+            L.env_scale = d.env_scale;
+            L.env_visual = d.env_visual != 0;
+            L.env_bg = ld3(d.env_background);
+            L.env_rgb.assign(d.env_rgb, d.env_rgb + 3 * (size_t)d.env_width * d.env_height);
+            env_build(L);
+            sc->env_light = l;
         } else if (L.type != DL_LIGHT_POINT) {
-            g_error = "environment light not supported by the oracle";
+            g_error = "bad light type";
             delete sc;
             return nullptr;
         }
@@ -1358,12 +1542,23 @@ int orc_emitter_sample(void* p, const dl_render_opts* opts, int64_t n, const flo
         DirSample ds;
         V3 sp;
         bool delta;
-        sample_emitter(sc, its, P2{smp[2 * i], smp[2 * i + 1]}, ds, sp, delta, flags);
+        sample_emitter(sc, its, P2{smp[2 * i], smp[2 * i + 1]}, ds, sp, delta, flags, nullptr);
         d[3 * i] = ds.d.x; d[3 * i + 1] = ds.d.y; d[3 * i + 2] = ds.d.z;
         spec[3 * i] = sp.x; spec[3 * i + 1] = sp.y; spec[3 * i + 2] = sp.z;
         dist[i] = ds.dist;
         pdf[i] = ds.pdf;
     }
+    return 0;
+}
+
+int orc_env_tables(void* p, float* q, uint32_t* alias, float* pdf) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    if (sc.env_light < 0) return 1;
+    const Light& L = sc.lights[sc.env_light];
+    size_t n = (size_t)L.env_w * L.env_h;
+    std::copy(L.env_q.begin(), L.env_q.begin() + n, q);
+    std::copy(L.env_alias.begin(), L.env_alias.begin() + n, alias);
+    std::copy(L.env_pdf.begin(), L.env_pdf.begin() + n, pdf);
     return 0;
 }
 

@@ -61,6 +61,10 @@ int orc_emitter_sample(void* scene, const dl_render_opts* opts, int64_t n, const
                        const float* nrm, const float* smp, float* d, float* dist, float* pdf,
                        float* spec);
 
+/* The envmap's alias table and pdf (src/tracer/emitter/envmap.cpp:59-141),
+ * env_width x env_height entries each.  Returns nonzero without an envmap. */
+int orc_env_tables(void* scene, float* q, uint32_t* alias, float* pdf);
+
 #ifdef __cplusplus
 }
 #endif

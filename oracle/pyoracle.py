@@ -149,6 +149,19 @@ class OracleScene:
                                     _f(smp), _f(d), _f(dist), _f(pdf), _f(spec))
         return d, dist, pdf, spec
 
+    def env_tables(self):
+        """(q, alias, pdf) of the envmap, each (env_height, env_width)."""
+        env = [x for x in self.scene.lights if x.type == abi.DL_LIGHT_ENVMAP]
+        if not env:
+            raise ValueError("scene has no envmap")
+        h, w = env[0].env_rgb.shape[:2]
+        q = np.empty((h, w), np.float32)
+        alias = np.empty((h, w), np.uint32)
+        pdf = np.empty((h, w), np.float32)
+        if self.lib.orc_env_tables(self.h, _f(q), _f(alias), _f(pdf)) != 0:
+            raise RuntimeError("oracle has no envmap tables")
+        return q, alias, pdf
+
 
 class RefScene:
     """The reference's own CPU code bound to one scene (x86 container only)."""

@@ -51,6 +51,38 @@ def test_struct_sizes_match_header():
     assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1)
 
 
+STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts",
+           "dl_scene_info", "dl_stats", "dl_traversal_counts"]
+
+
+def test_struct_layouts_match_a_c_compiler(tmp_path):
+    # every field offset and struct size of the ctypes mirrors against gcc
+    # compiling the header itself
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "drawlab.h"', "int main(void) {"]
+    for name in STRUCTS:
+        cls = getattr(abi, name)
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                 text=True).stdout.splitlines())
+    for name in STRUCTS:
+        cls = getattr(abi, name)
+        assert int(out[name]) == C.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(out["%s.%s" % (name, f)]) == getattr(cls, f).offset, (name, f)
+
+
 def test_null_handles_are_rejected(lib):
     assert lib.dl_scene_destroy(None) == abi.DL_ERR_INVALID_ARG
     assert lib.dl_context_destroy(None) == abi.DL_ERR_INVALID_ARG

@@ -51,6 +51,9 @@ LI_CASES = {
     "spheres16": (lambda: scenes.material_spheres(width=96, height=54, num_spheres=16, level=3),
                   dict(max_depth=16)),
     "mis_plates": (lambda: scenes.mis_plates(width=96, height=54), dict(max_depth=8)),
+    "env_spheres": (lambda: scenes.env_spheres(width=64, height=40), dict(max_depth=8)),
+    "env_only_bg": (lambda: scenes.env_spheres(width=64, height=40, with_area_light=False, visual=0),
+                    dict(max_depth=6)),
 }
 
 

@@ -131,3 +131,51 @@ def test_unsupported_plugin_is_reported(ctx, tmp_path):
     with pytest.raises(api.DrawlabError) as e:
         api.Scene.from_xml(ctx, str(p))
     assert e.value.status == abi.DL_ERR_UNSUPPORTED
+
+
+def write_pfm(path, rgb):
+    """PFM: rows bottom to top, little endian (negative scale)."""
+    h, w, _ = rgb.shape
+    with open(path, "wb") as f:
+        f.write(b"PF\n%d %d\n-1.0\n" % (w, h))
+        f.write(np.ascontiguousarray(rgb[::-1], dtype="<f4").tobytes())
+
+
+def test_xml_envmap_matches_arrays(ctx, tmp_path):
+    arr, (P, F, N) = arrays_equivalent()
+    sky = scenes.sky_envmap(64, 32, sun_peak=50.0, sun_radius_deg=8.0)
+    arr.lights.append(scenes.Light(type=abi.DL_LIGHT_ENVMAP, env_rgb=sky, env_scale=2.0, env_visual=0,
+                                   env_background=(0.1, 0.2, 0.3)))
+    write_obj(tmp_path / "cuboid.obj", P, F, N)
+    write_pfm(tmp_path / "sky.pfm", sky)
+    text = cornell_xml(arr, "cuboid.obj").replace(
+        "</scene>",
+        '  <color name="bg_color" value="0.1, 0.2, 0.3"/>\n'
+        '  <emitter type="envmap"><string name="filename" value="sky.pfm"/>'
+        '<float name="scale" value="2"/><boolean name="visual" value="false"/></emitter>\n</scene>')
+    (tmp_path / "scene.xml").write_text(text)
+    gx = api.Scene.from_xml(ctx, str(tmp_path / "scene.xml"))
+    ga = api.Scene.from_data(ctx, arr)
+    assert gx.info().num_lights == 2
+    xys = np.array([(x, y, s) for y in range(32) for x in range(40) for s in range(2)], np.int32)
+    opts = abi.make_opts(seed=4, max_depth=6)
+    La, _ = gx.li(opts, xys)
+    Lb, _ = ga.li(opts, xys)
+    np.testing.assert_array_equal(La, Lb)
+    assert (La > 0).any()
+
+
+def test_xml_envmap_bad_image(ctx, tmp_path):
+    (tmp_path / "bad.pfm").write_bytes(b"P6\n2 2\n255\n")
+    (tmp_path / "s.xml").write_text(
+        "<scene><integrator type='path'/><emitter type='envmap'>"
+        "<string name='filename' value='bad.pfm'/></emitter></scene>")
+    with pytest.raises(api.DrawlabError) as e:
+        api.Scene.from_xml(ctx, str(tmp_path / "s.xml"))
+    assert e.value.status == abi.DL_ERR_PARSE and "not a PFM image" in str(e.value)
+    (tmp_path / "t.xml").write_text(
+        "<scene><integrator type='path'/><emitter type='envmap'>"
+        "<string name='filename' value='sky.exr'/></emitter></scene>")
+    with pytest.raises(api.DrawlabError) as e:
+        api.Scene.from_xml(ctx, str(tmp_path / "t.xml"))
+    assert e.value.status == abi.DL_ERR_UNSUPPORTED
