@@ -48,7 +48,7 @@ void check_opts(const dl_render_opts* o) {
     need(o->filter == DL_FILTER_GAUSSIAN || o->filter == DL_FILTER_BOX, "unknown filter");
     need(o->spp_offset >= 0, "spp_offset must be >= 0");
     need(o->max_paths_in_flight >= 0 && o->max_paths_in_flight <= ((int64_t)1 << 28), "max_paths_in_flight out of range");
-    need((o->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT)) == 0, "unsupported render flags");
+    need((o->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT | DL_RENDER_POWER_LIGHT_PICK)) == 0, "unsupported render flags");
 }
 
 }  // namespace

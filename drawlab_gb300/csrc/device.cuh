@@ -552,6 +552,7 @@ constexpr float kHalfInvPiF = (float)(0.5 / (double)kPiF);  // (float)(0.5 / M_P
 
 __device__ __forceinline__ float3 env_lookup(const DevScene& sc, float u, float v) {
     const int W = sc.env_w, H = sc.env_h;
+    if (!isfinite(u) || !isfinite(v)) return f3(0.f, 0.f, 0.f);  // no direction
     u = __fsub_rn(u, floorf(u));
     v = __fsub_rn(v, floorf(v));
     float x = __fsub_rn(__fmul_rn(u, (float)W), 0.5f);

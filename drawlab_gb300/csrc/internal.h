@@ -171,7 +171,7 @@ struct dl_scene {
     dl_context* ctx = nullptr;
     dl::DevScene dev{};
     dl::DevBuf nodes, tris, tri_vidx, normals, meshes, materials, lights, emit_tris, emit_cdf;
-    dl::DevBuf env_tex, env_accel;
+    dl::DevBuf env_tex, env_accel, light_pick;
     std::vector<int32_t> tri_order;   // leaf-order triangle -> original id
     dl_scene_info info{};
     dl_render_opts defaults{};

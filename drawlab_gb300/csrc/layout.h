@@ -68,6 +68,9 @@ struct DevScene {
     // +y pole; per texel {alias probability q, alias index, pdf, 0}.
     const float4* __restrict__ env_tex;
     const float4* __restrict__ env_accel;
+    // power-proportional emitter pick: per light {alias q, alias index, pick
+    // probability, 0}
+    const float4* __restrict__ light_pick;
     int env_light;
     int env_w, env_h;
     int env_visual;

@@ -78,7 +78,7 @@ extern "C" int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t
         ctx->error = "dl_li_static: max_paths_in_flight exceeds the static pool of 16384 paths";
         return DL_ERR_INVALID_ARG;
     }
-    if (opts->rr_depth < 0 || (opts->flags & ~(uint32_t)DL_RENDER_FIX_POINT_LIGHT) ||
+    if (opts->rr_depth < 0 || (opts->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT | DL_RENDER_POWER_LIGHT_PICK)) ||
         (opts->filter != DL_FILTER_GAUSSIAN && opts->filter != DL_FILTER_BOX)) {
         ctx->error = "dl_li_static: unsupported render options";
         return DL_ERR_INVALID_ARG;

@@ -255,10 +255,36 @@ __device__ __forceinline__ void sample_area(const DevScene& sc, const DevLight& 
     n = normalize(n);
 }
 
-// Index of the emitter that the NEE sample `s` picks (scene.cpp:148-163).
-__device__ __forceinline__ int picked_light(const DevScene& sc, float sx) {
+// The emitter that the NEE sample's first number picks, that number rescaled
+// to [0, 1) for reuse: uniformly (scene.cpp:148-163), or, with
+// DL_RENDER_POWER_LIGHT_PICK, through the power alias table (slot from the
+// number, alias coin from its fraction).
+__device__ __forceinline__ int pick_light(const RenderParams& P, float& sx) {
+    const DevScene& sc = P.sc;
     const int N = sc.num_lights;
-    return N > 1 ? min((int)__fmul_rn(sx, (float)N), N - 1) : 0;
+    if (!(P.flags & DL_RENDER_POWER_LIGHT_PICK)) {
+        if (N <= 1) return 0;
+        int idx = min((int)__fmul_rn(sx, (float)N), N - 1);
+        sx = __fsub_rn(__fmul_rn(sx, (float)N), (float)idx);
+        return idx;
+    }
+    float u = __fmul_rn(sx, (float)N);
+    int i = min((int)u, N - 1);
+    float coin = fminf(__fsub_rn(u, (float)i), 0.99999994f);
+    float4 a = __ldg(sc.light_pick + i);
+    if (coin < a.x) {
+        sx = __fdiv_rn(coin, a.x);
+        return i;
+    }
+    sx = __fdiv_rn(__fsub_rn(coin, a.x), __fsub_rn(1.f, a.x));
+    return __float_as_int(a.y);
+}
+
+// pdf of direction sample `pdf` of emitter `l` times its pick probability
+// (pdfEmitterDirection, scene.cpp:171-179).
+__device__ __forceinline__ float with_pick_pdf(const RenderParams& P, int l, float pdf) {
+    if (P.flags & DL_RENDER_POWER_LIGHT_PICK) return __fmul_rn(pdf, __ldg(P.sc.light_pick + l).z);
+    return P.sc.num_lights != 1 ? __fdiv_rn(pdf, (float)P.sc.num_lights) : pdf;
 }
 
 // Three fresh numbers for an envmap NEE sample, drawn after the NEE 2D sample.
@@ -283,8 +309,7 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     dist = 0.f;
     d = zero;
     if (N == 0) return zero;
-    int idx = picked_light(sc, s.x);
-    if (N > 1) s.x = __fsub_rn(__fmul_rn(s.x, (float)N), (float)idx);
+    const int idx = pick_light(P, s.x);
     const DevLight& L = sc.lights[idx];
     float3 spec;
     if (L.type == LIGHT_AREA) {
@@ -316,7 +341,11 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     } else {
         spec = zero;
     }
-    if (N > 1) {
+    if (P.flags & DL_RENDER_POWER_LIGHT_PICK) {
+        const float pl = __ldg(sc.light_pick + idx).z;
+        spec = divs(spec, pl);
+        pdf = __fmul_rn(pdf, pl);
+    } else if (N > 1) {
         spec = scale(spec, (float)N);
         pdf = __fmul_rn(pdf, __fdiv_rn(1.f, (float)N));
     }
@@ -599,7 +628,7 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
                     float w = 1.f;
                     if (m.y & PF_PREV_DIFFUSE) {
                         float ep = env_pdf(sc, dir);
-                        if (sc.num_lights != 1) ep = __fdiv_rn(ep, (float)sc.num_lights);
+                        ep = with_pick_pdf(P, sc.env_light, ep);
                         w = mis_weight(pr.L.w, ep);
                     }
                     L = add(L, mul(scale(f3(pr.tp.x, pr.tp.y, pr.tp.z), w), le));
@@ -657,7 +686,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     float dist = length(vec);
                     float dp = fmaxf(dot(h.sh.n, neg(dd)), 0.f);
                     float ep = dp != 0.f ? __fdiv_rn(__fmul_rn(__fmul_rn(Lt.pA, dist), dist), dp) : 0.f;
-                    if (sc.num_lights != 1) ep = __fdiv_rn(ep, (float)sc.num_lights);
+                    ep = with_pick_pdf(P, light, ep);
                     float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(pr.L.w, ep) : 1.f;
                     Lr = add(Lr, mul(scale(tp, w), le));
                 }
@@ -682,7 +711,8 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 float ldist = 0.f;
                 if (T == MAT_MIRROR || T == MAT_DIELECTRIC) {
                     // no NEE contribution, but an envmap pick still draws its numbers
-                    if (sc.env_light >= 0 && picked_light(sc, s_nee.x) == sc.env_light) (void)env_xi(g);
+                    float sx = s_nee.x;
+                    if (sc.env_light >= 0 && sc.num_lights > 0 && pick_light(P, sx) == sc.env_light) (void)env_xi(g);
                 } else {
                     float lpdf;
                     bool delta;

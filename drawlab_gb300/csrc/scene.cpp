@@ -39,25 +39,55 @@ inline HV hnorm(HV a) {
 inline HV hscale(HV a, float s) { return {a.x * s, a.y * s, a.z * s}; }
 inline HV ld(const float* p) { return {p[0], p[1], p[2]}; }
 
-// EnvironmentMap::activate + build_alias_map (src/tracer/emitter/envmap.cpp:
-// 59-141): the importance of a texel is its solid angle times max(r, g, b)
-// (float, as the reference computes it; its unqualified cos of a float is the
-// double cos); an alias table (Walker/Vose, one partition array, the
-// reference's steps) picks texels in proportion to it; pdf = max(r, g, b) /
+// Alias table over non-negative weights: the steps of the reference's
+// build_alias_map (src/tracer/emitter/envmap.cpp:111-141; one partition
+// array, small entries from the front, large from the back, each small entry
+// topped up from the current large one).  The normalised weights and the
+// residual chain (q[k] += q[j] - 1) run in double: in the reference's float a
+// long chain misstates a pick probability by up to tens of percent on maps
+// with a bright sun, and the pick would no longer follow the pdf.  Returns
+// the sum of the weights; with a zero sum every entry picks itself.
+double alias_table(const std::vector<double>& w, std::vector<double>& q, std::vector<unsigned>& alias) {
+    const unsigned size = (unsigned)w.size();
+    q.assign(size, 1.0);
+    alias.resize(size);
+    double sum = 0.0;
+    for (unsigned i = 0; i < size; ++i) sum += w[i];
+    for (unsigned i = 0; i < size; ++i) alias[i] = i;
+    if (!(sum > 0.0)) return 0.0;
+    for (unsigned i = 0; i < size; ++i) q[i] = (double)size * w[i] / sum;
+    std::vector<unsigned> part(size);
+    unsigned s = 0u, large = size;
+    for (unsigned i = 0; i < size; ++i) part[(q[i] < 1.0) ? (s++) : (--large)] = i;
+    for (s = 0; s < large && large < size; ++s) {
+        const unsigned j = part[s], k = part[large];
+        alias[j] = k;
+        q[k] += q[j] - 1.0;
+        large = (q[k] < 1.0) ? (large + 1u) : large;
+    }
+    return sum;
+}
+
+float4 alias_entry(double q, unsigned alias, float prob) {
+    float a;
+    std::memcpy(&a, &alias, 4);
+    return make_float4((float)q, a, prob, 0.f);
+}
+
+// EnvironmentMap::activate (src/tracer/emitter/envmap.cpp:59-110): the
+// importance of a texel is its solid angle times max(r, g, b) (float, as the
+// reference computes it; its unqualified cos of a float is the double cos);
+// the alias table picks texels in proportion to it; pdf = max(r, g, b) /
 // sum(importance) is the solid-angle density of a direction in the texel.
-// The sum and the table's residual chain (q[k] += q[j] - 1) run in double:
-// in the reference's float they misstate a texel's pick probability by up to
-// tens of percent on maps with a bright sun, and the pick would no longer
-// follow the pdf.  A map with zero importance everywhere gets pdf 0.
-void build_env_tables(const dl_light_desc& L, std::vector<float4>& tex, std::vector<float4>& accel) {
+// Returns sum(importance): the integral of max(r, g, b) over the sphere.
+double build_env_tables(const dl_light_desc& L, std::vector<float4>& tex, std::vector<float4>& accel) {
     const unsigned rx = (unsigned)L.env_width, ry = (unsigned)L.env_height, size = rx * ry;
     const float* px = L.env_rgb;
     const float pi = 3.14159265358979323846f;
     tex.resize(size);
     accel.resize(size);
-    std::vector<float> imp(size);
-    std::vector<double> q(size);
-    std::vector<unsigned> alias(size);
+    std::vector<double> imp(size), q;
+    std::vector<unsigned> alias;
     auto maxc = [&](unsigned i) { return std::max(px[3 * i], std::max(px[3 * i + 1], px[3 * i + 2])); };
     float cos_theta0 = 1.0f;
     const float step_phi = (float)(2.0 * (double)pi) / (float)rx;
@@ -67,34 +97,14 @@ void build_env_tables(const dl_light_desc& L, std::vector<float4>& tex, std::vec
         const float cos_theta1 = (float)std::cos((double)theta1);
         const float area = (cos_theta0 - cos_theta1) * step_phi;
         cos_theta0 = cos_theta1;
-        for (unsigned x = 0; x < rx; ++x) imp[y * rx + x] = area * maxc(y * rx + x);
+        for (unsigned x = 0; x < rx; ++x) imp[y * rx + x] = (double)(area * maxc(y * rx + x));
     }
-    double sum = 0.0;
-    for (unsigned i = 0; i < size; ++i) sum += imp[i];
-    if (sum > 0.0) {
-        for (unsigned i = 0; i < size; ++i) q[i] = (double)size * imp[i] / sum;
-        std::vector<unsigned> part(size);
-        unsigned s = 0u, large = size;
-        for (unsigned i = 0; i < size; ++i) part[(q[i] < 1.0) ? (s++) : (--large)] = alias[i] = i;
-        for (s = 0; s < large && large < size; ++s) {
-            const unsigned j = part[s], k = part[large];
-            alias[j] = k;
-            q[k] += q[j] - 1.0;
-            large = (q[k] < 1.0) ? (large + 1u) : large;
-        }
-    } else {
-        for (unsigned i = 0; i < size; ++i) {
-            q[i] = 1.0;
-            alias[i] = i;
-        }
-    }
+    const double sum = alias_table(imp, q, alias);
     for (unsigned i = 0; i < size; ++i) {
-        float a;
-        std::memcpy(&a, &alias[i], 4);
-        float pdf = sum > 0.0 ? (float)((double)maxc(i) / sum) : 0.0f;
-        accel[i] = make_float4((float)q[i], a, pdf, 0.f);
+        accel[i] = alias_entry(q[i], alias[i], sum > 0.0 ? (float)((double)maxc(i) / sum) : 0.0f);
         tex[i] = make_float4(px[3 * i], px[3 * i + 1], px[3 * i + 2], 0.f);
     }
+    return sum;
 }
 
 void check(bool ok, const std::string& msg) {
@@ -288,11 +298,12 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
         }
     }
     int env_light = -1;
+    double env_integral = 0.0;
     std::vector<float4> env_tex, env_accel;
     for (int l = 0; l < nl; l++) {
         if (lights[l].type != DL_LIGHT_ENVMAP) continue;
         env_light = l;
-        build_env_tables(lights[l], env_tex, env_accel);
+        env_integral = build_env_tables(lights[l], env_tex, env_accel);
     }
     if (env_tex.empty()) {
         env_tex.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
@@ -300,6 +311,52 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     }
     S->env_tex.upload(env_tex, st);
     S->env_accel.upload(env_accel, st);
+    // power-proportional emitter pick (DL_RENDER_POWER_LIGHT_PICK)
+    std::vector<double> power(std::max(nl, 1), 0.0), pq;
+    std::vector<unsigned> palias;
+    {
+        const double kPi = 3.14159265358979323846;
+        // bounding box of every vertex of every mesh; R = half its diagonal
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        bool any = false;
+        for (int i = 0; i < nm; i++)
+            for (int64_t k = 0; k < 3 * meshes[i].num_vertices; k++) {
+                lo[k % 3] = std::min(lo[k % 3], (double)meshes[i].positions[k]);
+                hi[k % 3] = std::max(hi[k % 3], (double)meshes[i].positions[k]);
+                any = true;
+            }
+        double r2 = 0.0;
+        if (any)
+            for (int k = 0; k < 3; k++) r2 += 0.25 * (hi[k] - lo[k]) * (hi[k] - lo[k]);
+        for (int l = 0; l < nl; l++) {
+            const dl_light_desc& L = lights[l];
+            double m = std::max(L.radiance[0], std::max(L.radiance[1], L.radiance[2]));
+            if (L.type == DL_LIGHT_AREA) {
+                double area = 0.0;
+                const dl_mesh_desc& me = meshes[L.mesh];
+                for (int64_t f = 0; f < me.num_triangles; f++) {
+                    HV p[3];
+                    for (int k = 0; k < 3; k++) p[k] = ld(me.positions + 3 * me.indices[3 * f + k]);
+                    area += (double)(0.5f * hlen(hcross(hsub(p[1], p[0]), hsub(p[2], p[0]))));
+                }
+                power[l] = kPi * area * std::max(m, 0.0);
+            } else if (L.type == DL_LIGHT_POINT) {
+                power[l] = 4.0 * kPi * std::max(m, 0.0);
+            } else if (L.type == DL_LIGHT_ENVMAP) {
+                power[l] = kPi * r2 * env_integral * (double)std::fabs(L.env_scale);
+            }
+        }
+        power.resize(std::max(nl, 1));
+        if (nl == 0) power[0] = 1.0;
+    }
+    std::vector<float4> pick(power.size());
+    {
+        double psum = alias_table(power, pq, palias);
+        for (size_t l = 0; l < power.size(); l++)
+            pick[l] = alias_entry(pq[l], palias[l],
+                                  psum > 0.0 ? (float)(power[l] / psum) : 1.0f / (float)power.size());
+    }
+    S->light_pick.upload(pick, st);
 
     S->nodes.upload(bvh.nodes, st);
     S->tris.upload(bvh.tris, st);
@@ -327,6 +384,7 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     D.num_tris = (int)ntri;
     D.num_lights = nl;
     D.cam = make_camera(*cam);
+    D.light_pick = S->light_pick.as<float4>();
     D.env_tex = S->env_tex.as<float4>();
     D.env_accel = S->env_accel.as<float4>();
     D.env_light = env_light;
@@ -350,7 +408,8 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     I.bvh_sah_cost = bvh.sah_cost;
     I.device_bytes = (int64_t)(S->nodes.bytes + S->tris.bytes + S->tri_vidx.bytes + S->normals.bytes +
                                S->meshes.bytes + S->materials.bytes + S->lights.bytes + S->emit_tris.bytes +
-                               S->emit_cdf.bytes + S->env_tex.bytes + S->env_accel.bytes);
+                               S->emit_cdf.bytes + S->env_tex.bytes + S->env_accel.bytes +
+                               S->light_pick.bytes);
     dl_render_opts& O = S->defaults;
     std::memset(&O, 0, sizeof(O));
     O.spp = 1;

@@ -205,7 +205,12 @@ enum dl_render_flags {
      * Off: the reference CPU form (no cosine, power-heuristic weight,
      * src/tracer/emitter/point.cpp:17-33, src/tracer/integrator/path.cpp:53). */
     DL_RENDER_FIX_POINT_LIGHT = 1u << 0,
-    /* Pick emitters by power through an alias table instead of uniformly. */
+    /* Pick the NEE emitter through an alias table in proportion to an
+     * estimate of its power -- area: pi * area * max(radiance); point:
+     * 4 pi * max(intensity); envmap: pi * R^2 * integral of max(radiance) over
+     * the sphere, R the radius of the scene's bounding sphere -- instead of
+     * uniformly (src/tracer/scene/scene.cpp:148-163).  The pick probability
+     * replaces 1/N in the NEE weight and in the MIS weights of emitter hits. */
     DL_RENDER_POWER_LIGHT_PICK = 1u << 1
 };
 

@@ -25,6 +25,10 @@
 //                                         include/optix/math/wrap.h:54-77,
 //                                         include/optix/math/onb.h:11-43
 //   point light with cosine (fix flag)    include/optix/light/point.h:15-42
+//   envmap emitter and miss shading       include/optix/light/envmap.h:25-94,
+//                                         src/tracer/emitter/envmap.cpp:59-141,
+//                                         src/optix/cuda/miss.cu:11-49
+// and the renderer's own option of a power-proportional emitter pick.
 //
 // Where the reference calls an unqualified libm function (cos, sin, atan,
 // log, exp, acos) on a float, C++ overload resolution picks the double
@@ -397,6 +401,7 @@ struct Light {
     std::vector<float> env_rgb;      // rows from the +y pole down
     std::vector<float> env_q, env_pdf;
     std::vector<uint32_t> env_alias;
+    double env_sum = 0.0;            // integral of max(r, g, b) over the sphere
 };
 
 struct Node {
@@ -432,6 +437,9 @@ struct Scene {
     std::vector<Material> mats;
     std::vector<Light> lights;
     int env_light = -1;
+    // power-proportional emitter pick (DL_RENDER_POWER_LIGHT_PICK)
+    std::vector<float> pick_q, pick_prob;
+    std::vector<uint32_t> pick_alias;
     std::vector<Node> nodes;
     int root = -1;
     Camera cam;
@@ -831,6 +839,7 @@ void env_build(Light& L) {
         }
         return;
     }
+    L.env_sum = sum;
     std::vector<double> q(size);
     for (uint32_t i = 0; i < size; ++i) q[i] = (double)size * imp[i] / sum;
     std::vector<uint32_t> part(size);
@@ -851,6 +860,7 @@ void env_build(Light& L) {
 // linear filter, wrap addressing, normalised coordinates
 V3 env_lookup(const Light& L, float u, float v) {
     const int W = L.env_w, H = L.env_h;
+    if (!std::isfinite(u) || !std::isfinite(v)) return V3();  // no direction
     u = u - std::floor(u);
     v = v - std::floor(v);
     float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
@@ -950,6 +960,23 @@ void sample_emitter(const Scene& sc, const Hit& its, P2 s, DirSample& ds, V3& sp
     };
     if (N == 0) {
         spec = V3();
+    } else if (flags & DL_RENDER_POWER_LIGHT_PICK) {
+        // alias pick: slot from s.x * N, coin from its fraction, reused
+        float u = s.x * (float)N;
+        size_t i = std::min((size_t)u, N - 1);
+        float coin = std::fmin(u - (float)i, 0.99999994f);
+        size_t idx = i;
+        if (coin < sc.pick_q[i]) {
+            s.x = coin / sc.pick_q[i];
+        } else {
+            s.x = (coin - sc.pick_q[i]) / (1.f - sc.pick_q[i]);
+            idx = sc.pick_alias[i];
+        }
+        const float pl = sc.pick_prob[idx];
+        spec = one(sc.lights[idx], s);
+        delta = sc.lights[idx].type == DL_LIGHT_POINT;
+        spec = spec / pl;
+        ds.pdf *= pl;
     } else if (N == 1) {
         spec = one(sc.lights[0], s);
         delta = sc.lights[0].type == DL_LIGHT_POINT;
@@ -968,7 +995,8 @@ void sample_emitter(const Scene& sc, const Hit& its, P2 s, DirSample& ds, V3& sp
     }
 }
 
-float pdf_emitter(const Scene& sc, int light, const DirSample& ds) {
+float pdf_emitter(const Scene& sc, int light, const DirSample& ds, uint32_t flags) {
+    if (flags & DL_RENDER_POWER_LIGHT_PICK) return emitter_pdf_direction(sc, sc.lights[light], ds) * sc.pick_prob[light];
     if (sc.lights.size() == 1) return emitter_pdf_direction(sc, sc.lights[0], ds);
     return emitter_pdf_direction(sc, sc.lights[light], ds) / sc.lights.size();
 }
@@ -1049,20 +1077,21 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
             if (lt >= 0) {
                 V3 le = emitter_eval(sc.lights[lt], its, -ray.d);
                 DirSample hs = make_ds(ray.o, its.p, its.sh.n);
-                float ep = pdf_emitter(sc, lt, hs);
+                float ep = pdf_emitter(sc, lt, hs, o.flags);
                 float bp = bsdf_pdf(bsdf, bq);
                 float w = is_diffuse(bsdf) ? mis(bp, ep) : 1.f;
                 result = result + mul(w * tp, le);
             }
         } else {
-            // miss.cu:28-44: envmap radiance, MIS-weighted after a diffuse bounce
-            if (sc.env_light >= 0) {
+            // miss.cu:28-44: envmap radiance, MIS-weighted after a diffuse
+            // bounce (a path with zero throughput adds nothing)
+            if (sc.env_light >= 0 && (tp.x != 0.f || tp.y != 0.f || tp.z != 0.f)) {
                 V3 le = env_eval(sc.lights[sc.env_light], ray.d);
                 float w = 1.f;
                 if (is_diffuse(bsdf)) {
                     DirSample hs;
                     hs.d = ray.d;
-                    w = mis(bsdf_pdf(bsdf, bq), pdf_emitter(sc, sc.env_light, hs));
+                    w = mis(bsdf_pdf(bsdf, bq), pdf_emitter(sc, sc.env_light, hs, o.flags));
                 }
                 result = result + mul(w * tp, le);
             }
@@ -1337,6 +1366,62 @@ void* orc_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
             return nullptr;
         }
         sc->lights.push_back(L);
+    }
+    // Power-proportional emitter pick, as the renderer defines it (no
+    // reference counterpart): area pi*A*max(L), point 4pi*max(I), envmap
+    // pi*R^2*integral*|scale| with R half the diagonal of the box of all
+    // vertices; alias table in double over these weights.
+    {
+        const double kPiD = 3.14159265358979323846;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        bool any = false;
+        for (const Mesh& m : sc->meshes)
+            for (size_t k = 0; k < m.V.size(); k++) {
+                lo[k % 3] = std::min(lo[k % 3], (double)m.V[k]);
+                hi[k % 3] = std::max(hi[k % 3], (double)m.V[k]);
+                any = true;
+            }
+        double r2 = 0.0;
+        if (any)
+            for (int k = 0; k < 3; k++) r2 += 0.25 * (hi[k] - lo[k]) * (hi[k] - lo[k]);
+        const size_t N = sc->lights.size();
+        std::vector<double> w(N, 0.0), q(N, 1.0);
+        sc->pick_alias.resize(N);
+        for (size_t l = 0; l < N; l++) {
+            const Light& L = sc->lights[l];
+            double m = std::max(L.radiance.x, std::max(L.radiance.y, L.radiance.z));
+            if (L.type == DL_LIGHT_AREA) {
+                double area = 0.0;
+                const Mesh& me = sc->meshes[L.mesh];
+                for (uint32_t f = 0; f < me.tri_count(); f++) area += (double)me.area(f);
+                w[l] = kPiD * area * std::max(m, 0.0);
+            } else if (L.type == DL_LIGHT_POINT) {
+                w[l] = 4.0 * kPiD * std::max(m, 0.0);
+            } else {
+                w[l] = kPiD * r2 * L.env_sum * (double)std::fabs(L.env_scale);
+            }
+        }
+        double sum = 0.0;
+        for (size_t l = 0; l < N; l++) sum += w[l];
+        for (size_t l = 0; l < N; l++) sc->pick_alias[l] = (uint32_t)l;
+        if (sum > 0.0) {
+            for (size_t l = 0; l < N; l++) q[l] = (double)N * w[l] / sum;
+            std::vector<uint32_t> part(N);
+            uint32_t s = 0u, large = (uint32_t)N;
+            for (uint32_t l = 0; l < N; l++) part[(q[l] < 1.0) ? (s++) : (--large)] = l;
+            for (s = 0; s < large && large < N; ++s) {
+                const uint32_t j = part[s], k = part[large];
+                sc->pick_alias[j] = k;
+                q[k] += q[j] - 1.0;
+                large = (q[k] < 1.0) ? (large + 1u) : large;
+            }
+        }
+        sc->pick_q.resize(N);
+        sc->pick_prob.resize(N);
+        for (size_t l = 0; l < N; l++) {
+            sc->pick_q[l] = (float)q[l];
+            sc->pick_prob[l] = sum > 0.0 ? (float)(w[l] / sum) : 1.0f / (float)N;
+        }
     }
     // OCTree::build (octree.cpp:135-151): meshes in scene order.
     BBox box;

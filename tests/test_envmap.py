@@ -108,3 +108,25 @@ def test_camera_rays_see_sky_or_background():
     sc0 = scenes.env_spheres(width=32, height=20, visual=0)
     L0, _ = po.OracleScene(sc0).li(abi.make_opts(max_depth=1, seed=1), xys)
     np.testing.assert_array_equal(L0, np.tile(np.float32([0.1, 0.2, 0.3]), (32, 1)))
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.reference_spheres(width=12, height=8),
+                                  lambda: scenes.env_spheres(width=12, height=8)])
+def test_power_light_pick_is_unbiased(make):
+    # the power-proportional emitter pick changes the variance, not the mean
+    # (with the point light in its unbiased form: the reference CPU form
+    # weights a delta light by MIS against the BSDF, so its expectation
+    # depends on the pick probability)
+    sc = make()
+    orc = po.OracleScene(sc)
+    spp = 512
+    xys = np.array([(x, y, s) for y in range(8) for x in range(12) for s in range(spp)], np.int32)
+    means, sig = [], []
+    fix = abi.DL_RENDER_FIX_POINT_LIGHT
+    for flags in (fix, fix | abi.DL_RENDER_POWER_LIGHT_PICK):
+        L, _ = orc.li(abi.make_opts(spp=spp, max_depth=4, seed=9 + flags, flags=flags), xys, threads=4)
+        L = L[np.isfinite(L).all(1)]
+        means.append(L.mean(0))
+        sig.append(L.std(0) / np.sqrt(len(L)))
+    z = np.abs(means[0] - means[1]) / np.sqrt(sig[0] ** 2 + sig[1] ** 2)
+    assert (z < 4).all(), (means, z)

@@ -54,6 +54,10 @@ LI_CASES = {
     "env_spheres": (lambda: scenes.env_spheres(width=64, height=40), dict(max_depth=8)),
     "env_only_bg": (lambda: scenes.env_spheres(width=64, height=40, with_area_light=False, visual=0),
                     dict(max_depth=6)),
+    "refspheres_power": (lambda: scenes.reference_spheres(width=64, height=40),
+                         dict(max_depth=8, flags=abi.DL_RENDER_POWER_LIGHT_PICK)),
+    "env_spheres_power": (lambda: scenes.env_spheres(width=64, height=40),
+                          dict(max_depth=8, flags=abi.DL_RENDER_POWER_LIGHT_PICK)),
 }
 
 
