@@ -156,6 +156,25 @@ class dl_traversal_counts(C.Structure):
     ]
 
 
+class dl_request(C.Structure):
+    _fields_ = [
+        ("scene", C.c_void_p),
+        ("opts", dl_render_opts),
+        ("rgb", C.POINTER(C.c_float)),
+        ("film_device", C.POINTER(C.c_float)),
+    ]
+
+
+class dl_tune_params(C.Structure):
+    _fields_ = [
+        ("paths_in_flight", C.c_int64),
+        ("traverse_ctas_per_sm", C.c_int32),
+        ("shade_ctas_per_sm", C.c_int32),
+        ("iterations_per_graph", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
 def make_opts(spp=1, max_depth=0, rr_depth=3, filter=DL_FILTER_GAUSSIAN, seed=0, flags=0,
               spp_offset=0, max_paths_in_flight=0) -> dl_render_opts:
     o = dl_render_opts()

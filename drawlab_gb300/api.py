@@ -45,6 +45,10 @@ SIGNATURES = {
     "dl_render_traversal_counts": (C.c_int, [_vp, _vp, _vp]),
     "dl_context_set_kernel_timing": (C.c_int, [_vp, C.c_int]),
     "dl_li_static": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
+    "dl_render_batch": (C.c_int, [_vp, _vp, _i32]),
+    "dl_context_get_tune": (C.c_int, [_vp, _vp]),
+    "dl_context_set_tune": (C.c_int, [_vp, _vp]),
+    "dl_autotune": (C.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
 }
 
 
@@ -116,6 +120,44 @@ class Context:
         s = abi.dl_stats()
         self.check(self.lib.dl_stats_get(self.h, C.byref(s)))
         return s
+
+    @staticmethod
+    def _requests(items):
+        reqs = (abi.dl_request * max(len(items), 1))()
+        outs = []
+        for i, (scene, opts) in enumerate(items):
+            rgb = np.empty((scene.height, scene.width, 3), np.float32)
+            outs.append(rgb)
+            reqs[i].scene = scene.h
+            reqs[i].opts = opts
+            reqs[i].rgb = rgb.ctypes.data_as(C.POINTER(C.c_float))
+            reqs[i].film_device = None
+        return reqs, outs
+
+    def render_batch(self, items) -> list:
+        """Render [(Scene, dl_render_opts), ...] in one wavefront; returns the
+        RGB images in order."""
+        reqs, outs = self._requests(items)
+        self.check(self.lib.dl_render_batch(self.h, C.cast(reqs, C.c_void_p), len(items)))
+        return outs
+
+    def get_tune(self) -> abi.dl_tune_params:
+        t = abi.dl_tune_params()
+        self.check(self.lib.dl_context_get_tune(self.h, C.byref(t)))
+        return t
+
+    def set_tune(self, t: abi.dl_tune_params):
+        self.check(self.lib.dl_context_set_tune(self.h, C.byref(t)))
+
+    def autotune(self, items, trial_spp: int = 0):
+        """Time launch shapes on [(Scene, opts), ...]; keeps and returns the
+        fastest (dl_tune_params) and the number of shapes timed."""
+        reqs, _ = self._requests(items)
+        t = abi.dl_tune_params()
+        n = C.c_int32()
+        self.check(self.lib.dl_autotune(self.h, C.cast(reqs, C.c_void_p), len(items), trial_spp, C.byref(t),
+                                        C.byref(n)))
+        return t, n.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -40,6 +40,9 @@ int guard(dl_context* ctx, F&& fn) {
 void need(bool ok, const char* what) {
     if (!ok) throw dl::Error(DL_ERR_INVALID_ARG, what);
 }
+void need(bool ok, const std::string& what) {
+    if (!ok) throw dl::Error(DL_ERR_INVALID_ARG, what);
+}
 
 void check_opts(const dl_render_opts* o) {
     need(o != nullptr, "opts is NULL");
@@ -321,6 +324,150 @@ int dl_render_traversal_counts(dl_scene* S, const dl_render_opts* opts, dl_trave
         out->extension_triangle_tests = (int64_t)rc.stat_tris_ext;
         out->shadow_node_visits = (int64_t)rc.stat_nodes_sh;
         out->shadow_triangle_tests = (int64_t)rc.stat_tris_sh;
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+// Validated batch items; requests without a device film get one in the
+// context's batch film buffer (offsets in floats in `film_off`, -1 when the
+// caller gave one).  trial_spp >= 0 overrides every request's spp (0: an
+// eighth of it, at least 1).
+std::vector<dl::BatchItem> batch_items(dl_context* ctx, const dl_request* reqs, int32_t n, bool outputs,
+                                       int trial_spp, std::vector<int64_t>& film_off) {
+    need(n >= 0 && (n == 0 || reqs != nullptr), "bad request array");
+    need(n <= (1 << 20), "at most 2^20 requests per batch");
+    std::vector<dl::BatchItem> items((size_t)n);
+    film_off.assign((size_t)n, -1);
+    int64_t floats = 0;
+    for (int32_t r = 0; r < n; r++) {
+        const dl_request& q = reqs[r];
+        need(q.scene != nullptr, "request " + std::to_string(r) + ": scene is NULL");
+        need(q.scene->ctx == ctx, "request " + std::to_string(r) + ": scene belongs to another context");
+        check_opts(&q.opts);
+        if (outputs) need(q.rgb || q.film_device, "request " + std::to_string(r) + ": no output");
+        items[r].scene = q.scene;
+        items[r].opts = q.opts;
+        if (trial_spp >= 0) items[r].opts.spp = trial_spp > 0 ? trial_spp : std::max(1, q.opts.spp / 8);
+        items[r].d_film = outputs ? q.film_device : nullptr;
+        if (!items[r].d_film) {
+            film_off[r] = floats;
+            floats += dl::film_floats(q.scene->dev.cam.w, q.scene->dev.cam.h, q.opts.filter);
+        }
+    }
+    ctx->render.batch_films.ensure((size_t)std::max<int64_t>(floats, 1) * 4);
+    for (int32_t r = 0; r < n; r++)
+        if (film_off[r] >= 0) items[r].d_film = ctx->render.batch_films.as<float>() + film_off[r];
+    return items;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dl_render_batch(dl_context* ctx, const dl_request* reqs, int32_t n) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    return guard(ctx, [&] {
+        std::vector<int64_t> off;
+        std::vector<dl::BatchItem> items = batch_items(ctx, reqs, n, true, -1, off);
+        if (n == 0) return;
+        dl::render_batch(ctx, items.data(), n, false);
+        size_t maxrgb = 0;
+        for (int32_t r = 0; r < n; r++)
+            if (reqs[r].rgb) maxrgb = std::max(maxrgb, (size_t)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h * 3);
+        ctx->render.rgb.ensure(std::max<size_t>(maxrgb, 1) * 4);
+        for (int32_t r = 0; r < n; r++) {
+            if (!reqs[r].rgb) continue;
+            dl_scene* S = items[r].scene;
+            size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;
+            dl::resolve_film(S, items[r].d_film, items[r].opts.filter, ctx->render.rgb.as<float>());
+            DL_CUDA(cudaMemcpyAsync(reqs[r].rgb, ctx->render.rgb.ptr, nrgb * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            DL_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+    });
+}
+
+int dl_context_get_tune(const dl_context* ctx, dl_tune_params* out) {
+    if (!ctx || !out) return DL_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    out->paths_in_flight = ctx->tune.paths_in_flight;
+    out->traverse_ctas_per_sm = ctx->tune.trav_ctas_per_sm;
+    out->shade_ctas_per_sm = ctx->tune.shade_ctas_per_sm;
+    out->iterations_per_graph = ctx->tune.iters_per_graph;
+    return DL_OK;
+}
+
+int dl_context_set_tune(dl_context* ctx, const dl_tune_params* t) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    return guard(ctx, [&] {
+        need(t != nullptr, "tune is NULL");
+        need(t->paths_in_flight >= 32 && t->paths_in_flight <= ((int64_t)1 << 28), "paths_in_flight out of range");
+        need(t->traverse_ctas_per_sm >= 1 && t->traverse_ctas_per_sm <= 16, "traverse_ctas_per_sm out of range");
+        need(t->shade_ctas_per_sm >= 1 && t->shade_ctas_per_sm <= 64, "shade_ctas_per_sm out of range");
+        need(t->iterations_per_graph >= 2 && t->iterations_per_graph <= 8 && t->iterations_per_graph % 2 == 0,
+             "iterations_per_graph must be 2, 4, 6 or 8");
+        ctx->tune.paths_in_flight = t->paths_in_flight;
+        ctx->tune.trav_ctas_per_sm = t->traverse_ctas_per_sm;
+        ctx->tune.shade_ctas_per_sm = t->shade_ctas_per_sm;
+        ctx->tune.iters_per_graph = t->iterations_per_graph;
+    });
+}
+
+int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t trial_spp, dl_tune_params* out,
+                int32_t* trials) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    return guard(ctx, [&] {
+        need(trial_spp >= 0, "trial_spp must be >= 0");
+        need(n >= 1, "autotune needs at least one request");
+        std::vector<int64_t> off;
+        std::vector<dl::BatchItem> items = batch_items(ctx, reqs, n, false, trial_spp, off);
+        for (auto& it : items) it.opts.max_paths_in_flight = 0;  // the pool size is what is tuned
+        const bool timing = ctx->kernel_timing;
+        ctx->kernel_timing = false;
+        int count = 0;
+        auto time_of = [&](const dl::TuneParams& tp) {
+            ctx->tune = tp;
+            dl::render_batch(ctx, items.data(), n, false);
+            count++;
+            return ctx->stats.render_ms;
+        };
+        dl::TuneParams best = ctx->tune;
+        try {
+            (void)time_of(best);  // warm-up: buffers, graph
+            double best_ms = time_of(best);
+            auto search = [&](auto setter, std::initializer_list<int64_t> values) {
+                for (int64_t v : values) {
+                    dl::TuneParams tp = best;
+                    setter(tp, v);
+                    double ms = time_of(tp);
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = tp;
+                    }
+                }
+            };
+            search([](dl::TuneParams& t, int64_t v) { t.paths_in_flight = v; },
+                   {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23});
+            search([](dl::TuneParams& t, int64_t v) { t.trav_ctas_per_sm = (int)v; }, {4, 6, 8});
+            search([](dl::TuneParams& t, int64_t v) { t.shade_ctas_per_sm = (int)v; }, {8, 16, 32});
+            search([](dl::TuneParams& t, int64_t v) { t.iters_per_graph = (int)v; }, {2, 4, 8});
+        } catch (...) {
+            ctx->tune = best;
+            ctx->kernel_timing = timing;
+            throw;
+        }
+        ctx->tune = best;
+        ctx->kernel_timing = timing;
+        if (trials) *trials = count;
+        if (out) {
+            std::memset(out, 0, sizeof(*out));
+            out->paths_in_flight = best.paths_in_flight;
+            out->traverse_ctas_per_sm = best.trav_ctas_per_sm;
+            out->shade_ctas_per_sm = best.shade_ctas_per_sm;
+            out->iterations_per_graph = best.iters_per_graph;
+        }
     });
 }
 

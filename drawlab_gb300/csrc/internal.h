@@ -84,6 +84,16 @@ struct HostBuf {
 
 constexpr int kNumMaterialTypes = 5;
 
+// Launch shape of the wavefront, chosen by dl_autotune (these defaults
+// otherwise): path slots in flight, resident CTAs per SM of the traversal
+// kernels and of the shading kernels, iterations per captured graph (even).
+struct TuneParams {
+    int64_t paths_in_flight = (int64_t)1 << 22;
+    int trav_ctas_per_sm = 8;
+    int shade_ctas_per_sm = 16;
+    int iters_per_graph = 4;
+};
+
 // A queue length that kernels bump with atomics, alone in its 128-byte line:
 // atomics on one line serialise in one L2 slice, so the hot counters are
 // spread over separate lines (and so over slices).
@@ -119,6 +129,9 @@ struct RenderBuffers {
     DevBuf sh_o, sh_d, sh_c;
     DevBuf counters, invalid;
     DevBuf samples;   // per-path radiance of the current sample chunk (film gather input)
+    DevBuf requests;  // batch: the pass's request table
+    HostBuf host_requests;
+    DevBuf batch_films;  // batch: films of requests without a caller film
     DevBuf film;      // internal film when the caller gives no device film
     DevBuf rgb;       // resolved image
     DevBuf li_xys, li_out, li_pos;
@@ -144,6 +157,7 @@ struct dl_context {
     dl::RenderBuffers render;
     dl::TraceBuffers trace;
     int num_sms = 0;
+    dl::TuneParams tune;
     bool kernel_timing = false;
     std::vector<cudaEvent_t> timing_events;  // created on first timed render
     // CUDA graph of one batch of wavefront iterations, reused while the

@@ -36,6 +36,7 @@
 
 #include "device.cuh"
 #include "internal.h"
+#include "scene.h"
 
 namespace dl {
 
@@ -63,8 +64,25 @@ constexpr size_t kSlotBytes = 4 * 32 + 8 + 3 * 16 + 4 * (2 + kNumMaterialTypes +
 
 constexpr int kMissQueue = kNumMaterialTypes;  // queue index of rays that hit nothing
 
-struct RenderParams {
+// One render request: a scene and its render options.  A single render has
+// one request, carried in the kernel parameters; a batch has a table of them
+// in device memory and every path carries its request's index (in the path
+// flags, in the ray records' w slot).
+struct DevRequest {
     DevScene sc;
+    unsigned long long pid_first;  // the request's first path index in the current pass
+    int spp_offset;                // sample index of its first sample in the pass
+    int max_depth;
+    int rr_depth;
+    unsigned int flags;
+    unsigned long long seed_mix;
+};
+constexpr int kReqShift = 8;  // path flags: request index << kReqShift | PathFlags
+
+struct RenderParams {
+    DevRequest r0;                 // the request of a single render
+    const DevRequest* reqs;        // batch: request table (pid_first ascending)
+    int num_reqs;
     RayRec* ray;
     PathRec* path;
     MetaRec* meta;
@@ -82,12 +100,23 @@ struct RenderParams {
     float* li_L;
     float* li_pos;
     unsigned long long total_paths;
-    int spp_offset;
-    int max_depth;
-    int rr_depth;
-    unsigned int flags;
-    unsigned long long seed_mix;
 };
+
+template <bool kMulti>
+__device__ __forceinline__ const DevRequest& request(const RenderParams& P, int rid) {
+    if (kMulti) return P.reqs[rid];
+    return P.r0;
+}
+
+// Request of batch path `pid`: the last request whose first path is <= pid.
+__device__ __forceinline__ int find_request(const RenderParams& P, unsigned long long pid) {
+    int lo = 0, hi = P.num_reqs;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (P.reqs[mid].pid_first <= pid) lo = mid; else hi = mid;
+    }
+    return lo;
+}
 
 // ------------------------------------------------------------ warp helpers
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
@@ -127,22 +156,28 @@ __device__ __forceinline__ unsigned long long path_index(const int4& m) {
 }
 
 // Start path `pid` in `slot`: camera sample and ray (cpu_renderer.cpp:36-44).
+// Ray records carry the request index in o.w (every render ray starts at
+// tmin = kRayEps).
+template <bool kMulti>
 __device__ void start_path(const RenderParams& P, int slot, unsigned long long pid) {
-    const DevCamera& cam = P.sc.cam;
+    const int rid = kMulti ? find_request(P, pid) : 0;
+    const DevRequest& R = request<kMulti>(P, rid);
+    const DevCamera& cam = R.sc.cam;
     int x, y, s;
     if (P.mode == 1) {
         x = P.xys[3 * pid];
         y = P.xys[3 * pid + 1];
         s = P.xys[3 * pid + 2];
     } else {
+        unsigned long long local = pid - R.pid_first;
         unsigned long long npix = (unsigned long long)cam.w * cam.h;
-        unsigned long long pix = pid % npix;
-        s = (int)(pid / npix) + P.spp_offset;
+        unsigned long long pix = local % npix;
+        s = (int)(local / npix) + R.spp_offset;
         x = (int)(pix % cam.w);
         y = (int)(pix / cam.w);
     }
     Pcg32 g;
-    seed_path(g, P.seed_mix, cam.w, cam.h, x, y, s);
+    seed_path(g, R.seed_mix, cam.w, cam.h, x, y, s);
     float2 ps = g.next2d();
     ps.x = __fadd_rn((float)x, ps.x);
     ps.y = __fadd_rn((float)y, ps.y);
@@ -150,7 +185,7 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     float3 o, d;
     camera_ray(cam, ps, o, d);
     RayRec r;
-    r.o = make_float4(o.x, o.y, o.z, kRayEps);
+    r.o = make_float4(o.x, o.y, o.z, __int_as_float(rid));
     r.d = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
     P.ray[slot] = r;
     PathRec pr;
@@ -158,7 +193,7 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     pr.L = make_float4(0.f, 0.f, 0.f, 0.f);
     P.path[slot] = pr;
     MetaRec mr;
-    mr.m = make_int4(0, PF_CAMERA, (int)(pid & 0xffffffffu), (int)(pid >> 32));
+    mr.m = make_int4(0, PF_CAMERA | (rid << kReqShift), (int)(pid & 0xffffffffu), (int)(pid >> 32));
     mr.rng = store_rng(g);
     P.meta[slot] = mr;
     if (P.mode == 1) P.pos[slot] = ps;
@@ -194,10 +229,11 @@ __device__ __forceinline__ void add_to_sample(const RenderParams& P, unsigned lo
 
 // Claim new path indices for the lanes in `want`, start them; returns true
 // for lanes that now hold a fresh camera ray.
+template <bool kMulti>
 __device__ __forceinline__ bool regenerate(const RenderParams& P, int slot, bool want) {
     unsigned long long pid = warp_claim(&P.cnt->next_path, want);
     bool ok = want && pid < P.total_paths;
-    if (ok) start_path(P, slot, pid);
+    if (ok) start_path<kMulti>(P, slot, pid);
     return ok;
 }
 
@@ -259,10 +295,10 @@ __device__ __forceinline__ void sample_area(const DevScene& sc, const DevLight& 
 // to [0, 1) for reuse: uniformly (scene.cpp:148-163), or, with
 // DL_RENDER_POWER_LIGHT_PICK, through the power alias table (slot from the
 // number, alias coin from its fraction).
-__device__ __forceinline__ int pick_light(const RenderParams& P, float& sx) {
-    const DevScene& sc = P.sc;
+__device__ __forceinline__ int pick_light(const DevRequest& R, float& sx) {
+    const DevScene& sc = R.sc;
     const int N = sc.num_lights;
-    if (!(P.flags & DL_RENDER_POWER_LIGHT_PICK)) {
+    if (!(R.flags & DL_RENDER_POWER_LIGHT_PICK)) {
         if (N <= 1) return 0;
         int idx = min((int)__fmul_rn(sx, (float)N), N - 1);
         sx = __fsub_rn(__fmul_rn(sx, (float)N), (float)idx);
@@ -282,9 +318,9 @@ __device__ __forceinline__ int pick_light(const RenderParams& P, float& sx) {
 
 // pdf of direction sample `pdf` of emitter `l` times its pick probability
 // (pdfEmitterDirection, scene.cpp:171-179).
-__device__ __forceinline__ float with_pick_pdf(const RenderParams& P, int l, float pdf) {
-    if (P.flags & DL_RENDER_POWER_LIGHT_PICK) return __fmul_rn(pdf, __ldg(P.sc.light_pick + l).z);
-    return P.sc.num_lights != 1 ? __fdiv_rn(pdf, (float)P.sc.num_lights) : pdf;
+__device__ __forceinline__ float with_pick_pdf(const DevRequest& R, int l, float pdf) {
+    if (R.flags & DL_RENDER_POWER_LIGHT_PICK) return __fmul_rn(pdf, __ldg(R.sc.light_pick + l).z);
+    return R.sc.num_lights != 1 ? __fdiv_rn(pdf, (float)R.sc.num_lights) : pdf;
 }
 
 // Three fresh numbers for an envmap NEE sample, drawn after the NEE 2D sample.
@@ -299,9 +335,9 @@ __device__ __forceinline__ float3 env_xi(Pcg32& g) {
 // Scene::sampleEmitterDirection without the visibility test (the caller
 // traces the shadow ray).  Returns the unoccluded spectrum.  An envmap pick
 // draws three more numbers from `g`.
-__device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 its_p, float3 sh_n, float2 s,
+__device__ __forceinline__ float3 sample_emitter(const DevRequest& R, float3 its_p, float3 sh_n, float2 s,
                                                  Pcg32& g, float3& d, float& dist, float& pdf, bool& delta) {
-    const DevScene& sc = P.sc;
+    const DevScene& sc = R.sc;
     int N = sc.num_lights;
     float3 zero = f3(0.f, 0.f, 0.f);
     delta = false;
@@ -309,7 +345,7 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     dist = 0.f;
     d = zero;
     if (N == 0) return zero;
-    const int idx = pick_light(P, s.x);
+    const int idx = pick_light(R, s.x);
     const DevLight& L = sc.lights[idx];
     float3 spec;
     if (L.type == LIGHT_AREA) {
@@ -329,7 +365,7 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
         pdf = 1.f;
         delta = true;
         float inv = __fdiv_rn(1.0f, dist);
-        if (P.flags & DL_RENDER_FIX_POINT_LIGHT) {
+        if (R.flags & DL_RENDER_FIX_POINT_LIGHT) {
             float c = fmaxf(dot(sh_n, d), 0.f);
             spec = c > 0.f ? scale(scale(scale(ld3(L.radiance), c), inv), inv) : zero;
         } else {
@@ -341,7 +377,7 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
     } else {
         spec = zero;
     }
-    if (P.flags & DL_RENDER_POWER_LIGHT_PICK) {
+    if (R.flags & DL_RENDER_POWER_LIGHT_PICK) {
         const float pl = __ldg(sc.light_pick + idx).z;
         spec = divs(spec, pl);
         pdf = __fmul_rn(pdf, pl);
@@ -353,12 +389,13 @@ __device__ __forceinline__ float3 sample_emitter(const RenderParams& P, float3 i
 }
 
 // ---------------------------------------------------------------- kernels
+template <bool kMulti>
 __global__ void k_init(RenderParams P, int capacity) {
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < capacity;
          i0 += gridDim.x * blockDim.x) {
         int slot = i0 + lane_id();
         bool active = slot < capacity;
-        bool ok = regenerate(P, slot, active);
+        bool ok = regenerate<kMulti>(P, slot, active);
         int e = warp_push(&P.cnt->ext[0], ok);
         if (ok) P.ext_q[0][e] = slot;
     }
@@ -382,10 +419,9 @@ constexpr unsigned kFetchChunk = 32;
 constexpr int kTraverseWarps = 4;  // 128 threads
 constexpr int kStage = 64;         // staged entries per warp and destination (flushed at 32)
 
-template <bool kCount, bool kAny>
+template <bool kCount, bool kAny, bool kMulti>
 __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     const int q = p ^ 1;
-    const DevScene& sc = P.sc;
     const int n = kAny ? P.cnt->shadow[p] : P.cnt->ext[p];
     unsigned int* work = kAny ? &P.cnt->work_sh : &P.cnt->work_ext;
     constexpr int kDests = kAny ? 1 : kNumMaterialTypes + 1;
@@ -417,6 +453,10 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     rb.idir = o;
     rb.ood = o;
     int stack[kStackSize];
+    int rid = 0;  // the ray's request
+    const float4* nodes = P.r0.sc.nodes;
+    const float4* tris = P.r0.sc.tris;
+    int ntris = P.r0.sc.num_tris;
     unsigned c_next = 0, c_end = 0;  // the warp's reserved queue entries [c_next, c_end)
     for (;;) {
         bool need = !has && !exhausted;
@@ -450,10 +490,17 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                     }
                     o = xyz(ro);
                     d = xyz(rd);
-                    tmin = ro.w;
+                    tmin = kRayEps;
                     tmax = rd.w;
+                    if (kMulti) {
+                        rid = __float_as_int(ro.w);
+                        const DevScene& rs = P.reqs[rid].sc;
+                        nodes = rs.nodes;
+                        tris = rs.tris;
+                        ntris = rs.num_tris;
+                    }
                     rb = make_raybox(o, d);
-                    node = sc.num_tris > 0 ? 0 : kDone;
+                    node = ntris > 0 ? 0 : kDone;
                     sp = 0;
                     hit_tri = -1;
                     has = true;
@@ -468,7 +515,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
         if (has) {
             // descend inner nodes until a leaf (or the end of the traversal)
             while (node >= 0 && node != kDone) {
-                const float4* np = sc.nodes + 4 * node;
+                const float4* np = nodes + 4 * node;
                 float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
                 int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
                 if (kCount) nn++;
@@ -497,7 +544,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 int first = ref >> 4, count = (ref & 15) + 1;
                 bool any = false;
                 for (int k = 0; k < count; k++) {
-                    const float4* tp = sc.tris + 3 * (first + k);
+                    const float4* tp = tris + 3 * (first + k);
                     float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
                     if (kCount) nt++;
                     float t, u, v;
@@ -540,6 +587,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                     hr.pad = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (hit_tri >= 0) {
                         hr.h = make_float4(ht, hu, hv, __int_as_float(hit_tri));
+                        const DevScene& sc = request<kMulti>(P, rid).sc;
                         int mesh = __ldg(sc.tri_vidx + hit_tri).w;
                         dest = sc.materials[sc.meshes[mesh].material].type;
                     } else {
@@ -606,9 +654,9 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
 // background colour; later rays weight it by MIS against the BSDF pdf after
 // a diffuse bounce).  Store the sample, then start new camera paths in the
 // freed slots.
+template <bool kMulti>
 __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
-    const DevScene& sc = P.sc;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
     const int n = P.cnt->mat[p][kMissQueue].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -618,6 +666,8 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
         if (active) {
             PathRec pr = P.path[slot];
             int4 m = P.meta[slot].m;
+            const DevRequest& R = request<kMulti>(P, m.y >> kReqShift);
+            const DevScene& sc = R.sc;
             float3 L = f3(pr.L.x, pr.L.y, pr.L.z);
             if (sc.env_light >= 0) {
                 float3 dir = xyz(P.ray[slot].d);
@@ -628,7 +678,7 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
                     float w = 1.f;
                     if (m.y & PF_PREV_DIFFUSE) {
                         float ep = env_pdf(sc, dir);
-                        ep = with_pick_pdf(P, sc.env_light, ep);
+                        ep = with_pick_pdf(R, sc.env_light, ep);
                         w = mis_weight(pr.L.w, ep);
                     }
                     L = add(L, mul(scale(f3(pr.tp.x, pr.tp.y, pr.tp.z), w), le));
@@ -636,7 +686,7 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
             }
             store_sample(P, path_index(m), L, slot);
         }
-        bool ok = regenerate(P, slot, active);
+        bool ok = regenerate<kMulti>(P, slot, active);
         int e = warp_push(&P.cnt->ext[q], ok);
         if (ok) P.ext_q[q][e] = slot;
     }
@@ -649,10 +699,9 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 // starts a new camera path at once; a shadow ray it emitted on the way adds
 // to the stored sample when traced.  Mirror and dielectric still draw the NEE
 // sample (their eval and pdf are zero: no contribution, no shadow ray).
-template <int T>
+template <int T, bool kMulti>
 __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
     const int q = p ^ 1;
-    const DevScene& sc = P.sc;
     const int n = P.cnt->mat[p][T].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
         int i = i0 + lane_id();
@@ -672,6 +721,9 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             float3 Lr = f3(pr.L.x, pr.L.y, pr.L.z);
             float3 dir = xyz(ray.d);
             int depth = mr.m.x, flags = mr.m.y;
+            const int rid = flags >> kReqShift;
+            const DevRequest& R = request<kMulti>(P, rid);
+            const DevScene& sc = R.sc;
             HitInfo h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
             int light = sc.meshes[h.mesh].light;
             if (flags & PF_CAMERA) {
@@ -686,18 +738,18 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     float dist = length(vec);
                     float dp = fmaxf(dot(h.sh.n, neg(dd)), 0.f);
                     float ep = dp != 0.f ? __fdiv_rn(__fmul_rn(__fmul_rn(Lt.pA, dist), dist), dp) : 0.f;
-                    ep = with_pick_pdf(P, light, ep);
+                    ep = with_pick_pdf(R, light, ep);
                     float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(pr.L.w, ep) : 1.f;
                     Lr = add(Lr, mul(scale(tp, w), le));
                 }
-                if (depth > P.rr_depth) {
+                if (depth > R.rr_depth) {
                     float pq = fminf(maxc(scale(scale(tp, eta), eta)), 0.99f);
                     if (g.next_float() > pq) done = true;
                     else tp = divs(tp, pq);
                 }
                 depth += 1;
             }
-            if (!done && P.max_depth > 0 && depth >= P.max_depth) done = true;
+            if (!done && R.max_depth > 0 && depth >= R.max_depth) done = true;
             float prev_pdf = pr.L.w;
             int target = slot;
             if (!done) {
@@ -712,11 +764,11 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 if (T == MAT_MIRROR || T == MAT_DIELECTRIC) {
                     // no NEE contribution, but an envmap pick still draws its numbers
                     float sx = s_nee.x;
-                    if (sc.env_light >= 0 && sc.num_lights > 0 && pick_light(P, sx) == sc.env_light) (void)env_xi(g);
+                    if (sc.env_light >= 0 && sc.num_lights > 0 && pick_light(R, sx) == sc.env_light) (void)env_xi(g);
                 } else {
                     float lpdf;
                     bool delta;
-                    float3 espec = sample_emitter(P, h.p, h.sh.n, s_nee, g, ld, ldist, lpdf, delta);
+                    float3 espec = sample_emitter(R, h.p, h.sh.n, s_nee, g, ld, ldist, lpdf, delta);
                     if (__fadd_rn(__fadd_rn(espec.x, espec.y), espec.z) > 0.f && lpdf > 0.f) {
                         BRec q1;
                         q1.wi = wi;
@@ -725,7 +777,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                         q1.eta = 1.f;
                         float3 bv = bsdf_eval<T>(m, q1);
                         float bp = bsdf_pdf<T>(m, q1);
-                        float w = (delta && (P.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
+                        float w = (delta && (R.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
                         c = mul(mul(scale(tp, w), bv), espec);
                         emit = c.x != 0.f || c.y != 0.f || c.z != 0.f;
                     }
@@ -739,21 +791,21 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 tp = mul(tp, f);
                 eta = __fmul_rn(eta, q2.eta);
                 prev_pdf = bsdf_pdf<T>(m, q2);
-                flags = is_diffuse(T) ? PF_PREV_DIFFUSE : 0;
+                flags = (rid << kReqShift) | (is_diffuse(T) ? PF_PREV_DIFFUSE : 0);
                 float3 nd = to_world(fr, q2.wo);
                 if (T == MAT_ANISO_GGX) nd = normalize(nd);
                 if (tp.x == 0.f && tp.y == 0.f && tp.z == 0.f) {
                     done = true;  // every later contribution is zero
                 } else {
                     RayRec nr;
-                    nr.o = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
+                    nr.o = make_float4(h.p.x, h.p.y, h.p.z, __int_as_float(rid));
                     nr.d = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
                     P.ray[slot] = nr;
                     cont = true;
                 }
                 if (emit) {
                     if (done) target = -1 - (int)pid;  // lands in the stored sample
-                    sh_o = make_float4(h.p.x, h.p.y, h.p.z, kRayEps);
+                    sh_o = make_float4(h.p.x, h.p.y, h.p.z, __int_as_float(rid));
                     sh_d = make_float4(ld.x, ld.y, ld.z, __fsub_rn(ldist, kRayEps));
                     sh_c = make_float4(c.x, c.y, c.z, __int_as_float(target));
                 }
@@ -777,7 +829,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             P.sh_d[sp] = sh_d;
             P.sh_c[sp] = sh_c;
         }
-        bool fresh = regenerate(P, slot, done);
+        bool fresh = regenerate<kMulti>(P, slot, done);
         bool push = cont || fresh;
         int e = warp_push(&P.cnt->ext[q], push);
         if (push) P.ext_q[q][e] = slot;
@@ -940,46 +992,47 @@ size_t RenderBuffers::device_bytes() const {
     return s;
 }
 
-constexpr int kBatch = 4;  // iterations per counter check and per captured graph (even)
 constexpr int kKernelsPerIteration = 8;
 
-// Launches one wavefront iteration (8 kernels).  `ev`, when given, holds 8
-// events bracketing extend, shadow, the material kernels, miss (kernels then
-// run one after another).  Otherwise, with `fj` given, the miss kernel and
-// the five material kernels (disjoint slots and queues) run concurrently on
-// the context's side streams, joined before the next iteration.
-static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, bool count, cudaEvent_t* ev,
-                             const dl_context* fj) {
-    const int tb = sms * 8, wb = sms * 16, th = 128;
+// Launches one wavefront iteration (8 kernels) with the context's launch
+// shape.  `ev`, when given, holds 8 events bracketing extend, shadow, the
+// material kernels, miss (kernels then run one after another).  Otherwise,
+// with `fj` given, the miss kernel and the five material kernels (disjoint
+// slots and queues) run concurrently on the context's side streams, joined
+// before the next iteration.
+template <bool kMulti>
+static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, const TuneParams& tp,
+                             bool count, cudaEvent_t* ev, const dl_context* fj) {
+    const int tb = sms * tp.trav_ctas_per_sm, wb = sms * tp.shade_ctas_per_sm, th = 128;
     if (ev) cudaEventRecord(ev[0], st);
-    if (count) k_traverse<true, false><<<tb, th, 0, st>>>(P, p);
-    else k_traverse<false, false><<<tb, th, 0, st>>>(P, p);
+    if (count) k_traverse<true, false, kMulti><<<tb, th, 0, st>>>(P, p);
+    else k_traverse<false, false, kMulti><<<tb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[1], st); cudaEventRecord(ev[2], st); }
-    if (count) k_traverse<true, true><<<tb, th, 0, st>>>(P, p);
-    else k_traverse<false, true><<<tb, th, 0, st>>>(P, p);
+    if (count) k_traverse<true, true, kMulti><<<tb, th, 0, st>>>(P, p);
+    else k_traverse<false, true, kMulti><<<tb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[6], st); }
     if (!ev && fj) {
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
-        k_miss<<<wb, th, 0, st>>>(P, p);
-        k_material<MAT_DIFFUSE><<<wb, th, 0, fj->aux[0]>>>(P, p);
-        k_material<MAT_MIRROR><<<wb, th, 0, fj->aux[1]>>>(P, p);
-        k_material<MAT_DIELECTRIC><<<wb, th, 0, fj->aux[2]>>>(P, p);
-        k_material<MAT_MICROFACET><<<wb, th, 0, fj->aux[3]>>>(P, p);
-        k_material<MAT_ANISO_GGX><<<wb, th, 0, fj->aux[4]>>>(P, p);
+        k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
+        k_material<MAT_DIFFUSE, kMulti><<<wb, th, 0, fj->aux[0]>>>(P, p);
+        k_material<MAT_MIRROR, kMulti><<<wb, th, 0, fj->aux[1]>>>(P, p);
+        k_material<MAT_DIELECTRIC, kMulti><<<wb, th, 0, fj->aux[2]>>>(P, p);
+        k_material<MAT_MICROFACET, kMulti><<<wb, th, 0, fj->aux[3]>>>(P, p);
+        k_material<MAT_ANISO_GGX, kMulti><<<wb, th, 0, fj->aux[4]>>>(P, p);
         for (int i = 0; i < dl_context::kAux; i++) {
             cudaEventRecord(fj->join_ev[i], fj->aux[i]);
             cudaStreamWaitEvent(st, fj->join_ev[i], 0);
         }
         return;
     }
-    k_miss<<<wb, th, 0, st>>>(P, p);
+    k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[7], st); cudaEventRecord(ev[4], st); }
-    k_material<MAT_DIFFUSE><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_MIRROR><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_DIELECTRIC><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_MICROFACET><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_ANISO_GGX><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_DIFFUSE, kMulti><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_MIRROR, kMulti><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_DIELECTRIC, kMulti><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_MICROFACET, kMulti><<<wb, th, 0, st>>>(P, p);
+    k_material<MAT_ANISO_GGX, kMulti><<<wb, th, 0, st>>>(P, p);
     if (ev) cudaEventRecord(ev[5], st);
 }
 
@@ -1021,36 +1074,54 @@ int64_t film_floats(int w, int h, int filter) {
     return (int64_t)(w + 2 * b) * (h + 2 * b) * 4;
 }
 
-static void common_params(RenderParams& P, dl_scene* S, const dl_render_opts& o) {
-    P.sc = S->dev;
-    P.spp_offset = o.spp_offset;
-    P.max_depth = o.max_depth;
-    P.rr_depth = o.rr_depth;
-    P.flags = o.flags;
-    P.seed_mix = splitmix64(o.seed);
+static DevRequest make_request(dl_scene* S, const dl_render_opts& o) {
+    DevRequest R;
+    std::memset(&R, 0, sizeof(R));
+    R.sc = S->dev;
+    R.pid_first = 0;
+    R.spp_offset = o.spp_offset;
+    R.max_depth = o.max_depth;
+    R.rr_depth = o.rr_depth;
+    R.flags = o.flags;
+    R.seed_mix = splitmix64(o.seed);
+    return R;
 }
 
-// Wavefront loop over the paths [0, P.total_paths) of one chunk, until every
-// path and every shadow ray has finished.  Adds the chunk's counters into
-// `acc` and per-kernel times into kms.
-static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool count_traversal, double* kms,
-                          int64_t& launches, int64_t& iters, RenderCounters& acc) {
+// Wavefront loop over the paths [0, P.total_paths) of one pass, until every
+// path and every shadow ray has finished.  Adds the pass's counters into
+// `acc` and per-kernel times into kms.  `multi`: paths of a request table.
+static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool multi, bool count_traversal,
+                          double* kms, int64_t& launches, int64_t& iters, RenderCounters& acc) {
     cudaStream_t st = ctx->stream;
     RenderBuffers& B = ctx->render;
+    const TuneParams tp = ctx->tune;
+    const int batch = tp.iters_per_graph;
     const unsigned long long total = P.total_paths;
     DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     const bool timing = ctx->kernel_timing;
     const bool use_graph = !timing && !count_traversal;
-    if (timing && ctx->timing_events.empty()) {
-        ctx->timing_events.resize(8 * kBatch);
-        for (auto& e : ctx->timing_events) DL_CUDA(cudaEventCreate(&e));
+    if (timing && (int)ctx->timing_events.size() < 8 * batch) {
+        size_t have = ctx->timing_events.size();
+        ctx->timing_events.resize(8 * batch);
+        for (size_t k = have; k < ctx->timing_events.size(); k++) DL_CUDA(cudaEventCreate(&ctx->timing_events[k]));
     }
+    auto iteration = [&](int k, bool count, cudaEvent_t* ev) {
+        if (multi) launch_iteration<true>(P, k & 1, st, sms, tp, count, ev, ctx);
+        else launch_iteration<false>(P, k & 1, st, sms, tp, count, ev, ctx);
+    };
     if (use_graph) {
-        std::vector<unsigned char> key(sizeof(P) + sizeof(int) + sizeof(cudaStream_t));
-        std::memcpy(key.data(), &P, sizeof(P));
-        std::memcpy(key.data() + sizeof(P), &sms, sizeof(int));
-        std::memcpy(key.data() + sizeof(P) + sizeof(int), &st, sizeof(cudaStream_t));
+        std::vector<unsigned char> key(sizeof(P) + sizeof(int) + sizeof(cudaStream_t) + sizeof(TuneParams) + 1);
+        unsigned char* kp = key.data();
+        std::memcpy(kp, &P, sizeof(P));
+        kp += sizeof(P);
+        std::memcpy(kp, &sms, sizeof(int));
+        kp += sizeof(int);
+        std::memcpy(kp, &st, sizeof(cudaStream_t));
+        kp += sizeof(cudaStream_t);
+        std::memcpy(kp, &tp, sizeof(TuneParams));
+        kp += sizeof(TuneParams);
+        *kp = multi ? 1 : 0;
         if (!ctx->graph_exec || key != ctx->graph_key) {
             if (ctx->graph_exec) {
                 cudaGraphExecDestroy(ctx->graph_exec);
@@ -1058,7 +1129,7 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
             }
             cudaGraph_t g = nullptr;
             DL_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr, ctx);
+            for (int k = 0; k < batch; k++) iteration(k, false, nullptr);
             DL_CUDA(cudaStreamEndCapture(st, &g));
             cudaError_t e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
             cudaGraphDestroy(g);
@@ -1069,24 +1140,24 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
             ctx->graph_key = key;
         }
     }
-    k_init<<<sms * 16, 128, 0, st>>>(P, (int)cap);
+    if (multi) k_init<true><<<sms * 16, 128, 0, st>>>(P, (int)cap);
+    else k_init<false><<<sms * 16, 128, 0, st>>>(P, (int)cap);
     launches += 1;
     RenderCounters* hc = B.host_counters.as<RenderCounters>();
     for (;;) {
         if (use_graph) {
             DL_CUDA(cudaGraphLaunch(ctx->graph_exec, st));
         } else {
-            for (int k = 0; k < kBatch; k++)
-                launch_iteration(P, k & 1, st, sms, count_traversal, timing ? &ctx->timing_events[8 * k] : nullptr,
-                                 ctx);
+            for (int k = 0; k < batch; k++)
+                iteration(k, count_traversal, timing ? &ctx->timing_events[8 * k] : nullptr);
         }
-        iters += kBatch;
-        launches += kBatch * kKernelsPerIteration;
+        iters += batch;
+        launches += batch * kKernelsPerIteration;
         DL_CUDA(cudaGetLastError());
         DL_CUDA(cudaMemcpyAsync(hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st));
         DL_CUDA(cudaStreamSynchronize(st));
         if (timing) {
-            for (int k = 0; k < kBatch; k++)
+            for (int k = 0; k < batch; k++)
                 for (int j = 0; j < 4; j++) {
                     float ms = 0.f;
                     DL_CUDA(cudaEventElapsedTime(&ms, ctx->timing_events[8 * k + 2 * j],
@@ -1107,9 +1178,52 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool co
     acc.stat_tris_sh += hc->stat_tris_sh;
 }
 
-// Budget of the per-path sample buffer; larger frames render in chunks of
+// Budget of the per-path sample buffer; larger frames render in passes of
 // whole samples per pixel.
 constexpr size_t kSampleBufferBytes = (size_t)4 << 30;
+
+static FilmParams film_params(const DevCamera& cam, const DevRequest& R, int filter, float* d_film,
+                              const float4* samples, unsigned long long* invalid) {
+    FilmParams F;
+    std::memset(&F, 0, sizeof(F));
+    float radius;
+    filter_setup(filter, radius, F.border, F.lookup, F.table);
+    F.film = reinterpret_cast<float4*>(d_film);
+    F.samples = samples;
+    F.invalid = invalid;
+    F.w = cam.w;
+    F.h = cam.h;
+    F.cols = cam.w + 2 * F.border;
+    F.rows = cam.h + 2 * F.border;
+    F.seed_mix = R.seed_mix;
+    return F;
+}
+
+static void finish_stats(dl_context* ctx, const RenderCounters& acc, unsigned long long invalid, int64_t iters,
+                         int64_t launches, const double* kms) {
+    cudaStream_t st = ctx->stream;
+    DL_CUDA(cudaEventRecord(ctx->ev1, st));
+    DL_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.camera_rays = (int64_t)acc.stat_camera;
+    ctx->stats.extension_rays = (int64_t)acc.stat_ext;
+    ctx->stats.shadow_rays = (int64_t)acc.stat_shadow;
+    ctx->stats.invalid_samples = (int64_t)invalid;
+    ctx->stats.iterations = iters;
+    ctx->stats.render_ms = ms;
+    ctx->stats.extend_ms = kms[0];
+    ctx->stats.shadow_ms = kms[1];
+    ctx->stats.shade_ms = kms[2];
+    ctx->stats.retire_ms = kms[3];
+    ctx->stats.kernel_launches = launches;
+}
+
+static int64_t pool_capacity(dl_context* ctx, int64_t requested, unsigned long long paths) {
+    int64_t cap = requested > 0 ? requested : ctx->tune.paths_in_flight;
+    cap = std::min<int64_t>(cap, (int64_t)std::max<unsigned long long>(paths, 1ull));
+    return ((cap + 31) / 32) * 32;
+}
 
 // Runs one render.  mode 0: the film (d_film) receives every sample through
 // the gather kernel; mode 1: Li of li_n explicit paths (d_xys -> d_L, d_pos).
@@ -1120,15 +1234,13 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
     const DevCamera& cam = S->dev.cam;
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
-    common_params(P, S, o);
+    P.r0 = make_request(S, o);
     P.mode = li_n > 0 ? 1 : 0;
     const unsigned long long npix = (unsigned long long)cam.w * cam.h;
     const int spp = std::max(o.spp, 1);
     int chunk_spp = P.mode == 1 ? 1 : (int)std::max<size_t>(1, std::min<size_t>(spp, kSampleBufferBytes / (npix * 16)));
     unsigned long long chunk_total = P.mode == 1 ? (unsigned long long)li_n : npix * (unsigned long long)chunk_spp;
-    int64_t cap = o.max_paths_in_flight > 0 ? o.max_paths_in_flight : (int64_t)1 << 22;
-    cap = std::min<int64_t>(cap, (int64_t)std::max<unsigned long long>(chunk_total, 1ull));
-    cap = ((cap + 31) / 32) * 32;
+    const int64_t cap = pool_capacity(ctx, o.max_paths_in_flight, chunk_total);
     RenderBuffers& B = ctx->render;
     B.ensure(cap);
     bind_pool(P, B);
@@ -1147,27 +1259,16 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
     unsigned long long invalid = 0;
     if (P.mode == 1) {
         P.total_paths = (unsigned long long)li_n;
-        run_wavefront(ctx, P, cap, count_traversal, kms, launches, iters, acc);
+        run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc);
     } else {
-        FilmParams F;
-        std::memset(&F, 0, sizeof(F));
-        float radius;
-        filter_setup(o.filter, radius, F.border, F.lookup, F.table);
-        F.film = reinterpret_cast<float4*>(d_film);
-        F.samples = P.samples;
-        F.invalid = B.invalid.as<unsigned long long>();
-        F.w = cam.w;
-        F.h = cam.h;
-        F.cols = cam.w + 2 * F.border;
-        F.rows = cam.h + 2 * F.border;
-        F.seed_mix = P.seed_mix;
+        FilmParams F = film_params(cam, P.r0, o.filter, d_film, P.samples, B.invalid.as<unsigned long long>());
         DL_CUDA(cudaMemsetAsync(F.invalid, 0, sizeof(unsigned long long), st));
         dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
         for (int s0 = 0; s0 < spp; s0 += chunk_spp) {
             int ns = std::min(chunk_spp, spp - s0);
-            P.spp_offset = o.spp_offset + s0;
+            P.r0.spp_offset = o.spp_offset + s0;
             P.total_paths = npix * (unsigned long long)ns;
-            run_wavefront(ctx, P, cap, count_traversal, kms, launches, iters, acc);
+            run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc);
             F.nspp = ns;
             F.s_first = o.spp_offset + s0;
             F.accumulate = s0 > 0;
@@ -1181,23 +1282,100 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
         DL_CUDA(cudaStreamSynchronize(st));
         invalid = *hinv;
     }
-    DL_CUDA(cudaEventRecord(ctx->ev1, st));
-    DL_CUDA(cudaEventSynchronize(ctx->ev1));
-    float ms = 0.f;
-    DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     acc.stat_invalid = invalid;
-    ctx->stats.camera_rays = (int64_t)acc.stat_camera;
-    ctx->stats.extension_rays = (int64_t)acc.stat_ext;
-    ctx->stats.shadow_rays = (int64_t)acc.stat_shadow;
-    ctx->stats.invalid_samples = (int64_t)invalid;
-    ctx->stats.iterations = iters;
-    ctx->stats.render_ms = ms;
-    ctx->stats.extend_ms = kms[0];
-    ctx->stats.shadow_ms = kms[1];
-    ctx->stats.shade_ms = kms[2];
-    ctx->stats.retire_ms = kms[3];
-    ctx->stats.kernel_launches = launches;
+    finish_stats(ctx, acc, invalid, iters, launches, kms);
     if (out_counters) *out_counters = acc;
+}
+
+// Batch of requests in one wavefront: every pass renders, for each request
+// with samples left, its next slice of samples per pixel; all requests' paths
+// share the path pool and the material queues (each path carries its
+// request), and after the pass one gather per request adds the slice to its
+// film.  Slices are sized so a pass fits the sample buffer.
+void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_traversal) {
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& B = ctx->render;
+    std::vector<int> done(n, 0);
+    unsigned long long all = 0;
+    for (int r = 0; r < n; r++)
+        all += (unsigned long long)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h * items[r].opts.spp;
+    const unsigned long long budget = kSampleBufferBytes / 16;
+    // slice of request r per pass: its share of the budget, at least one sample
+    std::vector<int> slice(n);
+    unsigned long long max_pass = 0;
+    for (int r = 0; r < n; r++) {
+        const unsigned long long npix = (unsigned long long)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h;
+        double share = all <= budget ? 1.0 : (double)budget / (double)all;
+        slice[r] = std::max(1, std::min(items[r].opts.spp, (int)(items[r].opts.spp * share)));
+        max_pass += npix * (unsigned long long)slice[r];
+    }
+    int64_t requested = 0;
+    for (int r = 0; r < n; r++) requested = std::max<int64_t>(requested, items[r].opts.max_paths_in_flight);
+    const int64_t cap = pool_capacity(ctx, requested, max_pass);
+    B.ensure(cap);
+    B.samples.ensure((size_t)std::max<unsigned long long>(max_pass, 1) * 16);
+    B.requests.ensure(sizeof(DevRequest) * (size_t)std::max(n, 1));
+    B.host_requests.ensure(sizeof(DevRequest) * (size_t)std::max(n, 1));
+    DevRequest* hreq = B.host_requests.as<DevRequest>();
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    bind_pool(P, B);
+    P.mode = 0;
+    P.samples = B.samples.as<float4>();
+    P.reqs = B.requests.as<DevRequest>();
+    unsigned long long* d_invalid = B.invalid.as<unsigned long long>();
+    double kms[4] = {0, 0, 0, 0};
+    int64_t launches = 0, iters = 0;
+    RenderCounters acc;
+    std::memset(&acc, 0, sizeof(acc));
+    DL_CUDA(cudaEventRecord(ctx->ev0, st));
+    DL_CUDA(cudaMemsetAsync(d_invalid, 0, sizeof(unsigned long long), st));
+    std::vector<int> active(n), ns(n);
+    for (;;) {
+        int na = 0;
+        unsigned long long first = 0;
+        for (int r = 0; r < n; r++) {
+            if (done[r] >= items[r].opts.spp) continue;
+            const dl_scene* S = items[r].scene;
+            const unsigned long long npix = (unsigned long long)S->dev.cam.w * S->dev.cam.h;
+            ns[na] = std::min(slice[r], items[r].opts.spp - done[r]);
+            DevRequest R = make_request(items[r].scene, items[r].opts);
+            R.pid_first = first;
+            R.spp_offset = items[r].opts.spp_offset + done[r];
+            hreq[na] = R;
+            active[na] = r;
+            first += npix * (unsigned long long)ns[na];
+            na++;
+        }
+        if (na == 0) break;
+        // the pass's request table; the copy is ordered before the pass's kernels
+        DL_CUDA(cudaMemcpyAsync(B.requests.ptr, hreq, sizeof(DevRequest) * na, cudaMemcpyHostToDevice, st));
+        P.num_reqs = na;
+        P.total_paths = first;
+        run_wavefront(ctx, P, cap, true, count_traversal, kms, launches, iters, acc);
+        for (int a = 0; a < na; a++) {
+            const int r = active[a];
+            const DevCamera& cam = items[r].scene->dev.cam;
+            FilmParams F = film_params(cam, hreq[a], items[r].opts.filter, items[r].d_film,
+                                       P.samples + hreq[a].pid_first, d_invalid);
+            F.nspp = ns[a];
+            F.s_first = hreq[a].spp_offset;
+            F.accumulate = done[r] > 0;
+            dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
+            k_film_gather<<<fgrid, 256, 0, st>>>(F);
+            launches += 1;
+            DL_CUDA(cudaGetLastError());
+            done[r] += ns[a];
+        }
+        // host_requests is rewritten next pass: wait for this pass's copy
+        DL_CUDA(cudaStreamSynchronize(st));
+    }
+    unsigned long long* hinv =
+        reinterpret_cast<unsigned long long*>(B.host_counters.as<char>() + sizeof(RenderCounters));
+    DL_CUDA(cudaMemcpyAsync(hinv, d_invalid, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    acc.stat_invalid = *hinv;
+    finish_stats(ctx, acc, *hinv, iters, launches, kms);
 }
 
 // Li of explicit paths with every piece of path state in caller-provided
@@ -1213,7 +1391,7 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     cudaStream_t st = ctx->stream;
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
-    common_params(P, S, o);
+    P.r0 = make_request(S, o);
     P.mode = 1;
     size_t c = (size_t)slots;
     char* b = static_cast<char*>(pool);
@@ -1243,12 +1421,14 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     cudaError_t e = cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st);
     if (e != cudaSuccess) return e;
-    k_init<<<sms * 16, 128, 0, st>>>(P, (int)cap);
+    k_init<false><<<sms * 16, 128, 0, st>>>(P, (int)cap);
     RenderCounters hc;
     int64_t iters = 0;
+    const TuneParams tp;  // default launch shape
     for (;;) {
-        for (int k = 0; k < kBatch; k++) launch_iteration(P, k & 1, st, sms, false, nullptr, nullptr);
-        iters += kBatch;
+        for (int k = 0; k < tp.iters_per_graph; k++)
+            launch_iteration<false>(P, k & 1, st, sms, tp, false, nullptr, nullptr);
+        iters += tp.iters_per_graph;
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
         if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;

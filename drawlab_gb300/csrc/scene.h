@@ -19,6 +19,14 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
                 float* d_pos, bool count_traversal, RenderCounters* out_counters);
 void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb);
 
+// One request of a batch: scene, options, device film (film_floats sized).
+struct BatchItem {
+    dl_scene* scene;
+    dl_render_opts opts;
+    float* d_film;
+};
+void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_traversal);
+
 // XML scene loading (xml.cpp): fills arrays and default render options.
 struct XmlScene;
 int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out);

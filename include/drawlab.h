@@ -272,6 +272,50 @@ int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
 int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t n,
                  const int32_t* d_xys, float* d_L, float* d_pos);
 
+/* ----------------------------------------------------------------- batches */
+
+/* One request of a batch: a scene of the context, its render options and at
+ * least one output -- `rgb` (host, height x width x 3, as dl_render) and/or
+ * `film_device` (device film, as dl_render_film_device). */
+typedef struct dl_request {
+    dl_scene* scene;
+    dl_render_opts opts;
+    float* rgb;
+    float* film_device;
+} dl_request;
+
+/* Render many requests -- of different scenes, resolutions and sample
+ * counts -- in one wavefront: their paths share the path pool, the
+ * material-sorted queues and the captured iteration graph, each path
+ * carrying its request; every pass renders a slice of every unfinished
+ * request's samples and gathers each slice into its request's film.  Each
+ * request's image equals its dl_render image up to float summation order.
+ * No reference counterpart: the reference renders one scene per process
+ * (src/main.cpp, src/tracer/backend/cpu_renderer.cpp). */
+int dl_render_batch(dl_context* ctx, const dl_request* reqs, int32_t n);
+
+/* Launch shape of the wavefront renderer: path slots in flight (the pool),
+ * resident CTAs per SM of the traversal kernels and of the shading kernels,
+ * wavefront iterations per captured graph launch (between queue checks). */
+typedef struct dl_tune_params {
+    int64_t paths_in_flight;        /* 32 .. 2^28; opts.max_paths_in_flight overrides */
+    int32_t traverse_ctas_per_sm;   /* 1 .. 16 */
+    int32_t shade_ctas_per_sm;      /* 1 .. 64 */
+    int32_t iterations_per_graph;   /* 2, 4, 6 or 8 */
+    int32_t reserved;
+} dl_tune_params;
+int dl_context_get_tune(const dl_context* ctx, dl_tune_params* out);
+int dl_context_set_tune(dl_context* ctx, const dl_tune_params* tune);
+
+/* Autotuner: renders the requests at `trial_spp` samples per pixel each (0:
+ * an eighth of each request's spp, at least 1) under candidate launch shapes
+ * -- a coordinate search over the pool size, then the traversal and shading
+ * grid sizes, then the graph length -- times each on the GPU, and keeps the
+ * fastest on the context.  `out` (may be NULL) receives it; `trials` (may be
+ * NULL) the number of shapes timed.  Outputs of the requests are not written. */
+int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t trial_spp, dl_tune_params* out,
+                int32_t* trials);
+
 /* --------------------------------------------------------------- statistics */
 
 typedef struct dl_stats {

@@ -51,7 +51,8 @@ def test_struct_sizes_match_header():
     assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1)
 
 
-STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts",
+STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts", "dl_request",
+           "dl_tune_params",
            "dl_scene_info", "dl_stats", "dl_traversal_counts"]
 
 

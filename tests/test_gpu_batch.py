@@ -1,0 +1,76 @@
+"""Batched rendering (dl_render_batch): requests of different scenes,
+resolutions and sample counts in one wavefront give the same images as
+rendering each alone; the autotuner picks a valid launch shape that renders
+the same images."""
+import numpy as np
+import pytest
+
+from drawlab_gb300 import abi, api, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return api.Context(0)
+
+
+def small_batch(ctx):
+    sa = api.Scene.from_data(ctx, scenes.cornell(width=48, height=40))
+    sb = api.Scene.from_data(ctx, scenes.env_spheres(width=40, height=24))
+    sc = api.Scene.from_data(ctx, scenes.reference_spheres(width=32, height=20))
+    return [(sa, abi.make_opts(spp=8, max_depth=6, seed=1)),
+            (sb, abi.make_opts(spp=4, max_depth=8, seed=2)),
+            (sc, abi.make_opts(spp=6, max_depth=5, seed=3, flags=abi.DL_RENDER_POWER_LIGHT_PICK)),
+            (sa, abi.make_opts(spp=3, max_depth=2, seed=4, filter=abi.DL_FILTER_BOX))]
+
+
+def test_batch_equals_single_renders(ctx):
+    items = small_batch(ctx)
+    outs = ctx.render_batch(items)
+    st = ctx.stats()
+    assert st.camera_rays == sum(s.width * s.height * o.spp for s, o in items)
+    for (s, o), img in zip(items, outs):
+        np.testing.assert_array_equal(img, s.render(o))
+
+
+def test_batch_in_several_passes(ctx):
+    # 2 x 1024^2 x 200 samples exceed one pass of the sample buffer
+    s1 = api.Scene.from_data(ctx, scenes.cornell(width=1024, height=1024))
+    s2 = api.Scene.from_data(ctx, scenes.env_spheres(width=1024, height=1024))
+    items = [(s1, abi.make_opts(spp=200, max_depth=3, seed=5)), (s2, abi.make_opts(spp=200, max_depth=3, seed=6))]
+    outs = ctx.render_batch(items)
+    for (s, o), img in zip(items, outs):
+        np.testing.assert_allclose(img, s.render(o), rtol=1e-5, atol=1e-6)
+
+
+def test_autotune_keeps_a_valid_shape(ctx):
+    items = small_batch(ctx)
+    t, trials = ctx.autotune(items, trial_spp=2)
+    assert trials == 15
+    assert t.paths_in_flight in (1 << 20, 1 << 21, 1 << 22, 1 << 23)
+    assert t.traverse_ctas_per_sm in (4, 6, 8) and t.shade_ctas_per_sm in (8, 16, 32)
+    assert t.iterations_per_graph in (2, 4, 8)
+    g = ctx.get_tune()
+    assert (g.paths_in_flight, g.iterations_per_graph) == (t.paths_in_flight, t.iterations_per_graph)
+    # images do not depend on the launch shape
+    for (s, o), img in zip(items, ctx.render_batch(items)):
+        np.testing.assert_array_equal(img, s.render(o))
+    bad = abi.dl_tune_params(paths_in_flight=64, traverse_ctas_per_sm=8, shade_ctas_per_sm=16,
+                             iterations_per_graph=3)
+    with pytest.raises(api.DrawlabError):
+        ctx.set_tune(bad)
+    ctx.set_tune(abi.dl_tune_params(paths_in_flight=1 << 22, traverse_ctas_per_sm=8, shade_ctas_per_sm=16,
+                                    iterations_per_graph=4))
+
+
+def test_batch_arguments_are_checked(ctx):
+    other = api.Context(0)
+    s_other = api.Scene.from_data(other, scenes.cornell(width=16, height=16))
+    with pytest.raises(api.DrawlabError) as e:
+        ctx.render_batch([(s_other, abi.make_opts(spp=1))])
+    assert "another context" in str(e.value)
+    s = api.Scene.from_data(ctx, scenes.cornell(width=16, height=16))
+    with pytest.raises(api.DrawlabError):
+        ctx.render_batch([(s, abi.make_opts(spp=0))])
+    assert ctx.render_batch([]) == []
