@@ -1,4 +1,4 @@
-"""Benchmark: the procedural material scene (327,682 triangles, 1920x1080,
+"""Benchmark: the procedural material scene (327,690 triangles, 1920x1080,
 64 spp, max depth 16) rendered by the GB300 wavefront path tracer.
 
 One step = one full frame: 1920*1080*64 = 132.7M camera paths.  The scene
@@ -46,6 +46,11 @@ METRIC = "samples/s (material-sphere scene 1920x1080, 64 spp, depth 16)"
 # algorithmic bytes per closest-hit ray: node = 64 B (both child boxes + refs),
 # triangle = 48 B (3 x float4), ray in 32 B, hit out 16 B
 NODE_BYTES, TRI_BYTES, RAY_IN, HIT_OUT = 64, 48, 32, 16
+# DRAM bytes (read + write) per closest-hit traversal launch of this workload,
+# from one ncu capture of the full-size launch list (dram__bytes_read.sum +
+# dram__bytes_write.sum over the 374 extension launches of that capture /
+# 374); a profile measurement, not a live one.
+TRAVERSE_DRAM_BYTES_PER_LAUNCH = (137.13e9 + 39.96e9) / 374
 
 
 def peaks():
@@ -250,6 +255,7 @@ def main():
     ext_ms, sh_ms, shade_ms, ret_ms = st.extend_ms, st.shadow_ms, st.shade_ms, st.retire_ms
     timed_frame_ms = st.render_ms
     t_ext_rays, t_sh_rays = st.extension_rays, st.shadow_rays
+    ext_launches = st.iterations  # one closest-hit launch per wavefront iteration
     t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -303,8 +309,11 @@ def main():
                     "d2h_bytes_per_step": W * H * 3 * 4,
                     "call": "dl_render (render options by value; image returned to host memory)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
-                         "kernel": "k_extend (closest-hit traversal)",
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": TRAVERSE_DRAM_BYTES_PER_LAUNCH,
+                         "traffic_note": "ncu DRAM bytes per extension launch (profile capture)",
+                         "algorithmic_bytes_per_launch": bytes_per_ray * t_ext_rays / max(1, ext_launches),
+                         "kernel": "k_traverse<extension> (closest-hit traversal)",
                          "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": n_node,
                          "tri_tests_per_ray": n_tri,
                          "note": "algorithmic node+triangle fetch bytes (64 B node, 48 B triangle, 32 B ray, "
