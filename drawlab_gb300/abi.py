@@ -175,6 +175,19 @@ class dl_tune_params(C.Structure):
     ]
 
 
+DL_GUIDE_PARAMS = 16560
+
+
+class dl_guide_config(C.Structure):
+    _fields_ = [
+        ("learning_rate", C.c_float),
+        ("guide_fraction", C.c_float),
+        ("batch", C.c_int32),
+        ("steps_per_pass", C.c_int32),
+        ("seed", C.c_uint64),
+    ]
+
+
 def make_opts(spp=1, max_depth=0, rr_depth=3, filter=DL_FILTER_GAUSSIAN, seed=0, flags=0,
               spp_offset=0, max_paths_in_flight=0) -> dl_render_opts:
     o = dl_render_opts()

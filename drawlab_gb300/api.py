@@ -49,6 +49,14 @@ SIGNATURES = {
     "dl_context_get_tune": (C.c_int, [_vp, _vp]),
     "dl_context_set_tune": (C.c_int, [_vp, _vp]),
     "dl_autotune": (C.c_int, [_vp, _vp, _i32, _i32, _vp, _vp]),
+    "dl_guide_default_config": (C.c_int, [_vp]),
+    "dl_guide_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    "dl_guide_destroy": (C.c_int, [_vp]),
+    "dl_guide_get_params": (C.c_int, [_vp, _vp]),
+    "dl_guide_set_params": (C.c_int, [_vp, _vp]),
+    "dl_guide_forward": (C.c_int, [_vp, _i64, _vp, _vp]),
+    "dl_guide_gradient": (C.c_int, [_vp, _i64, _vp, _vp, _vp]),
+    "dl_guide_train": (C.c_int, [_vp, _i64, _vp, _i32, _vp]),
 }
 
 
@@ -253,6 +261,63 @@ class Scene:
             if getattr(self.ctx, "h", None):   # the context still exists
                 self.ctx.lib.dl_scene_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Guide:
+    """The learned guiding proposal (network parameters and Adam state on
+    the device)."""
+
+    def __init__(self, ctx: Context, **cfg):
+        self.ctx = ctx
+        c = abi.dl_guide_config()
+        ctx.check(ctx.lib.dl_guide_default_config(C.byref(c)))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.dl_guide_create(ctx.h, C.byref(c), C.byref(h)))
+        self.h = h
+        self.config = c
+        ctx._scenes.add(self)
+
+    def params(self) -> np.ndarray:
+        p = np.empty(abi.DL_GUIDE_PARAMS, np.float32)
+        self.ctx.check(self.ctx.lib.dl_guide_get_params(self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.shape == (abi.DL_GUIDE_PARAMS,)
+        self.ctx.check(self.ctx.lib.dl_guide_set_params(self.h, _ptr(p)))
+
+    def forward(self, inputs) -> np.ndarray:
+        x = np.ascontiguousarray(inputs, np.float32)
+        out = np.empty((x.shape[0], 40), np.float32)
+        self.ctx.check(self.ctx.lib.dl_guide_forward(self.h, x.shape[0], _ptr(x), _ptr(out)))
+        return out
+
+    def gradient(self, records):
+        r = np.ascontiguousarray(records, np.float32)
+        g = np.empty(abi.DL_GUIDE_PARAMS, np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.dl_guide_gradient(self.h, r.shape[0], _ptr(r), _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def train(self, records, steps: int = 1) -> float:
+        r = np.ascontiguousarray(records, np.float32)
+        loss = C.c_float()
+        self.ctx.check(self.ctx.lib.dl_guide_train(self.h, r.shape[0], _ptr(r), steps, C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
+            self.ctx.lib.dl_guide_destroy(self.h)
+        self.h = None
 
     def __del__(self):
         try:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -468,6 +469,121 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
             out->shade_ctas_per_sm = best.shade_ctas_per_sm;
             out->iterations_per_graph = best.iters_per_graph;
         }
+    });
+}
+
+int dl_guide_default_config(dl_guide_config* cfg) {
+    if (!cfg) return DL_ERR_INVALID_ARG;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->learning_rate = 1e-3f;
+    cfg->guide_fraction = 0.5f;
+    cfg->batch = 65536;
+    cfg->steps_per_pass = 8;
+    cfg->seed = 1;
+    return DL_OK;
+}
+
+int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    dl_guide* G = nullptr;
+    int rc = guard(ctx, [&] {
+        need(cfg != nullptr && out != nullptr, "cfg/out is NULL");
+        need(cfg->learning_rate > 0.f && cfg->learning_rate < 1.f, "learning_rate out of range");
+        need(cfg->guide_fraction >= 0.f && cfg->guide_fraction < 1.f, "guide_fraction must be in [0, 1)");
+        need(cfg->batch >= 16 && cfg->batch <= (1 << 24), "batch out of range");
+        need(cfg->steps_per_pass >= 0 && cfg->steps_per_pass <= 1024, "steps_per_pass out of range");
+        *out = nullptr;
+        G = new dl_guide();
+        G->ctx = ctx;
+        G->cfg = *cfg;
+        const size_t pb = dl::kGuideParams * 4;
+        for (dl::DevBuf* b : {&G->w32, &G->grad, &G->m, &G->v}) b->ensure(pb);
+        G->w16.ensure(dl::kGuideParams * 2);
+        G->scratch.ensure(256);
+        for (dl::DevBuf* b : {&G->grad, &G->m, &G->v}) DL_CUDA(cudaMemsetAsync(b->ptr, 0, pb, ctx->stream));
+        std::vector<float> w;
+        dl::guide_init_params(cfg->seed, w);
+        dl::guide_upload_params(G, w.data());
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+    if (rc != DL_OK) {
+        delete G;
+        return rc;
+    }
+    *out = G;
+    return DL_OK;
+}
+
+int dl_guide_destroy(dl_guide* G) {
+    if (!G) return DL_ERR_INVALID_ARG;
+    cudaSetDevice(G->ctx->device);
+    cudaStreamSynchronize(G->ctx->stream);
+    delete G;
+    return DL_OK;
+}
+
+int dl_guide_get_params(const dl_guide* G, float* params) {
+    if (!G || !params) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = G->ctx;
+    return guard(ctx, [&] {
+        DL_CUDA(cudaMemcpyAsync(params, G->w32.ptr, dl::kGuideParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int dl_guide_set_params(dl_guide* G, const float* params) {
+    if (!G) return DL_ERR_INVALID_ARG;
+    return guard(G->ctx, [&] {
+        need(params != nullptr, "params is NULL");
+        for (int i = 0; i < dl::kGuideParams; i++) need(std::isfinite(params[i]), "params must be finite");
+        dl::guide_upload_params(G, params);
+        DL_CUDA(cudaStreamSynchronize(G->ctx->stream));
+    });
+}
+
+int dl_guide_forward(dl_guide* G, int64_t n, const float* inputs, float* outputs) {
+    if (!G) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = G->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && n < ((int64_t)1 << 31) && (n == 0 || (inputs && outputs)), "bad buffers");
+        if (n == 0) return;
+        G->io_in.ensure((size_t)n * 6 * 4);
+        G->io_out.ensure((size_t)n * 40 * 4);
+        DL_CUDA(cudaMemcpyAsync(G->io_in.ptr, inputs, (size_t)n * 24, cudaMemcpyHostToDevice, ctx->stream));
+        dl::guide_forward(G, G->io_in.as<float>(), G->io_out.as<float>(), n);
+        DL_CUDA(cudaMemcpyAsync(outputs, G->io_out.ptr, (size_t)n * 160, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad, float* loss) {
+    if (!G) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = G->ctx;
+    return guard(ctx, [&] {
+        need(n >= 1 && n <= (1 << 24) && records && grad, "bad buffers");
+        G->recs.ensure((size_t)n * 48);
+        DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
+        DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
+        dl::guide_gradient(G, G->recs.ptr, n);
+        DL_CUDA(cudaMemcpyAsync(grad, G->grad.ptr, dl::kGuideParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        float l = 0.f;
+        DL_CUDA(cudaMemcpyAsync(&l, G->scratch.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (loss) *loss = l;
+    });
+}
+
+int dl_guide_train(dl_guide* G, int64_t n, const float* records, int32_t steps, float* loss) {
+    if (!G) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = G->ctx;
+    return guard(ctx, [&] {
+        need(n >= 1 && n <= (1 << 24) && records, "bad buffers");
+        need(steps >= 0 && steps <= 100000, "steps out of range");
+        G->recs.ensure((size_t)n * 48);
+        DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
+        float l = dl::guide_train(G, G->recs.ptr, n, steps);
+        if (loss) *loss = l;
     });
 }
 

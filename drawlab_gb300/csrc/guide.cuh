@@ -1,0 +1,248 @@
+// Learned path-guiding proposal: a small MLP maps (position, normal) of a
+// shading point to a mixture of von Mises-Fisher lobes over incident
+// directions.  Device code shared by the renderer (inference inside the
+// guided material kernels) and by the training kernels (guide.cu).
+//
+// Network (FP16 weights and activations, FP32 accumulation on the tensor
+// cores with mma.sync m16n8k16):
+//   input   6 scalars: position scaled to [0, 1]^3 by the scene bounds,
+//           shading normal in [-1, 1]^3
+//   encode  sin / cos (2^k pi x), k = 0..11, for each scalar: 144 features
+//   layer 1 144 -> 64, ReLU
+//   layer 2  64 -> 64, ReLU
+//   layer 3  64 -> 40 (rows 40..47 of the padded weight are zero)
+//   output  8 lobes x (mean direction m (3, normalised), log kappa, logit)
+//           kappa = exp(clamp(log kappa, -3, 8)), weights = softmax(logits)
+// vMF lobe: pdf(w) = kappa / (2 pi (1 - e^{-2 kappa})) exp(kappa (mu.w - 1)).
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "device.cuh"
+
+namespace dl {
+
+constexpr int kGIn = 6;
+constexpr int kGFreq = 12;
+constexpr int kGEnc = kGIn * kGFreq * 2;  // 144
+constexpr int kGHid = 64;
+constexpr int kGLobes = 8;
+constexpr int kGOut = 5 * kGLobes;         // 40
+constexpr int kGOutPad = 48;
+// parameter layout (floats / halves, one contiguous array)
+constexpr int kGW1 = 0;
+constexpr int kGB1 = kGW1 + kGHid * kGEnc;
+constexpr int kGW2 = kGB1 + kGHid;
+constexpr int kGB2 = kGW2 + kGHid * kGHid;
+constexpr int kGW3 = kGB2 + kGHid;
+constexpr int kGB3 = kGW3 + kGOutPad * kGHid;
+constexpr int kGParams = kGB3 + kGOutPad;  // 16560
+constexpr float kGLogKappaMin = -3.f, kGLogKappaMax = 8.f;
+
+// Per-warp shared-memory tile of 16 rows (one m16 tile).
+constexpr int kGXs = kGEnc + 8;   // row stride (halves) of the encoding / layer-2 output
+constexpr int kGHs = kGHid + 8;   // row stride (halves) of the layer-1 output
+constexpr int kGOs = kGOutPad + 1;  // row stride (floats) of the network output
+struct GuideTile {
+    __half x[16 * kGXs];   // encoding; later layer-2 output (aliased)
+    __half h[16 * kGHs];   // layer-1 output
+    float o[16 * kGOs];    // network output
+};
+
+struct GuideNet {
+    const __half* w16;   // kGParams halves
+    float3 lo;           // scene bounds: position -> [0, 1]^3
+    float3 inv_ext;
+    float fraction;      // probability of sampling the learned proposal
+};
+
+// ------------------------------------------------------------- encoding
+// sin / cos of (2^k pi x) for k = 0..11: exact sincospi at k = 0, 4, 8,
+// double-angle steps in between (at most three, error ~1e-6).
+__device__ __forceinline__ void encode_scalar(float x, __half* out) {
+#pragma unroll
+    for (int k0 = 0; k0 < kGFreq; k0 += 4) {
+        float s, c;
+        sincospif(x * (float)(1 << k0), &s, &c);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            out[2 * (k0 + k)] = __float2half_rn(s);
+            out[2 * (k0 + k) + 1] = __float2half_rn(c);
+            float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
+            s = s2;
+            c = c2;
+        }
+    }
+}
+
+__device__ __forceinline__ void encode_input(const float* in6, __half* row) {
+#pragma unroll
+    for (int i = 0; i < kGIn; i++) encode_scalar(in6[i], row + i * 2 * kGFreq);
+}
+
+// ---------------------------------------------------------- mma helpers
+__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ uint32_t pack2(__half lo, __half hi) {
+    return (uint32_t)__half_as_ushort(lo) | ((uint32_t)__half_as_ushort(hi) << 16);
+}
+__device__ __forceinline__ uint32_t ld2(const __half* p) {  // two consecutive halves, 4-byte aligned
+    return *reinterpret_cast<const uint32_t*>(p);
+}
+
+// A fragment of a row-major 16 x 16 block at `a` (row stride lda halves).
+__device__ __forceinline__ void frag_a(uint32_t* r, const __half* a, int lda, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    r[0] = ld2(a + g * lda + 2 * t);
+    r[1] = ld2(a + (g + 8) * lda + 2 * t);
+    r[2] = ld2(a + g * lda + 2 * t + 8);
+    r[3] = ld2(a + (g + 8) * lda + 2 * t + 8);
+}
+// B fragment (16 x 8, B[k][n]) of y = x W^T with W row-major [n][k] at `w`
+// (row stride ldw): B[k][n] = W[n][k], consecutive k are contiguous.
+__device__ __forceinline__ void frag_b_wt(uint32_t* r, const __half* w, int ldw, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    r[0] = ld2(w + g * ldw + 2 * t);
+    r[1] = ld2(w + g * ldw + 2 * t + 8);
+}
+// B fragment of y = x W with W row-major [k][n] (row stride ldw).
+__device__ __forceinline__ void frag_b_w(uint32_t* r, const __half* w, int ldw, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    r[0] = pack2(w[(2 * t) * ldw + g], w[(2 * t + 1) * ldw + g]);
+    r[1] = pack2(w[(2 * t + 8) * ldw + g], w[(2 * t + 9) * ldw + g]);
+}
+
+// One dense layer on a 16-row tile: out[16][N] = act(in[16][K] W^T + b),
+// W row-major [N][K] (halves, row stride K), b floats.  ReLU output goes to
+// `out16` (halves, row stride ldo); the linear output (no ReLU) to `outf`.
+template <int K, int N, bool kRelu>
+__device__ __forceinline__ void layer16(const __half* in, int ldi, const __half* W, const float* b, __half* out16,
+                                        int ldo, float* outf, int ldf, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < N / 8; nt++) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int ks = 0; ks < K / 16; ks++) {
+            uint32_t a[4], bb[2];
+            frag_a(a, in + ks * 16, ldi, lane);
+            frag_b_wt(bb, W + (nt * 8) * K + ks * 16, K, lane);
+            mma16816(c, a, bb);
+        }
+        const int col = nt * 8 + 2 * t;
+        const float b0 = b[col], b1 = b[col + 1];
+        c[0] += b0;
+        c[1] += b1;
+        c[2] += b0;
+        c[3] += b1;
+        if (kRelu) {
+            out16[g * ldo + col] = __float2half_rn(fmaxf(c[0], 0.f));
+            out16[g * ldo + col + 1] = __float2half_rn(fmaxf(c[1], 0.f));
+            out16[(g + 8) * ldo + col] = __float2half_rn(fmaxf(c[2], 0.f));
+            out16[(g + 8) * ldo + col + 1] = __float2half_rn(fmaxf(c[3], 0.f));
+        } else {
+            outf[g * ldf + col] = c[0];
+            outf[g * ldf + col + 1] = c[1];
+            outf[(g + 8) * ldf + col] = c[2];
+            outf[(g + 8) * ldf + col + 1] = c[3];
+        }
+    }
+}
+
+// Forward pass of the 16 rows in `T.x` (encodings already written): the
+// network output lands in T.o; the layer-1 / layer-2 activations stay in
+// T.h / T.x for a backward pass.  Weights: halves `w16`; biases: floats
+// `bias` at the same offsets as in the parameter layout.
+__device__ __forceinline__ void forward16(GuideTile& T, const __half* w16, const float* bias, int lane) {
+    layer16<kGEnc, kGHid, true>(T.x, kGXs, w16 + kGW1, bias + kGB1, T.h, kGHs, nullptr, 0, lane);
+    __syncwarp();
+    layer16<kGHid, kGHid, true>(T.h, kGHs, w16 + kGW2, bias + kGB2, T.x, kGXs, nullptr, 0, lane);
+    __syncwarp();
+    layer16<kGHid, kGOutPad, false>(T.x, kGXs, w16 + kGW3, bias + kGB3, nullptr, 0, T.o, kGOs, lane);
+    __syncwarp();
+}
+
+// -------------------------------------------------------------- mixture
+struct VmfLobe {
+    float3 mu;
+    float kappa;
+    float lambda;
+    float inv_len;  // 1 / |m| (for gradients)
+    bool clamped;   // log kappa outside [min, max]
+};
+
+// Lobes from the 40 network outputs at `o` (stride 1).
+__device__ __forceinline__ void decode_lobes(const float* o, VmfLobe* L) {
+    float mx = -1e30f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) mx = fmaxf(mx, o[5 * j + 4]);
+    float sum = 0.f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) {
+        float3 m = f3(o[5 * j], o[5 * j + 1], o[5 * j + 2]);
+        float len = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z);
+        if (len > 1e-6f) {
+            L[j].mu = f3(m.x / len, m.y / len, m.z / len);
+            L[j].inv_len = 1.f / len;
+        } else {
+            L[j].mu = f3(0.f, 0.f, 1.f);
+            L[j].inv_len = 0.f;
+        }
+        float lk = o[5 * j + 3];
+        L[j].clamped = lk < kGLogKappaMin || lk > kGLogKappaMax;
+        L[j].kappa = expf(fminf(fmaxf(lk, kGLogKappaMin), kGLogKappaMax));
+        L[j].lambda = expf(o[5 * j + 4] - mx);
+        sum += L[j].lambda;
+    }
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) L[j].lambda /= sum;
+}
+
+__device__ __forceinline__ float vmf_pdf(float3 mu, float kappa, float3 w) {
+    float d = mu.x * w.x + mu.y * w.y + mu.z * w.z;
+    if (kappa < 1e-4f) return 0.25f * kInvPiF;
+    return kappa / (2.f * kPiF * (-expm1f(-2.f * kappa))) * expf(kappa * (d - 1.f));
+}
+
+__device__ __forceinline__ float mixture_pdf(const VmfLobe* L, float3 w) {
+    float p = 0.f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) p += L[j].lambda * vmf_pdf(L[j].mu, L[j].kappa, w);
+    return p;
+}
+
+// Sample a direction: lobe by its weight (u0), then the vMF lobe (Jakob's
+// stable inversion of the cosine's distribution, u = (u1, u2)).
+__device__ __forceinline__ float3 mixture_sample(const VmfLobe* L, float u0, float2 u) {
+    int j = kGLobes - 1;
+    float acc = 0.f;
+#pragma unroll
+    for (int i = 0; i < kGLobes - 1; i++) {
+        acc += L[i].lambda;
+        if (u0 < acc) {
+            j = i;
+            break;
+        }
+    }
+    const float k = L[j].kappa;
+    float w;
+    if (k < 1e-4f) {
+        w = 2.f * u.x - 1.f;
+    } else {
+        w = 1.f + logf(u.x + (1.f - u.x) * expf(-2.f * k)) / k;
+    }
+    w = fminf(fmaxf(w, -1.f), 1.f);
+    float v = sqrtf(fmaxf(0.f, 1.f - w * w));
+    float s, c;
+    sincospif(2.f * u.y, &s, &c);
+    Frame f = make_onb(L[j].mu);
+    float3 loc = f3(v * c, v * s, w);
+    return normalize(to_world(f, loc));
+}
+
+}  // namespace dl

@@ -181,6 +181,15 @@ struct dl_context {
     }
 };
 
+// Learned guiding proposal: parameters (fp32 master, fp16 copy), Adam state
+// and training buffers (guide.cu).
+struct dl_guide {
+    dl_context* ctx = nullptr;
+    dl_guide_config cfg{};
+    dl::DevBuf w32, w16, grad, m, v, scratch, acts, recs, io_in, io_out;
+    int64_t step = 0;
+};
+
 struct dl_scene {
     dl_context* ctx = nullptr;
     dl::DevScene dev{};

@@ -27,6 +27,15 @@ struct BatchItem {
 };
 void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_traversal);
 
+// Learned guiding (guide.cu).
+constexpr int kGuideParams = 16560;
+void guide_init_params(uint64_t seed, std::vector<float>& w);
+void guide_upload_params(dl_guide* G, const float* host);
+void guide_gradient(dl_guide* G, const void* d_recs, int64_t n);
+void guide_adam(dl_guide* G);
+float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps);
+void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n);
+
 // XML scene loading (xml.cpp): fills arrays and default render options.
 struct XmlScene;
 int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out);

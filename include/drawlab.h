@@ -316,6 +316,44 @@ int dl_context_set_tune(dl_context* ctx, const dl_tune_params* tune);
 int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t trial_spp, dl_tune_params* out,
                 int32_t* trials);
 
+/* ------------------------------------------------------- learned guiding */
+
+/* A learned proposal for path guiding: an MLP on (position, normal) whose
+ * output is a mixture of 8 von Mises-Fisher lobes over incident directions,
+ * trained online on the renderer's own radiance samples and used as one
+ * extra technique in one-sample MIS with BSDF sampling (the estimator stays
+ * unbiased; BSDF + NEE remains the fallback).  No reference counterpart.
+ *
+ * Network: encoding sin/cos(2^k pi x), k < 12, of the 6 inputs (144
+ * features) -> 64 ReLU -> 64 ReLU -> 40 outputs = per lobe (mean direction
+ * m (3, normalised), log kappa (clamped to [-3, 8]), weight logit (softmax)).
+ * FP16 weights and activations, FP32 accumulation, on the tensor cores.
+ * Parameters (DL_GUIDE_PARAMS floats): W1 [64][144], b1 [64], W2 [64][64],
+ * b2 [64], W3 [48][64] (rows 40..47 zero), b3 [48] (40..47 zero). */
+#define DL_GUIDE_PARAMS 16560
+typedef struct dl_guide dl_guide;
+typedef struct dl_guide_config {
+    float learning_rate;     /* Adam step size (1e-3) */
+    float guide_fraction;    /* probability of sampling the learned proposal at a guided vertex (0.5) */
+    int32_t batch;           /* training records per Adam step (65536) */
+    int32_t steps_per_pass;  /* Adam steps after each pass of dl_render_guided (8) */
+    uint64_t seed;           /* initial weights */
+} dl_guide_config;
+int dl_guide_default_config(dl_guide_config* cfg);
+int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out);
+int dl_guide_destroy(dl_guide* guide);
+int dl_guide_get_params(const dl_guide* guide, float* params);
+int dl_guide_set_params(dl_guide* guide, const float* params);
+/* Network outputs (n x 40) for inputs (n x 6: position in [0,1]^3, normal). */
+int dl_guide_forward(dl_guide* guide, int64_t n, const float* inputs, float* outputs);
+/* Training records, 12 floats each: position in [0,1]^3 (3), normal (3),
+ * sampled direction (3), its sampling pdf, radiance estimate along it, 0.
+ * Loss: -(1/n) sum (L/p) / mean(L/p) log q(direction).  dl_guide_gradient
+ * returns the gradient of that loss (DL_GUIDE_PARAMS floats) and the loss
+ * without updating; dl_guide_train runs `steps` Adam steps on the batch. */
+int dl_guide_gradient(dl_guide* guide, int64_t n, const float* records, float* grad, float* loss);
+int dl_guide_train(dl_guide* guide, int64_t n, const float* records, int32_t steps, float* loss);
+
 /* --------------------------------------------------------------- statistics */
 
 typedef struct dl_stats {
