@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 2
+DL_ABI_VERSION = 3
 
 # status
 DL_OK = 0
@@ -142,6 +142,8 @@ class dl_stats(C.Structure):
         ("shade_ms", C.c_double),
         ("retire_ms", C.c_double),
         ("kernel_launches", C.c_int64),
+        ("guide_records", C.c_int64),
+        ("guide_train_ms", C.c_double),
     ]
 
 

@@ -57,6 +57,7 @@ SIGNATURES = {
     "dl_guide_forward": (C.c_int, [_vp, _i64, _vp, _vp]),
     "dl_guide_gradient": (C.c_int, [_vp, _i64, _vp, _vp, _vp]),
     "dl_guide_train": (C.c_int, [_vp, _i64, _vp, _i32, _vp]),
+    "dl_render_guided": (C.c_int, [_vp, _vp, _vp, _i32, _vp]),
 }
 
 
@@ -242,6 +243,11 @@ class Scene:
         film = np.empty((self.height + 2 * b, self.width + 2 * b, 4), np.float32)
         self.ctx.check(self.ctx.lib.dl_render_film(self.h, C.byref(opts), _ptr(film)))
         return film
+
+    def render_guided(self, opts: abi.dl_render_opts, guide, train: bool = True) -> np.ndarray:
+        rgb = np.empty((self.height, self.width, 3), np.float32)
+        self.ctx.check(self.ctx.lib.dl_render_guided(self.h, C.byref(opts), guide.h, 1 if train else 0, _ptr(rgb)))
+        return rgb
 
     def li(self, opts: abi.dl_render_opts, xys: np.ndarray):
         xys = np.ascontiguousarray(xys, np.int32)

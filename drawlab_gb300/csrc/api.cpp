@@ -587,6 +587,24 @@ int dl_guide_train(dl_guide* G, int64_t n, const float* records, int32_t steps, 
     });
 }
 
+int dl_render_guided(dl_scene* S, const dl_render_opts* opts, dl_guide* G, int32_t train, float* rgb_out) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        check_opts(opts);
+        need(G != nullptr && G->ctx == ctx, "guide is NULL or belongs to another context");
+        need(rgb_out != nullptr, "rgb_out is NULL");
+        int64_t nf = dl::film_floats(S->dev.cam.w, S->dev.cam.h, opts->filter);
+        size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;
+        ctx->render.film.ensure((size_t)nf * 4);
+        ctx->render.rgb.ensure(nrgb * 4);
+        dl::render_guided(S, *opts, G, ctx->render.film.as<float>(), train != 0);
+        dl::resolve_film(S, ctx->render.film.as<float>(), opts->filter, ctx->render.rgb.as<float>());
+        DL_CUDA(cudaMemcpyAsync(rgb_out, ctx->render.rgb.ptr, nrgb * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        DL_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 int dl_context_set_kernel_timing(dl_context* ctx, int enabled) {
     if (!ctx) return DL_ERR_INVALID_ARG;
     ctx->kernel_timing = enabled != 0;

@@ -28,15 +28,6 @@
 
 namespace dl {
 
-struct GuideRecord {   // one training sample, 48 bytes
-    float in[6];       // position in [0, 1]^3, normal
-    float w[3];        // sampled direction
-    float pdf;         // its sampling pdf (solid angle)
-    float L;           // radiance estimate along w (scalar)
-    float pad;
-};
-static_assert(sizeof(GuideRecord) == 48, "record layout");
-
 // ------------------------------------------------------------- inference
 constexpr int kInferWarps = 4;
 

@@ -49,8 +49,18 @@ struct GuideTile {
     float o[16 * kGOs];    // network output
 };
 
+struct GuideRecord {   // one training sample, 48 bytes
+    float in[6];       // position in [0, 1]^3, normal
+    float w[3];        // sampled direction
+    float pdf;         // its sampling pdf (solid angle)
+    float L;           // radiance estimate along w (scalar)
+    float pad;
+};
+static_assert(sizeof(GuideRecord) == 48, "record layout");
+
 struct GuideNet {
     const __half* w16;   // kGParams halves
+    const float* w32;    // fp32 master (the biases are read from it)
     float3 lo;           // scene bounds: position -> [0, 1]^3
     float3 inv_ext;
     float fraction;      // probability of sampling the learned proposal
@@ -243,6 +253,48 @@ __device__ __forceinline__ float3 mixture_sample(const VmfLobe* L, float u0, flo
     Frame f = make_onb(L[j].mu);
     float3 loc = f3(v * c, v * s, w);
     return normalize(to_world(f, loc));
+}
+
+// Decoded lobes stored as 8 x {mu.x, mu.y, mu.z, kappa, lambda} floats.
+__device__ __forceinline__ void store_lobes(const VmfLobe* L, float* dst) {
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) {
+        dst[5 * j] = L[j].mu.x;
+        dst[5 * j + 1] = L[j].mu.y;
+        dst[5 * j + 2] = L[j].mu.z;
+        dst[5 * j + 3] = L[j].kappa;
+        dst[5 * j + 4] = L[j].lambda;
+    }
+}
+
+__device__ __forceinline__ float stored_mixture_pdf(const float* lob, float3 w) {
+    float p = 0.f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++)
+        p += lob[5 * j + 4] * vmf_pdf(f3(lob[5 * j], lob[5 * j + 1], lob[5 * j + 2]), lob[5 * j + 3], w);
+    return p;
+}
+
+__device__ __forceinline__ float3 stored_mixture_sample(const float* lob, float u0, float2 u) {
+    VmfLobe L[kGLobes];
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) {
+        L[j].mu = f3(lob[5 * j], lob[5 * j + 1], lob[5 * j + 2]);
+        L[j].kappa = lob[5 * j + 3];
+        L[j].lambda = lob[5 * j + 4];
+    }
+    return mixture_sample(L, u0, u);
+}
+
+// Network input of a shading point: position scaled into [0, 1]^3 by the
+// scene bounds, the unit shading normal.
+__device__ __forceinline__ void guide_input(const DevScene& sc, float3 p, float3 n, float* in6) {
+    in6[0] = fminf(fmaxf((p.x - sc.bb_lo[0]) * sc.bb_inv_ext[0], 0.f), 1.f);
+    in6[1] = fminf(fmaxf((p.y - sc.bb_lo[1]) * sc.bb_inv_ext[1], 0.f), 1.f);
+    in6[2] = fminf(fmaxf((p.z - sc.bb_lo[2]) * sc.bb_inv_ext[2], 0.f), 1.f);
+    in6[3] = n.x;
+    in6[4] = n.y;
+    in6[5] = n.z;
 }
 
 }  // namespace dl

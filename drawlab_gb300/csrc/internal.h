@@ -109,6 +109,7 @@ struct RenderCounters {
     alignas(128) unsigned int work_ext;        // chunk cursors of the traversal kernels
     alignas(128) unsigned int work_sh;
     alignas(128) unsigned long long next_path;
+    alignas(128) unsigned int guide_next;      // training records claimed (guided renders)
     alignas(128) unsigned long long stat_ext;
     unsigned long long stat_shadow;
     unsigned long long stat_camera;   // filled on the host: paths started = min(next_path, paths)
@@ -129,6 +130,7 @@ struct RenderBuffers {
     DevBuf sh_o, sh_d, sh_c;
     DevBuf counters, invalid;
     DevBuf samples;   // per-path radiance of the current sample chunk (film gather input)
+    DevBuf grec;      // guided renders: per-slot training-record links (32 B)
     DevBuf requests;  // batch: the pass's request table
     HostBuf host_requests;
     DevBuf batch_films;  // batch: films of requests without a caller film
@@ -187,6 +189,7 @@ struct dl_guide {
     dl_context* ctx = nullptr;
     dl_guide_config cfg{};
     dl::DevBuf w32, w16, grad, m, v, scratch, acts, recs, io_in, io_out;
+    dl::DevBuf pass_recs;   // training records written by a guided render pass
     int64_t step = 0;
 };
 

@@ -71,6 +71,9 @@ struct DevScene {
     // power-proportional emitter pick: per light {alias q, alias index, pick
     // probability, 0}
     const float4* __restrict__ light_pick;
+    // bounds of every vertex: position -> [0, 1]^3 for the guiding network
+    float bb_lo[3];
+    float bb_inv_ext[3];
     int env_light;
     int env_w, env_h;
     int env_visual;

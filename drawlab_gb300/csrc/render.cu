@@ -32,9 +32,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <chrono>
 #include <cstring>
 
 #include "device.cuh"
+#include "guide.cuh"
 #include "internal.h"
 #include "scene.h"
 
@@ -79,6 +81,16 @@ struct DevRequest {
 };
 constexpr int kReqShift = 8;  // path flags: request index << kReqShift | PathFlags
 
+// Guided renders: per slot, the training records of the path's two most
+// recent guided vertices with the throughput after each (a: older, b: newer;
+// record index in w, -1 for none).  Radiance the path gathers later is
+// credited to them divided by that throughput: the estimate of the radiance
+// arriving along the direction sampled there.
+struct __align__(32) GuideRec {
+    float4 a;
+    float4 b;
+};
+
 struct RenderParams {
     DevRequest r0;                 // the request of a single render
     const DevRequest* reqs;        // batch: request table (pid_first ascending)
@@ -100,6 +112,12 @@ struct RenderParams {
     float* li_L;
     float* li_pos;
     unsigned long long total_paths;
+    // guided renders
+    int guided;
+    GuideNet gnet;
+    GuideRec* grec;
+    GuideRecord* grecords;
+    int grecord_cap;
 };
 
 template <bool kMulti>
@@ -140,6 +158,16 @@ __device__ __forceinline__ unsigned long long warp_claim(unsigned long long* cou
     if (lane_id() == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
     base = __shfl_sync(0xffffffffu, base, leader);
     return pred ? base + (unsigned long long)__popc(mask & ((1u << lane_id()) - 1u)) : ~0ull;
+}
+
+__device__ __forceinline__ unsigned long long warp_claim_u32(unsigned int* counter, bool pred) {
+    unsigned mask = __ballot_sync(0xffffffffu, pred);
+    if (mask == 0) return ~0ull;
+    int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return pred ? (unsigned long long)base + __popc(mask & ((1u << lane_id()) - 1u)) : ~0ull;
 }
 
 __device__ __forceinline__ Pcg32 load_rng(const uint4& r) {
@@ -197,6 +225,12 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     mr.rng = store_rng(g);
     P.meta[slot] = mr;
     if (P.mode == 1) P.pos[slot] = ps;
+    if (P.guided) {
+        GuideRec gr;
+        gr.a = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        gr.b = gr.a;
+        P.grec[slot] = gr;
+    }
 }
 
 // Radiance of ended path `pid` (slot `slot`): into the sample buffer at its
@@ -225,6 +259,24 @@ __device__ __forceinline__ void add_to_sample(const RenderParams& P, unsigned lo
         float4 s = P.samples[pid];
         P.samples[pid] = make_float4(__fadd_rn(s.x, c.x), __fadd_rn(s.y, c.y), __fadd_rn(s.z, c.z), s.w);
     }
+}
+
+// Radiance `c` reached the path: credit it to the training records of its
+// guided vertices (the newer one too if `both`), divided by the throughput
+// after each vertex (mean over the channels it is non-zero in).
+__device__ __forceinline__ void credit_one(const RenderParams& P, float4 t, float3 c) {
+    int idx = __float_as_int(t.w);
+    if (idx < 0) return;
+    float s = 0.f;
+    int k = 0;
+    if (t.x > 0.f) { s += c.x / t.x; k++; }
+    if (t.y > 0.f) { s += c.y / t.y; k++; }
+    if (t.z > 0.f) { s += c.z / t.z; k++; }
+    if (k > 0 && isfinite(s)) P.grecords[idx].L += s / (float)k;
+}
+__device__ __forceinline__ void credit(const RenderParams& P, const GuideRec& gr, float3 c, bool both) {
+    credit_one(P, gr.a, c);
+    if (both) credit_one(P, gr.b, c);
 }
 
 // Claim new path indices for the lanes in `want`, start them; returns true
@@ -578,6 +630,8 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                             pr.L = make_float4(__fadd_rn(pr.L.x, c.x), __fadd_rn(pr.L.y, c.y),
                                                __fadd_rn(pr.L.z, c.z), pr.L.w);
                             P.path[target] = pr;
+                            // NEE at the newest guided vertex feeds the record before it
+                            if (P.guided) credit(P, P.grec[target], xyz(c), false);
                         } else {
                             add_to_sample(P, (unsigned long long)(unsigned)(-1 - target), c);
                         }
@@ -681,7 +735,9 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
                         ep = with_pick_pdf(R, sc.env_light, ep);
                         w = mis_weight(pr.L.w, ep);
                     }
-                    L = add(L, mul(scale(f3(pr.tp.x, pr.tp.y, pr.tp.z), w), le));
+                    float3 c = mul(scale(f3(pr.tp.x, pr.tp.y, pr.tp.z), w), le);
+                    L = add(L, c);
+                    if (P.guided) credit(P, P.grec[slot], c, true);
                 }
             }
             store_sample(P, path_index(m), L, slot);
@@ -699,32 +755,61 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 // starts a new camera path at once; a shadow ray it emitted on the way adds
 // to the stored sample when traced.  Mirror and dielectric still draw the NEE
 // sample (their eval and pdf are zero: no contribution, no shadow ray).
-template <int T, bool kMulti>
+//
+// kGuided (diffuse, Beckmann, GGX in a guided render): the warp evaluates the
+// guiding network for its 32 shading points on the tensor cores (two 16-row
+// tiles), and each path samples its next direction by one-sample MIS between
+// the learned vMF mixture (probability `fraction`) and the BSDF, weighting
+// by f cos / (fraction q + (1 - fraction) p_bsdf); NEE's MIS weight uses the
+// same combined pdf.  The vertex becomes a training record.
+constexpr int kGuidedWarps = 2;  // 64-thread blocks for the guided kernels
+struct GuideWarpSmem {
+    GuideTile tile;
+    float lobes[32 * kGOut];
+};
+constexpr size_t kGuidedSmem = sizeof(GuideWarpSmem) * kGuidedWarps;
+
+template <int T, bool kMulti, bool kGuided>
 __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int q = p ^ 1;
+    const int lane = lane_id();
     const int n = P.cnt->mat[p][T].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
-        int i = i0 + lane_id();
+        int i = i0 + lane;
         bool active = i < n;
         int slot = active ? P.mat_q[T][i] : 0;
         bool cont = false, emit = false, done = false;
         float4 sh_o = make_float4(0.f, 0.f, 0.f, 0.f), sh_d = sh_o, sh_c = sh_o;
+        // ---- phase 1: emitter hit, Russian roulette, depth limit
+        RayRec ray;
+        PathRec pr;
+        MetaRec mr;
+        Pcg32 g;
+        HitInfo h;
+        GuideRec gr;
+        float3 tp = f3(0.f, 0.f, 0.f), Lr = tp, dir = tp;
+        float eta = 1.f;
+        int depth = 0, flags = 0, rid = 0;
+        unsigned long long pid = 0;
         if (active) {
             float4 hit = P.hit[slot].h;
-            RayRec ray = P.ray[slot];
-            PathRec pr = P.path[slot];
-            MetaRec mr = P.meta[slot];
-            Pcg32 g = load_rng(mr.rng);
-            unsigned long long pid = path_index(mr.m);
-            float3 tp = f3(pr.tp.x, pr.tp.y, pr.tp.z);
-            float eta = pr.tp.w;
-            float3 Lr = f3(pr.L.x, pr.L.y, pr.L.z);
-            float3 dir = xyz(ray.d);
-            int depth = mr.m.x, flags = mr.m.y;
-            const int rid = flags >> kReqShift;
+            ray = P.ray[slot];
+            pr = P.path[slot];
+            mr = P.meta[slot];
+            if (P.guided) gr = P.grec[slot];
+            g = load_rng(mr.rng);
+            pid = path_index(mr.m);
+            tp = f3(pr.tp.x, pr.tp.y, pr.tp.z);
+            eta = pr.tp.w;
+            Lr = f3(pr.L.x, pr.L.y, pr.L.z);
+            dir = xyz(ray.d);
+            depth = mr.m.x;
+            flags = mr.m.y;
+            rid = flags >> kReqShift;
             const DevRequest& R = request<kMulti>(P, rid);
             const DevScene& sc = R.sc;
-            HitInfo h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
+            h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
             int light = sc.meshes[h.mesh].light;
             if (flags & PF_CAMERA) {
                 if (light >= 0 && dot(h.sh.n, neg(dir)) > 0.f) Lr = add(Lr, mul(tp, ld3(sc.lights[light].radiance)));
@@ -740,7 +825,9 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     float ep = dp != 0.f ? __fdiv_rn(__fmul_rn(__fmul_rn(Lt.pA, dist), dist), dp) : 0.f;
                     ep = with_pick_pdf(R, light, ep);
                     float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(pr.L.w, ep) : 1.f;
-                    Lr = add(Lr, mul(scale(tp, w), le));
+                    float3 c = mul(scale(tp, w), le);
+                    Lr = add(Lr, c);
+                    if (P.guided) credit(P, gr, c, true);
                 }
                 if (depth > R.rr_depth) {
                     float pq = fminf(maxc(scale(scale(tp, eta), eta)), 0.99f);
@@ -750,6 +837,36 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 depth += 1;
             }
             if (!done && R.max_depth > 0 && depth >= R.max_depth) done = true;
+        }
+        // ---- phase 2 (guided): the network on the warp's shading points
+        const bool sampling = active && !done;
+        float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float* lob = nullptr;
+        if (kGuided) {
+            GuideWarpSmem& W = reinterpret_cast<GuideWarpSmem*>(dyn_smem)[threadIdx.x >> 5];
+            lob = W.lobes + lane * kGOut;
+            if (sampling) guide_input(request<kMulti>(P, rid).sc, h.p, normalize(h.sh.n), in6);
+            if (__any_sync(0xffffffffu, sampling)) {
+                for (int half = 0; half < 2; half++) {
+                    if ((lane >> 4) == half) encode_input(in6, W.tile.x + (lane & 15) * kGXs);
+                    __syncwarp();
+                    forward16(W.tile, P.gnet.w16, P.gnet.w32, lane);
+                    if ((lane >> 4) == half && sampling) {
+                        VmfLobe L[kGLobes];
+                        decode_lobes(W.tile.o + (lane & 15) * kGOs, L);
+                        store_lobes(L, lob);
+                    }
+                    __syncwarp();
+                }
+            }
+        }
+        // ---- phase 3: NEE and the next direction
+        bool record = false;
+        float rec_pdf = 0.f;
+        float3 nd = f3(0.f, 0.f, 0.f);
+        if (active) {
+            const DevRequest& R = request<kMulti>(P, rid);
+            const DevScene& sc = R.sc;
             float prev_pdf = pr.L.w;
             int target = slot;
             if (!done) {
@@ -757,6 +874,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 Frame fr = T == MAT_ANISO_GGX ? make_onb(normalize(h.sh.n)) : h.sh;
                 float3 wi = to_local(fr, neg(normalize(dir)));
                 if (T == MAT_ANISO_GGX) wi = normalize(wi);
+                const float alpha = kGuided ? P.gnet.fraction : 0.f;
                 float2 s_nee = g.next2d();
                 float3 c = f3(0.f, 0.f, 0.f);
                 float3 ld = c;
@@ -777,6 +895,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                         q1.eta = 1.f;
                         float3 bv = bsdf_eval<T>(m, q1);
                         float bp = bsdf_pdf<T>(m, q1);
+                        if (kGuided) bp = alpha * stored_mixture_pdf(lob, ld) + (1.f - alpha) * bp;
                         float w = (delta && (R.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
                         c = mul(mul(scale(tp, w), bv), espec);
                         emit = c.x != 0.f || c.y != 0.f || c.z != 0.f;
@@ -787,13 +906,37 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 q2.wo = f3(0.f, 0.f, 0.f);
                 q2.eta = 1.f;
                 q2.measure = M_UNKNOWN;
-                float3 f = bsdf_sample<T>(m, q2, g.next2d());
-                tp = mul(tp, f);
-                eta = __fmul_rn(eta, q2.eta);
-                prev_pdf = bsdf_pdf<T>(m, q2);
+                if (kGuided) {
+                    // one-sample MIS between the learned mixture and the BSDF
+                    float3 fcos_over_p;
+                    if (g.next_float() < alpha) {
+                        float u0 = g.next_float();
+                        nd = stored_mixture_sample(lob, u0, g.next2d());
+                        q2.wo = to_local(fr, nd);
+                        q2.measure = M_SOLID;
+                        float3 fv = bsdf_eval<T>(m, q2);
+                        float pb = bsdf_pdf<T>(m, q2);
+                        prev_pdf = alpha * stored_mixture_pdf(lob, nd) + (1.f - alpha) * pb;
+                        fcos_over_p = prev_pdf > 0.f ? scale(fv, fmaxf(q2.wo.z, 0.f) / prev_pdf) : f3(0.f, 0.f, 0.f);
+                    } else {
+                        float3 wgt = bsdf_sample<T>(m, q2, g.next2d());
+                        float pb = bsdf_pdf<T>(m, q2);
+                        nd = to_world(fr, q2.wo);
+                        if (T == MAT_ANISO_GGX) nd = normalize(nd);
+                        prev_pdf = alpha * stored_mixture_pdf(lob, nd) + (1.f - alpha) * pb;
+                        fcos_over_p = prev_pdf > 0.f ? scale(wgt, pb / prev_pdf) : f3(0.f, 0.f, 0.f);
+                    }
+                    tp = mul(tp, fcos_over_p);
+                    rec_pdf = prev_pdf;
+                } else {
+                    float3 f = bsdf_sample<T>(m, q2, g.next2d());
+                    tp = mul(tp, f);
+                    eta = __fmul_rn(eta, q2.eta);
+                    prev_pdf = bsdf_pdf<T>(m, q2);
+                    nd = to_world(fr, q2.wo);
+                    if (T == MAT_ANISO_GGX) nd = normalize(nd);
+                }
                 flags = (rid << kReqShift) | (is_diffuse(T) ? PF_PREV_DIFFUSE : 0);
-                float3 nd = to_world(fr, q2.wo);
-                if (T == MAT_ANISO_GGX) nd = normalize(nd);
                 if (tp.x == 0.f && tp.y == 0.f && tp.z == 0.f) {
                     done = true;  // every later contribution is zero
                 } else {
@@ -802,6 +945,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     nr.d = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
                     P.ray[slot] = nr;
                     cont = true;
+                    record = kGuided && P.grecords != nullptr;
                 }
                 if (emit) {
                     if (done) target = -1 - (int)pid;  // lands in the stored sample
@@ -821,6 +965,28 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 nmr.m = make_int4(depth, flags, mr.m.z, mr.m.w);
                 nmr.rng = store_rng(g);
                 P.meta[slot] = nmr;
+            }
+        }
+        // ---- phase 4 (guided): training record of the vertex
+        if (kGuided) {
+            unsigned long long ri = warp_claim_u32(&P.cnt->guide_next, record);
+            if (record) {
+                int idx = ri < (unsigned long long)P.grecord_cap ? (int)ri : -1;
+                if (idx >= 0) {
+                    GuideRecord rc;
+                    for (int k = 0; k < 6; k++) rc.in[k] = in6[k];
+                    rc.w[0] = nd.x;
+                    rc.w[1] = nd.y;
+                    rc.w[2] = nd.z;
+                    rc.pdf = rec_pdf;
+                    rc.L = 0.f;
+                    rc.pad = 0.f;
+                    P.grecords[idx] = rc;
+                }
+                GuideRec ngr;
+                ngr.a = gr.b;
+                ngr.b = make_float4(tp.x, tp.y, tp.z, __int_as_float(idx));
+                P.grec[slot] = ngr;
             }
         }
         int sp = warp_push(&P.cnt->shadow[q], emit);
@@ -994,6 +1160,17 @@ size_t RenderBuffers::device_bytes() const {
 
 constexpr int kKernelsPerIteration = 8;
 
+// The material kernel of type T: guided (64-thread blocks, the network's
+// tiles in dynamic shared memory) for the non-delta BSDFs of a guided render.
+template <int T, bool kMulti>
+static void launch_material(const RenderParams& P, int p, cudaStream_t st, int wb, int th) {
+    constexpr bool kCanGuide = !kMulti && T != MAT_MIRROR && T != MAT_DIELECTRIC;
+    if (kCanGuide && P.guided)
+        k_material<T, false, true><<<wb * (th / (32 * kGuidedWarps)), 32 * kGuidedWarps, kGuidedSmem, st>>>(P, p);
+    else
+        k_material<T, kMulti, false><<<wb, th, 0, st>>>(P, p);
+}
+
 // Launches one wavefront iteration (8 kernels) with the context's launch
 // shape.  `ev`, when given, holds 8 events bracketing extend, shadow, the
 // material kernels, miss (kernels then run one after another).  Otherwise,
@@ -1015,11 +1192,11 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
         k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
-        k_material<MAT_DIFFUSE, kMulti><<<wb, th, 0, fj->aux[0]>>>(P, p);
-        k_material<MAT_MIRROR, kMulti><<<wb, th, 0, fj->aux[1]>>>(P, p);
-        k_material<MAT_DIELECTRIC, kMulti><<<wb, th, 0, fj->aux[2]>>>(P, p);
-        k_material<MAT_MICROFACET, kMulti><<<wb, th, 0, fj->aux[3]>>>(P, p);
-        k_material<MAT_ANISO_GGX, kMulti><<<wb, th, 0, fj->aux[4]>>>(P, p);
+        launch_material<MAT_DIFFUSE, kMulti>(P, p, fj->aux[0], wb, th);
+        launch_material<MAT_MIRROR, kMulti>(P, p, fj->aux[1], wb, th);
+        launch_material<MAT_DIELECTRIC, kMulti>(P, p, fj->aux[2], wb, th);
+        launch_material<MAT_MICROFACET, kMulti>(P, p, fj->aux[3], wb, th);
+        launch_material<MAT_ANISO_GGX, kMulti>(P, p, fj->aux[4], wb, th);
         for (int i = 0; i < dl_context::kAux; i++) {
             cudaEventRecord(fj->join_ev[i], fj->aux[i]);
             cudaStreamWaitEvent(st, fj->join_ev[i], 0);
@@ -1028,11 +1205,11 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
     }
     k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
     if (ev) { cudaEventRecord(ev[7], st); cudaEventRecord(ev[4], st); }
-    k_material<MAT_DIFFUSE, kMulti><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_MIRROR, kMulti><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_DIELECTRIC, kMulti><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_MICROFACET, kMulti><<<wb, th, 0, st>>>(P, p);
-    k_material<MAT_ANISO_GGX, kMulti><<<wb, th, 0, st>>>(P, p);
+    launch_material<MAT_DIFFUSE, kMulti>(P, p, st, wb, th);
+    launch_material<MAT_MIRROR, kMulti>(P, p, st, wb, th);
+    launch_material<MAT_DIELECTRIC, kMulti>(P, p, st, wb, th);
+    launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, th);
+    launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, th);
     if (ev) cudaEventRecord(ev[5], st);
 }
 
@@ -1285,6 +1462,90 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
     acc.stat_invalid = invalid;
     finish_stats(ctx, acc, invalid, iters, launches, kms);
     if (out_counters) *out_counters = acc;
+}
+
+// Guided progressive render: passes of 1, 1, 2, 4, ... samples per pixel
+// (the last takes the rest).  During a pass every guided vertex writes a
+// training record; after the pass (train) the records feed steps_per_pass
+// Adam steps on consecutive batches, and the next pass samples with the
+// updated network.  All passes add to one film: each sample is an unbiased
+// estimate whichever network drew it.
+void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_film, bool train) {
+    dl_context* ctx = S->ctx;
+    cudaStream_t st = ctx->stream;
+    const DevCamera& cam = S->dev.cam;
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.r0 = make_request(S, o);
+    P.mode = 0;
+    const unsigned long long npix = (unsigned long long)cam.w * cam.h;
+    const int spp = std::max(o.spp, 1);
+    const int chunk_spp = (int)std::max<size_t>(1, std::min<size_t>(spp, kSampleBufferBytes / (npix * 16)));
+    const int64_t cap = pool_capacity(ctx, o.max_paths_in_flight, npix * (unsigned long long)chunk_spp);
+    RenderBuffers& B = ctx->render;
+    B.ensure(cap);
+    B.grec.ensure((size_t)cap * 32);
+    bind_pool(P, B);
+    B.samples.ensure((size_t)npix * chunk_spp * 16);
+    P.samples = B.samples.as<float4>();
+    P.guided = 1;
+    P.gnet.w16 = G->w16.as<__half>();
+    P.gnet.w32 = G->w32.as<float>();
+    P.gnet.fraction = G->cfg.guide_fraction;
+    P.grec = B.grec.as<GuideRec>();
+    const int64_t rec_cap = std::min<int64_t>((int64_t)G->cfg.batch * std::max(1, G->cfg.steps_per_pass), 1 << 23);
+    if (train) {
+        G->pass_recs.ensure((size_t)rec_cap * sizeof(GuideRecord));
+        P.grecords = G->pass_recs.as<GuideRecord>();
+        P.grecord_cap = (int)rec_cap;
+    }
+    double kms[4] = {0, 0, 0, 0};
+    int64_t launches = 0, iters = 0, records = 0;
+    double train_ms = 0.0;
+    RenderCounters acc;
+    std::memset(&acc, 0, sizeof(acc));
+    DL_CUDA(cudaEventRecord(ctx->ev0, st));
+    FilmParams F = film_params(cam, P.r0, o.filter, d_film, P.samples, B.invalid.as<unsigned long long>());
+    DL_CUDA(cudaMemsetAsync(F.invalid, 0, sizeof(unsigned long long), st));
+    dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
+    RenderCounters* hc = B.host_counters.as<RenderCounters>();
+    int done = 0;
+    for (int pass = 0; done < spp; pass++) {
+        int ns = std::min(std::min(pass == 0 ? 1 : (1 << (pass - 1)), spp - done), chunk_spp);
+        P.r0.spp_offset = o.spp_offset + done;
+        P.total_paths = npix * (unsigned long long)ns;
+        run_wavefront(ctx, P, cap, false, false, kms, launches, iters, acc);
+        const int64_t nrec = train ? std::min<int64_t>(hc->guide_next, rec_cap) : 0;
+        F.nspp = ns;
+        F.s_first = o.spp_offset + done;
+        F.accumulate = done > 0;
+        k_film_gather<<<fgrid, 256, 0, st>>>(F);
+        launches += 1;
+        DL_CUDA(cudaGetLastError());
+        done += ns;
+        if (train && nrec >= 16 && done < spp) {
+            auto h0 = std::chrono::steady_clock::now();
+            const int64_t bs = std::min<int64_t>(G->cfg.batch, nrec);
+            for (int k = 0; k < G->cfg.steps_per_pass; k++) {
+                int64_t off = ((int64_t)k * bs) % nrec;
+                int64_t cnt = std::min<int64_t>(bs, nrec - off);
+                DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, kGuideParams * 4, st));
+                guide_gradient(G, P.grecords + off, cnt);
+                guide_adam(G);
+            }
+            DL_CUDA(cudaStreamSynchronize(st));
+            train_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+        }
+        records += nrec;
+    }
+    unsigned long long* hinv =
+        reinterpret_cast<unsigned long long*>(B.host_counters.as<char>() + sizeof(RenderCounters));
+    DL_CUDA(cudaMemcpyAsync(hinv, F.invalid, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    acc.stat_invalid = *hinv;
+    finish_stats(ctx, acc, *hinv, iters, launches, kms);
+    ctx->stats.guide_records = records;
+    ctx->stats.guide_train_ms = train_ms;
 }
 
 // Batch of requests in one wavefront: every pass renders, for each request

@@ -328,6 +328,11 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
         double r2 = 0.0;
         if (any)
             for (int k = 0; k < 3; k++) r2 += 0.25 * (hi[k] - lo[k]) * (hi[k] - lo[k]);
+        for (int k = 0; k < 3; k++) {
+            double ext = any ? hi[k] - lo[k] : 0.0;
+            S->dev.bb_lo[k] = any ? (float)lo[k] : 0.f;
+            S->dev.bb_inv_ext[k] = ext > 0.0 ? (float)(1.0 / ext) : 0.f;
+        }
         for (int l = 0; l < nl; l++) {
             const dl_light_desc& L = lights[l];
             double m = std::max(L.radiance[0], std::max(L.radiance[1], L.radiance[2]));

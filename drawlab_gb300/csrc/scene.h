@@ -35,6 +35,8 @@ void guide_gradient(dl_guide* G, const void* d_recs, int64_t n);
 void guide_adam(dl_guide* G);
 float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps);
 void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n);
+// Guided progressive render into d_film (render.cu).
+void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_film, bool train);
 
 // XML scene loading (xml.cpp): fills arrays and default render options.
 struct XmlScene;

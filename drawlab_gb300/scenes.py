@@ -495,3 +495,81 @@ def env_spheres(width: int = 96, height: int = 64, spp: int = 4, max_depth: int 
     s.camera = Camera(width=width, height=height, eye=(0.0, 2.5, 9.0), lookat=(0.0, 0.5, 0.0),
                       up=(0.0, 1.0, 0.0), fov=40.0)
     return s
+
+
+def displaced_grid(center, size, n: int, height: float, seed: int = 0):
+    """n x n grid over size=(sx, sz) at `center`, displaced along +y by a sum
+    of seeded sines: 2 n^2 triangles, smooth normals."""
+    rng = np.random.default_rng(seed)
+    xs = np.linspace(-0.5, 0.5, n + 1)
+    X, Z = np.meshgrid(xs * size[0], xs * size[1], indexing="xy")
+    Y = np.zeros_like(X)
+    for _ in range(4):
+        fx, fz = rng.uniform(1.0, 6.0, 2)
+        ph = rng.uniform(0, 2 * np.pi, 2)
+        Y += np.sin(fx * X * 2 * np.pi / size[0] + ph[0]) * np.cos(fz * Z * 2 * np.pi / size[1] + ph[1])
+    Y = height * (Y / max(1e-9, np.abs(Y).max()) * 0.5 + 0.5)
+    P = np.stack([X, Y, Z], axis=-1).reshape(-1, 3) + np.asarray(center, np.float64)
+    # normals from the height field gradient
+    gy, gx = np.gradient(Y, xs * size[1], xs * size[0])
+    N = np.stack([-gx, np.ones_like(Y), -gy], axis=-1).reshape(-1, 3)
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    i = np.arange(n)[:, None] * (n + 1) + np.arange(n)[None, :]
+    a, b, c, d = i, i + 1, i + n + 1, i + n + 2
+    F = np.concatenate([np.stack([a, c, b], -1).reshape(-1, 3), np.stack([b, c, d], -1).reshape(-1, 3)])
+    return P.astype(np.float32), F.astype(np.uint32), N.astype(np.float32)
+
+
+def guiding_room(width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 12, grid: int = 700,
+                 env_width: int = 2048, env_height: int = 1024, seed: int = 5) -> SceneData:
+    """A closed 10 x 3 x 6 m room lit only through a 1 x 1 m window by the
+    procedural sky (sky gradient + 0.5-degree sun of peak 1e4): diffuse walls
+    0.2-0.8, furniture of cuboids (diffuse and GGX 0.1-0.4) and two
+    displaced-grid 'sculptures' of 2 grid^2 triangles each (grid 700: about
+    2M triangles in all).  The camera looks from the far end towards the
+    window wall."""
+    rng = np.random.default_rng(seed)
+    s = SceneData("guiding_room", spp=spp, max_depth=max_depth, rr_depth=3)
+    X0, X1, Y0, Y1, Z0, Z1 = -5.0, 5.0, 0.0, 3.0, -3.0, 3.0
+
+    def diffuse(lo=0.2, hi=0.8):
+        return s.add_material(Material(type=abi.DL_MAT_DIFFUSE, albedo=tuple(rng.uniform(lo, hi, 3))))
+
+    def quad(pos, e0, e1, m):
+        p, f, n = rectangle(pos, e0, e1)
+        s.add_mesh(Mesh(p, f, n, material=m))
+
+    # floor (+y), ceiling (-y), side walls, back wall (z = Z1, -z), window wall (z = Z0, +z)
+    quad((X0, Y0, Z1), (X1 - X0, 0, 0), (0, 0, Z0 - Z1), diffuse(0.4, 0.7))
+    quad((X0, Y1, Z0), (X1 - X0, 0, 0), (0, 0, Z1 - Z0), diffuse(0.6, 0.8))
+    quad((X0, Y0, Z0), (0, 0, Z1 - Z0), (0, Y1 - Y0, 0), diffuse())
+    quad((X1, Y0, Z1), (0, 0, Z0 - Z1), (0, Y1 - Y0, 0), diffuse())
+    quad((X1, Y0, Z1), (X0 - X1, 0, 0), (0, Y1 - Y0, 0), diffuse())
+    wall = diffuse(0.5, 0.8)
+    wx0, wx1, wy0, wy1 = -0.5, 0.5, 1.3, 2.3        # the window opening
+    quad((X0, Y0, Z0), (wx0 - X0, 0, 0), (0, Y1 - Y0, 0), wall)
+    quad((wx1, Y0, Z0), (X1 - wx1, 0, 0), (0, Y1 - Y0, 0), wall)
+    quad((wx0, Y0, Z0), (wx1 - wx0, 0, 0), (0, wy0 - Y0, 0), wall)
+    quad((wx0, wy1, Z0), (wx1 - wx0, 0, 0), (0, Y1 - wy1, 0), wall)
+    # furniture
+    for k in range(6):
+        sx, sy, sz = rng.uniform(0.4, 1.4), rng.uniform(0.3, 1.2), rng.uniform(0.4, 1.2)
+        cx, cz = rng.uniform(X0 + 1, X1 - 1), rng.uniform(Z0 + 1.2, Z1 - 1)
+        if k % 2 == 0:
+            m = diffuse()
+        else:
+            a = float(rng.uniform(0.1, 0.4))
+            m = s.add_material(Material(type=abi.DL_MAT_ANISO_GGX, albedo=tuple(rng.uniform(0.1, 0.5, 3)),
+                                        specular=(0.5, 0.5, 0.5), alpha=(a, a)))
+        P, F, N = cuboid((cx, Y0 + 0.5 * sy + 1e-3, cz), (sx, sy, sz), float(rng.uniform(0, 90)))
+        s.add_mesh(Mesh(P, F, N, material=m))
+    for k, (cx, cz) in enumerate([(-2.5, 0.5), (2.5, 1.0)]):
+        m = diffuse() if k == 0 else s.add_material(Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0.3, 0.3, 0.3),
+                                                             specular=(0.6, 0.6, 0.6), alpha=(0.25, 0.25)))
+        P, F, N = displaced_grid((cx, Y0 + 2e-3, cz), (2.0, 2.0), grid, 0.6, seed=seed + k)
+        s.add_mesh(Mesh(P, F, N, material=m))
+    sky = sky_envmap(env_width, env_height, sun_dir=(0.25, 0.55, -0.8), sun_peak=1.0e4, sun_radius_deg=0.5)
+    s.lights.append(Light(type=abi.DL_LIGHT_ENVMAP, env_rgb=sky, env_scale=1.0, env_visual=1))
+    s.camera = Camera(width=width, height=height, eye=(0.0, 1.6, 2.7), lookat=(0.0, 1.0, -3.0),
+                      up=(0.0, 1.0, 0.0), fov=60.0)
+    return s

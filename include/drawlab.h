@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 2
+#define DL_ABI_VERSION 3
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -354,6 +354,14 @@ int dl_guide_forward(dl_guide* guide, int64_t n, const float* inputs, float* out
 int dl_guide_gradient(dl_guide* guide, int64_t n, const float* records, float* grad, float* loss);
 int dl_guide_train(dl_guide* guide, int64_t n, const float* records, int32_t steps, float* loss);
 
+/* Progressive guided render (as dl_render, image to host): passes of 1, 1,
+ * 2, 4, ... samples per pixel; with `train` set, every pass writes training
+ * records at its guided vertices (diffuse, Beckmann, GGX surfaces; radiance
+ * gathered later on the path credited to the two most recent ones) and the
+ * guide takes steps_per_pass Adam steps on them before the next pass.  With
+ * `train` 0 the network is frozen.  All samples add to one film. */
+int dl_render_guided(dl_scene* scene, const dl_render_opts* opts, dl_guide* guide, int32_t train, float* rgb_out);
+
 /* --------------------------------------------------------------- statistics */
 
 typedef struct dl_stats {
@@ -369,9 +377,11 @@ typedef struct dl_stats {
      * enabled, see dl_context_set_kernel_timing). */
     double extend_ms;          /* closest-hit traversal */
     double shadow_ms;          /* any-hit traversal */
-    double shade_ms;           /* shading, NEE, BSDF sampling, film splat */
-    double retire_ms;          /* deferred path completion */
+    double shade_ms;           /* the material kernels (emitter hit, RR, NEE, BSDF sampling) */
+    double retire_ms;          /* the miss kernel (envmap, sample store, new camera paths) */
     int64_t kernel_launches;   /* kernels launched by the last render */
+    int64_t guide_records;     /* training records written by the last guided render */
+    double guide_train_ms;     /* host-timed training of the last guided render */
 } dl_stats;
 
 /* Enable (1) or disable (0) per-kernel event timing on a context. */

@@ -1,0 +1,79 @@
+"""Guided rendering (dl_render_guided): the learned vMF-mixture proposal in
+one-sample MIS with BSDF sampling stays unbiased (frozen random network and
+online training both converge to the plain render) and, on the room lit
+through a window, beats plain BSDF + NEE at equal time."""
+import numpy as np
+import pytest
+
+from drawlab_gb300 import abi, api, metrics, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return api.Context(0)
+
+
+def room(w, h, grid=16):
+    return scenes.guiding_room(width=w, height=h, grid=grid, env_width=512, env_height=256)
+
+
+def test_guided_render_is_unbiased(ctx):
+    # per-pixel means over 8 independent renders, guided vs plain: |z| > 3
+    # stays at the normal-tail rate, with a frozen (random) network and with
+    # online training
+    es = api.Scene.from_data(ctx, scenes.env_spheres(width=48, height=32))
+    K = 8
+    plain = np.stack([es.render(abi.make_opts(spp=256, max_depth=8, seed=100 + k)) for k in range(K)])
+    frozen = np.stack([es.render_guided(abi.make_opts(spp=256, max_depth=8, seed=200 + k), api.Guide(ctx, seed=9),
+                                        train=False) for k in range(K)])
+    trained = np.stack([es.render_guided(abi.make_opts(spp=256, max_depth=8, seed=300 + k),
+                                         api.Guide(ctx, seed=20 + k)) for k in range(K)])
+    assert ctx.stats().guide_records > 0
+    for x in (frozen, trained):
+        assert np.isfinite(x).all()
+        se = np.sqrt(plain.var(0, ddof=1) / K + x.var(0, ddof=1) / K) + 1e-7
+        z = (x.mean(0) - plain.mean(0)) / se
+        assert np.mean(np.abs(z) > 3) < 0.03 and abs(z.mean()) < 0.2, (np.mean(np.abs(z) > 3), z.mean())
+
+
+def test_guided_room_mean_matches_plain(ctx):
+    # the window-lit room: image means of guided renders within the spread
+    # of plain renders of the same total samples (the sun patch makes single
+    # renders noisy: plain 4096-spp means vary by several percent)
+    gs = api.Scene.from_data(ctx, room(48, 27))
+    ref = np.mean([gs.render(abi.make_opts(spp=4096, max_depth=12, seed=s)).mean() for s in (1, 2, 3)])
+    got = np.mean([gs.render_guided(abi.make_opts(spp=1024, max_depth=12, seed=s), api.Guide(ctx, seed=s)).mean()
+                   for s in (7, 8, 9)])
+    assert abs(got - ref) / ref < 0.08, (got, ref)
+
+
+def test_training_changes_the_network(ctx):
+    gs = api.Scene.from_data(ctx, room(32, 18))
+    g = api.Guide(ctx, seed=7)
+    p0 = g.params()
+    gs.render_guided(abi.make_opts(spp=16, max_depth=12, seed=1), g)
+    p1 = g.params()
+    assert np.isfinite(p1).all() and np.abs(p1 - p0).max() > 1e-4
+    g2 = api.Guide(ctx, seed=7)
+    gs.render_guided(abi.make_opts(spp=16, max_depth=12, seed=1), g2, train=False)
+    np.testing.assert_array_equal(g2.params(), p0)
+
+
+def test_guided_beats_plain_at_equal_time(ctx):
+    W, H = 96, 54
+    gs = api.Scene.from_data(ctx, room(W, H, grid=32))
+    ref = gs.render(abi.make_opts(spp=16384, max_depth=12, seed=100))
+    spp_g = 256
+    g = api.Guide(ctx, seed=11)
+    img_g = gs.render_guided(abi.make_opts(spp=spp_g, max_depth=12, seed=7), g)
+    t_g = ctx.stats().render_ms
+    gs.render(abi.make_opts(spp=64, max_depth=12, seed=8))
+    t_p64 = ctx.stats().render_ms
+    spp_p = max(1, int(round(64 * t_g / t_p64)))
+    img_p = gs.render(abi.make_opts(spp=spp_p, max_depth=12, seed=9))
+    e_g, e_p = metrics.relmse(img_g, ref), metrics.relmse(img_p, ref)
+    print("equal time: guided %d spp %.1f ms relMSE %.4g | plain %d spp relMSE %.4g | ratio %.2f"
+          % (spp_g, t_g, e_g, spp_p, e_p, e_p / e_g))
+    assert e_g < e_p
