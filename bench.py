@@ -190,9 +190,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=WORKLOAD["spp"])
+    ap.add_argument("--workload", default="material_spheres", choices=["material_spheres", "batch", "guided"],
+                    help="material_spheres: the headline frame; batch: 64 requests in one wavefront; "
+                         "guided: learned proposal vs plain at equal time")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "guided":
+        return run_guided(args)
 
     ws, rank, local = dist_env()
     import torch
@@ -332,6 +339,129 @@ def main():
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def _device_setup():
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return None
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__ as ge
+    ge.build()
+    return local
+
+
+def run_batch(args):
+    """64 requests (seed 4) of 1k-2M-triangle scenes, 128^2..1080p, 4..256
+    spp, half under the 2048x1024 sky, rendered by one dl_render_batch call
+    per step (images to host memory).  The launch shape comes from
+    dl_autotune on an eighth of the samples, outside the timed region."""
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import abi, api, scenes
+    scene_list, reqs = scenes.batch_workload(seed=4)
+    ctx = api.Context(local)
+    gscenes = [api.Scene.from_data(ctx, s) for s in scene_list]
+    items = [(gscenes[si], abi.make_opts(spp=spp, max_depth=8, seed=17 + k), cam)
+             for k, (si, spp, cam) in enumerate(reqs)]
+    samples = sum(c.width * c.height * spp for _, spp, c in reqs)
+    t_tune = time.perf_counter()
+    tune, trials = ctx.autotune(items, trial_spp=0)
+    t_tune = time.perf_counter() - t_tune
+    for _ in range(args.warmup):
+        ctx.render_batch(items)
+    dev_ms, wall, launches = 0.0, 0.0, 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ctx.render_batch(items)
+            wall += time.perf_counter() - t0
+            st = ctx.stats()
+            dev_ms += st.render_ms
+            launches += st.kernel_launches
+    ck = clocks.summary()
+    tris = [int(sum(m.indices.shape[0] for m in s.meshes)) for s in scene_list]
+    line = {"metric": "samples/s (64 batched requests, seed 4)", "value": samples * args.steps / (dev_ms / 1e3),
+            "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural scenes and sky, seed 4)",
+            "config": {"workload": "batch", "requests": len(reqs), "samples_per_step": samples,
+                       "scene_triangles": tris, "resolutions": "128^2..1920x1080", "spp": "4..256",
+                       "max_depth": 8, "l2_flush": "inputs larger than L2 (BVHs 2.6 GB, samples 4 GB)"},
+            "gpu_launches": launches,
+            "autotune": {"paths_in_flight": tune.paths_in_flight, "traverse_ctas_per_sm": tune.traverse_ctas_per_sm,
+                         "shade_ctas_per_sm": tune.shade_ctas_per_sm,
+                         "iterations_per_graph": tune.iterations_per_graph, "trials": trials, "seconds": t_tune},
+            "e2e": {"value": samples * args.steps / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": sum(c.width * c.height * 12 for _, _, c in reqs),
+                    "call": "dl_render_batch (64 requests; images returned to host memory)"},
+            "clocks": ck}
+    print(json.dumps(line))
+
+
+def run_guided(args):
+    """Learned guiding at equal time on the window-lit room (2M triangles,
+    depth 12): relMSE of guided vs plain against a 16k-spp plain reference at
+    480x270; throughput of the guided render at 1920x1080."""
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import abi, api, metrics, scenes
+    ctx = api.Context(local)
+    small = api.Scene.from_data(ctx, scenes.guiding_room(width=480, height=270))
+    ref = small.render(abi.make_opts(spp=16384, max_depth=12, seed=1000))
+    spp_g = 64
+    results = []
+    for rep in range(max(1, args.steps)):
+        g = api.Guide(ctx, seed=40 + rep)
+        img_g = small.render_guided(abi.make_opts(spp=spp_g, max_depth=12, seed=50 + rep), g)
+        st = ctx.stats()
+        t_g, train_ms = st.render_ms, st.guide_train_ms
+        small.render(abi.make_opts(spp=64, max_depth=12, seed=60 + rep))
+        t_p64 = ctx.stats().render_ms
+        spp_p = max(1, int(round(64 * t_g / t_p64)))
+        img_p = small.render(abi.make_opts(spp=spp_p, max_depth=12, seed=70 + rep))
+        t_p = ctx.stats().render_ms
+        results.append((metrics.relmse(img_g, ref), metrics.relmse(img_p, ref), t_g, t_p, spp_p, train_ms,
+                        metrics.relmse_robust(img_g, ref), metrics.relmse_robust(img_p, ref)))
+    e_g = float(np.median([r[0] for r in results]))
+    e_p = float(np.median([r[1] for r in results]))
+    r_g = float(np.median([r[6] for r in results]))
+    r_p = float(np.median([r[7] for r in results]))
+    big = api.Scene.from_data(ctx, scenes.guiding_room())
+    g = api.Guide(ctx, seed=99)
+    for _ in range(args.warmup):
+        big.render_guided(abi.make_opts(spp=4, max_depth=12, seed=5), g)
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        big.render_guided(abi.make_opts(spp=16, max_depth=12, seed=6), g)
+        wall = time.perf_counter() - t0
+        st = ctx.stats()
+    ck = clocks.summary()
+    samples = 1920 * 1080 * 16
+    line = {"metric": "relMSE ratio plain/guided at equal time (window-lit room, 2M triangles)",
+            "value": e_p / e_g, "unit": "x (median over runs)", "n_gpus": 1, "steps": len(results), "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r[2] for r in results])), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network fp16 in, fp32 accumulate)",
+            "data": "synthetic (procedural room and sky)",
+            "config": {"workload": "guided", "triangles": 1960090, "relmse_resolution": "480x270",
+                       "reference": "plain, 16384 spp", "guided_spp": spp_g, "max_depth": 12,
+                       "l2_flush": "inputs larger than L2 (BVH + samples)"},
+            "relmse": {"guided": e_g, "plain": e_p, "runs": [
+                {"guided": r[0], "plain": r[1], "guided_ms": r[2], "plain_ms": r[3], "plain_spp": r[4],
+                 "train_ms": r[5], "robust_guided": r[6], "robust_plain": r[7]} for r in results]},
+            "relmse_robust": {"guided": r_g, "plain": r_p, "ratio": r_p / r_g,
+                              "note": "relMSE without the 0.1 % largest per-pixel errors (sun-edge fireflies)"},
+            "guided_1080p": {"samples_per_s": samples / (st.render_ms / 1e3), "ms": st.render_ms,
+                             "records": st.guide_records, "train_ms": st.guide_train_ms},
+            "gpu_launches": st.kernel_launches,
+            "e2e": {"value": samples / wall, "unit": "samples/s (guided 1080p, 16 spp)", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 1920 * 1080 * 12, "call": "dl_render_guided"},
+            "clocks": ck}
+    print(json.dumps(line))
 
 
 if __name__ == "__main__":

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 3
+DL_ABI_VERSION = 4
 
 # status
 DL_OK = 0
@@ -164,6 +164,7 @@ class dl_request(C.Structure):
         ("opts", dl_render_opts),
         ("rgb", C.POINTER(C.c_float)),
         ("film_device", C.POINTER(C.c_float)),
+        ("camera", C.c_void_p),
     ]
 
 
@@ -186,6 +187,8 @@ class dl_guide_config(C.Structure):
         ("guide_fraction", C.c_float),
         ("batch", C.c_int32),
         ("steps_per_pass", C.c_int32),
+        ("max_guided_depth", C.c_int32),
+        ("reserved", C.c_int32),
         ("seed", C.c_uint64),
     ]
 

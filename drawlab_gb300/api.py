@@ -132,15 +132,32 @@ class Context:
 
     @staticmethod
     def _requests(items):
+        """items: (Scene, opts) or (Scene, opts, Camera override)."""
         reqs = (abi.dl_request * max(len(items), 1))()
-        outs = []
-        for i, (scene, opts) in enumerate(items):
-            rgb = np.empty((scene.height, scene.width, 3), np.float32)
+        outs, keep = [], []
+        for i, it in enumerate(items):
+            scene, opts = it[0], it[1]
+            cam = it[2] if len(it) > 2 else None
+            w, h = (cam.width, cam.height) if cam is not None else (scene.width, scene.height)
+            rgb = np.empty((h, w, 3), np.float32)
             outs.append(rgb)
             reqs[i].scene = scene.h
             reqs[i].opts = opts
             reqs[i].rgb = rgb.ctypes.data_as(C.POINTER(C.c_float))
             reqs[i].film_device = None
+            if cam is not None:
+                cd = abi.dl_camera_desc()
+                cd.type = abi.DL_CAMERA_VIRTUAL
+                cd.width, cd.height = cam.width, cam.height
+                cd.eye[:] = [float(v) for v in cam.eye]
+                cd.lookat[:] = [float(v) for v in cam.lookat]
+                cd.up[:] = [float(v) for v in cam.up]
+                cd.fov = cam.fov
+                keep.append(cd)
+                reqs[i].camera = C.cast(C.byref(cd), C.c_void_p)
+            else:
+                reqs[i].camera = None
+        reqs._keep = keep
         return reqs, outs
 
     def render_batch(self, items) -> list:

@@ -351,11 +351,19 @@ std::vector<dl::BatchItem> batch_items(dl_context* ctx, const dl_request* reqs, 
         if (outputs) need(q.rgb || q.film_device, "request " + std::to_string(r) + ": no output");
         items[r].scene = q.scene;
         items[r].opts = q.opts;
+        items[r].cam = q.scene->dev.cam;
+        if (q.camera) {
+            const dl_camera_desc& c = *q.camera;
+            need(c.type == DL_CAMERA_VIRTUAL && c.width > 0 && c.height > 0 && c.width <= 65536 &&
+                     c.height <= 65536 && c.fov > 0.f && c.fov < 180.f,
+                 "request " + std::to_string(r) + ": bad camera");
+            items[r].cam = dl::make_camera(c);
+        }
         if (trial_spp >= 0) items[r].opts.spp = trial_spp > 0 ? trial_spp : std::max(1, q.opts.spp / 8);
         items[r].d_film = outputs ? q.film_device : nullptr;
         if (!items[r].d_film) {
             film_off[r] = floats;
-            floats += dl::film_floats(q.scene->dev.cam.w, q.scene->dev.cam.h, q.opts.filter);
+            floats += dl::film_floats(items[r].cam.w, items[r].cam.h, q.opts.filter);
         }
     }
     ctx->render.batch_films.ensure((size_t)std::max<int64_t>(floats, 1) * 4);
@@ -377,13 +385,13 @@ int dl_render_batch(dl_context* ctx, const dl_request* reqs, int32_t n) {
         dl::render_batch(ctx, items.data(), n, false);
         size_t maxrgb = 0;
         for (int32_t r = 0; r < n; r++)
-            if (reqs[r].rgb) maxrgb = std::max(maxrgb, (size_t)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h * 3);
+            if (reqs[r].rgb) maxrgb = std::max(maxrgb, (size_t)items[r].cam.w * items[r].cam.h * 3);
         ctx->render.rgb.ensure(std::max<size_t>(maxrgb, 1) * 4);
         for (int32_t r = 0; r < n; r++) {
             if (!reqs[r].rgb) continue;
-            dl_scene* S = items[r].scene;
-            size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;
-            dl::resolve_film(S, items[r].d_film, items[r].opts.filter, ctx->render.rgb.as<float>());
+            size_t nrgb = (size_t)items[r].cam.w * items[r].cam.h * 3;
+            dl::resolve_film_cam(items[r].cam, ctx->stream, items[r].d_film, items[r].opts.filter,
+                                 ctx->render.rgb.as<float>());
             DL_CUDA(cudaMemcpyAsync(reqs[r].rgb, ctx->render.rgb.ptr, nrgb * 4, cudaMemcpyDeviceToHost, ctx->stream));
             DL_CUDA(cudaStreamSynchronize(ctx->stream));
         }
@@ -475,10 +483,11 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
 int dl_guide_default_config(dl_guide_config* cfg) {
     if (!cfg) return DL_ERR_INVALID_ARG;
     std::memset(cfg, 0, sizeof(*cfg));
-    cfg->learning_rate = 1e-3f;
+    cfg->learning_rate = 2e-3f;
     cfg->guide_fraction = 0.5f;
-    cfg->batch = 65536;
-    cfg->steps_per_pass = 8;
+    cfg->batch = 32768;
+    cfg->steps_per_pass = 16;
+    cfg->max_guided_depth = 6;
     cfg->seed = 1;
     return DL_OK;
 }
@@ -492,6 +501,7 @@ int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out)
         need(cfg->guide_fraction >= 0.f && cfg->guide_fraction < 1.f, "guide_fraction must be in [0, 1)");
         need(cfg->batch >= 16 && cfg->batch <= (1 << 24), "batch out of range");
         need(cfg->steps_per_pass >= 0 && cfg->steps_per_pass <= 1024, "steps_per_pass out of range");
+        need(cfg->max_guided_depth >= 0 && cfg->max_guided_depth <= 1 << 20, "max_guided_depth out of range");
         *out = nullptr;
         G = new dl_guide();
         G->ctx = ctx;
@@ -500,6 +510,13 @@ int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out)
         for (dl::DevBuf* b : {&G->w32, &G->grad, &G->m, &G->v}) b->ensure(pb);
         G->w16.ensure(dl::kGuideParams * 2);
         G->scratch.ensure(256);
+        DL_CUDA(cudaStreamCreateWithFlags(&G->train_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            DL_CUDA(cudaEventCreateWithFlags(&G->pass_done[k], cudaEventDisableTiming));
+            DL_CUDA(cudaEventCreateWithFlags(&G->train_done[k], cudaEventDisableTiming));
+        }
+        DL_CUDA(cudaEventCreate(&G->t0));
+        DL_CUDA(cudaEventCreate(&G->t1));
         for (dl::DevBuf* b : {&G->grad, &G->m, &G->v}) DL_CUDA(cudaMemsetAsync(b->ptr, 0, pb, ctx->stream));
         std::vector<float> w;
         dl::guide_init_params(cfg->seed, w);
@@ -564,7 +581,7 @@ int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad,
         G->recs.ensure((size_t)n * 48);
         DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
-        dl::guide_gradient(G, G->recs.ptr, n);
+        dl::guide_gradient(G, G->recs.ptr, n, 1, ctx->stream);
         DL_CUDA(cudaMemcpyAsync(grad, G->grad.ptr, dl::kGuideParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
         float l = 0.f;
         DL_CUDA(cudaMemcpyAsync(&l, G->scratch.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -3,7 +3,7 @@
 //
 // One training step on a batch of n records {position, normal, sampled
 // direction w, its sampling pdf p, radiance estimate L along w}:
-//   loss = -(1/n) sum_i (L_i / p_i) / mean(L / p) * log q(w_i)
+//   loss = -(1/n) sum_i min((L_i / p_i) / mean(L / p), 20) * log q(w_i)
 // (an estimate of the KL divergence from the normalised incident radiance to
 // the mixture q, up to a constant), then one Adam update.  Kernels:
 //   k_guide_weight_sum   mean(L / p) over the batch
@@ -55,6 +55,10 @@ __global__ void __launch_bounds__(32 * kInferWarps) k_guide_infer(const __half* 
 
 // -------------------------------------------------------------- training
 constexpr int kTrainWarps = 2;
+// Record weights L/p are normalised by their batch mean and clamped at this
+// multiple of it: a few records near the sun would otherwise carry the
+// whole gradient of a batch.
+constexpr float kGTargetClamp = 20.f;
 struct TrainTile {
     GuideTile f;                 // x: encoding, then layer-2 output; h: layer-1 output; o: output
     __half d0[16 * kGHs];        // dLoss / dOutput (48 used)
@@ -71,10 +75,12 @@ struct TrainActs {
     __half* d1;   // [n][64]
 };
 
-__global__ void k_guide_weight_sum(const GuideRecord* s, int n, float* sum) {
+__global__ void k_guide_weight_sum(const GuideRecord* s, int n, int stride, float* sum) {
     float acc = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        acc += s[i].pdf > 0.f ? s[i].L / s[i].pdf : 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const GuideRecord& r = s[(size_t)i * stride];
+        acc += r.pdf > 0.f ? r.L / r.pdf : 0.f;
+    }
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
 }
@@ -162,7 +168,7 @@ __device__ __forceinline__ float record_grad(const float* o, const GuideRecord& 
 }
 
 __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_fwd_bwd(const __half* w16, const float* w32,
-                                                                    const GuideRecord* s, int n,
+                                                                    const GuideRecord* s, int n, int stride,
                                                                     const float* wsum, float* grad,
                                                                     TrainActs A, float* loss) {
     __shared__ TrainTile tiles[kTrainWarps];
@@ -178,7 +184,7 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_fwd_bwd(const __half
         if (lane < 16) {
             float x[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (r < n)
-                for (int i = 0; i < 6; i++) x[i] = s[r].in[i];
+                for (int i = 0; i < 6; i++) x[i] = s[(size_t)r * stride].in[i];
             encode_input(x, T.f.x + lane * kGXs);
             for (int k = 0; k < kGEnc; k++) A.x[(size_t)r * kGEnc + k] = T.f.x[lane * kGXs + k];
         }
@@ -193,9 +199,9 @@ __global__ void __launch_bounds__(32 * kTrainWarps) k_guide_fwd_bwd(const __half
         if (lane < 16) {
             float d[kGOut];
             float sc = 0.f;
-            if (r < n && s[r].pdf > 0.f && mean > 0.f) sc = s[r].L / s[r].pdf / mean / (float)n;
             GuideRecord rec = {};
-            if (r < n) rec = s[r];
+            if (r < n) rec = s[(size_t)r * stride];
+            if (r < n && rec.pdf > 0.f && mean > 0.f) sc = fminf(rec.L / rec.pdf / mean, kGTargetClamp) / (float)n;
             lacc += record_grad(T.f.o + lane * kGOs, rec, sc, d);
             for (int j = 0; j < kGOutPad; j++) {
                 float v = j < kGOut ? d[j] : 0.f;
@@ -330,8 +336,7 @@ void guide_upload_params(dl_guide* G, const float* host) {
 
 // Gradient of the loss over `n` device records into G->grad (added to it);
 // returns nothing, the loss sum lands in scratch[1].
-void guide_gradient(dl_guide* G, const void* d_recs, int64_t n) {
-    cudaStream_t st = G->ctx->stream;
+void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cudaStream_t st) {
     const int64_t ntiles = (n + 15) / 16, npad = ntiles * 16;
     G->acts.ensure(guide_act_bytes(npad));
     __half* a = G->acts.as<__half>();
@@ -345,9 +350,10 @@ void guide_gradient(dl_guide* G, const void* d_recs, int64_t n) {
     float* sc = G->scratch.as<float>();
     DL_CUDA(cudaMemsetAsync(sc, 0, 2 * sizeof(float), st));
     const GuideRecord* R = static_cast<const GuideRecord*>(d_recs);
-    k_guide_weight_sum<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(R, (int)n, sc);
+    k_guide_weight_sum<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(R, (int)n, stride, sc);
     const int blocks = (int)std::min<int64_t>((ntiles + kTrainWarps - 1) / kTrainWarps, 152 * 16);
-    k_guide_fwd_bwd<<<blocks, 32 * kTrainWarps, 0, st>>>(G->w16.as<__half>(), G->w32.as<float>(), R, (int)n, sc,
+    k_guide_fwd_bwd<<<blocks, 32 * kTrainWarps, 0, st>>>(G->w16.as<__half>(), G->w32.as<float>(), R, (int)n, stride,
+                                                         sc,
                                                          G->grad.as<float>(), A, sc + 1);
     auto wgrad = [&](const __half* dy, int ldy, const __half* z, int ldz, int M, int N, float* out) {
         const int tiles = (M / 16) * (N / 8);
@@ -362,8 +368,7 @@ void guide_gradient(dl_guide* G, const void* d_recs, int64_t n) {
     DL_CUDA(cudaGetLastError());
 }
 
-void guide_adam(dl_guide* G) {
-    cudaStream_t st = G->ctx->stream;
+void guide_adam(dl_guide* G, cudaStream_t st) {
     G->step += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)G->step), c2 = 1.f - std::pow(b2, (float)G->step);
@@ -378,8 +383,8 @@ float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps) {
     cudaStream_t st = G->ctx->stream;
     float loss = 0.f;
     for (int k = 0; k < steps; k++) {
-        guide_gradient(G, d_recs, n);
-        guide_adam(G);
+        guide_gradient(G, d_recs, n, 1, st);
+        guide_adam(G, st);
     }
     if (steps > 0) {
         DL_CUDA(cudaMemcpyAsync(&loss, G->scratch.as<float>() + 1, 4, cudaMemcpyDeviceToHost, st));

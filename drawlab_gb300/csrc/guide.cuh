@@ -7,7 +7,7 @@
 // cores with mma.sync m16n8k16):
 //   input   6 scalars: position scaled to [0, 1]^3 by the scene bounds,
 //           shading normal in [-1, 1]^3
-//   encode  sin / cos (2^k pi x), k = 0..11, for each scalar: 144 features
+//   encode  sin / cos (2^(k-3) pi x), k = 0..11, for each scalar: 144 features
 //   layer 1 144 -> 64, ReLU
 //   layer 2  64 -> 64, ReLU
 //   layer 3  64 -> 40 (rows 40..47 of the padded weight are zero)
@@ -61,19 +61,20 @@ static_assert(sizeof(GuideRecord) == 48, "record layout");
 struct GuideNet {
     const __half* w16;   // kGParams halves
     const float* w32;    // fp32 master (the biases are read from it)
-    float3 lo;           // scene bounds: position -> [0, 1]^3
-    float3 inv_ext;
     float fraction;      // probability of sampling the learned proposal
+    int max_depth;       // vertices at depth >= max_depth sample the BSDF alone
 };
 
 // ------------------------------------------------------------- encoding
-// sin / cos of (2^k pi x) for k = 0..11: exact sincospi at k = 0, 4, 8,
-// double-angle steps in between (at most three, error ~1e-6).
+// sin / cos of (2^(k-3) pi x) for k = 0..11 (periods from 16 scene units
+// down to 1/128): exact sincospi at k = 0, 4, 8, double-angle steps in
+// between (at most three, error ~1e-6).
+constexpr int kGFreqShift = 3;
 __device__ __forceinline__ void encode_scalar(float x, __half* out) {
 #pragma unroll
     for (int k0 = 0; k0 < kGFreq; k0 += 4) {
         float s, c;
-        sincospif(x * (float)(1 << k0), &s, &c);
+        sincospif(x * ((float)(1 << k0) / (float)(1 << kGFreqShift)), &s, &c);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             out[2 * (k0 + k)] = __float2half_rn(s);

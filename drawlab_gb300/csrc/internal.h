@@ -110,6 +110,12 @@ struct RenderCounters {
     alignas(128) unsigned int work_sh;
     alignas(128) unsigned long long next_path;
     alignas(128) unsigned int guide_next;      // training records claimed (guided renders)
+    // Values of the current pass, written by the host after the counters are
+    // reset, so the captured graph stays valid across passes and frames.
+    alignas(128) unsigned long long pass_total;  // paths of the pass
+    int pass_spp_offset;                         // single render: sample index of the pass's first sample
+    unsigned int pass_keep;                      // guided: training-record keep threshold (24-bit hash)
+    void* pass_recs;                             // guided: where the pass writes its training records
     alignas(128) unsigned long long stat_ext;
     unsigned long long stat_shadow;
     unsigned long long stat_camera;   // filled on the host: paths started = min(next_path, paths)
@@ -139,6 +145,7 @@ struct RenderBuffers {
     DevBuf li_xys, li_out, li_pos;
     HostBuf host_counters;
     HostBuf host_stage;
+    HostBuf host_pass;   // staging of the pass values
     void ensure(int64_t cap);
     size_t device_bytes() const;
 };
@@ -189,8 +196,21 @@ struct dl_guide {
     dl_context* ctx = nullptr;
     dl_guide_config cfg{};
     dl::DevBuf w32, w16, grad, m, v, scratch, acts, recs, io_in, io_out;
-    dl::DevBuf pass_recs;   // training records written by a guided render pass
+    dl::DevBuf pass_recs;   // training records of guided render passes (two halves, alternating)
     int64_t step = 0;
+    // training runs on its own stream, overlapping the next pass
+    cudaStream_t train_stream = nullptr;
+    cudaEvent_t pass_done[2] = {nullptr, nullptr}, train_done[2] = {nullptr, nullptr};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    ~dl_guide() {
+        for (int k = 0; k < 2; k++) {
+            if (pass_done[k]) cudaEventDestroy(pass_done[k]);
+            if (train_done[k]) cudaEventDestroy(train_done[k]);
+        }
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+        if (train_stream) cudaStreamDestroy(train_stream);
+    }
 };
 
 struct dl_scene {

@@ -111,7 +111,6 @@ struct RenderParams {
     const int* xys;
     float* li_L;
     float* li_pos;
-    unsigned long long total_paths;
     // guided renders
     int guided;
     GuideNet gnet;
@@ -200,7 +199,7 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
         unsigned long long local = pid - R.pid_first;
         unsigned long long npix = (unsigned long long)cam.w * cam.h;
         unsigned long long pix = local % npix;
-        s = (int)(local / npix) + R.spp_offset;
+        s = (int)(local / npix) + (kMulti ? R.spp_offset : P.cnt->pass_spp_offset);
         x = (int)(pix % cam.w);
         y = (int)(pix / cam.w);
     }
@@ -272,7 +271,7 @@ __device__ __forceinline__ void credit_one(const RenderParams& P, float4 t, floa
     if (t.x > 0.f) { s += c.x / t.x; k++; }
     if (t.y > 0.f) { s += c.y / t.y; k++; }
     if (t.z > 0.f) { s += c.z / t.z; k++; }
-    if (k > 0 && isfinite(s)) P.grecords[idx].L += s / (float)k;
+    if (k > 0 && isfinite(s)) static_cast<GuideRecord*>(P.cnt->pass_recs)[idx].L += s / (float)k;
 }
 __device__ __forceinline__ void credit(const RenderParams& P, const GuideRec& gr, float3 c, bool both) {
     credit_one(P, gr.a, c);
@@ -284,7 +283,7 @@ __device__ __forceinline__ void credit(const RenderParams& P, const GuideRec& gr
 template <bool kMulti>
 __device__ __forceinline__ bool regenerate(const RenderParams& P, int slot, bool want) {
     unsigned long long pid = warp_claim(&P.cnt->next_path, want);
-    bool ok = want && pid < P.total_paths;
+    bool ok = want && pid < P.cnt->pass_total;
     if (ok) start_path<kMulti>(P, slot, pid);
     return ok;
 }
@@ -840,28 +839,28 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
         }
         // ---- phase 2 (guided): the network on the warp's shading points
         const bool sampling = active && !done;
+        const bool use_guide = kGuided && sampling && depth < P.gnet.max_depth;
         float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         float* lob = nullptr;
         if (kGuided) {
             GuideWarpSmem& W = reinterpret_cast<GuideWarpSmem*>(dyn_smem)[threadIdx.x >> 5];
             lob = W.lobes + lane * kGOut;
-            if (sampling) guide_input(request<kMulti>(P, rid).sc, h.p, normalize(h.sh.n), in6);
-            if (__any_sync(0xffffffffu, sampling)) {
-                for (int half = 0; half < 2; half++) {
-                    if ((lane >> 4) == half) encode_input(in6, W.tile.x + (lane & 15) * kGXs);
-                    __syncwarp();
-                    forward16(W.tile, P.gnet.w16, P.gnet.w32, lane);
-                    if ((lane >> 4) == half && sampling) {
-                        VmfLobe L[kGLobes];
-                        decode_lobes(W.tile.o + (lane & 15) * kGOs, L);
-                        store_lobes(L, lob);
-                    }
-                    __syncwarp();
+            if (use_guide) guide_input(request<kMulti>(P, rid).sc, h.p, normalize(h.sh.n), in6);
+            for (int half = 0; half < 2; half++) {
+                if (!__any_sync(0xffffffffu, use_guide && (lane >> 4) == half)) continue;
+                if ((lane >> 4) == half) encode_input(in6, W.tile.x + (lane & 15) * kGXs);
+                __syncwarp();
+                forward16(W.tile, P.gnet.w16, P.gnet.w32, lane);
+                if ((lane >> 4) == half && use_guide) {
+                    VmfLobe L[kGLobes];
+                    decode_lobes(W.tile.o + (lane & 15) * kGOs, L);
+                    store_lobes(L, lob);
                 }
+                __syncwarp();
             }
         }
         // ---- phase 3: NEE and the next direction
-        bool record = false;
+        bool record = false, rotate = false;
         float rec_pdf = 0.f;
         float3 nd = f3(0.f, 0.f, 0.f);
         if (active) {
@@ -874,7 +873,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 Frame fr = T == MAT_ANISO_GGX ? make_onb(normalize(h.sh.n)) : h.sh;
                 float3 wi = to_local(fr, neg(normalize(dir)));
                 if (T == MAT_ANISO_GGX) wi = normalize(wi);
-                const float alpha = kGuided ? P.gnet.fraction : 0.f;
+                const float alpha = use_guide ? P.gnet.fraction : 0.f;
                 float2 s_nee = g.next2d();
                 float3 c = f3(0.f, 0.f, 0.f);
                 float3 ld = c;
@@ -895,7 +894,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                         q1.eta = 1.f;
                         float3 bv = bsdf_eval<T>(m, q1);
                         float bp = bsdf_pdf<T>(m, q1);
-                        if (kGuided) bp = alpha * stored_mixture_pdf(lob, ld) + (1.f - alpha) * bp;
+                        if (use_guide) bp = alpha * stored_mixture_pdf(lob, ld) + (1.f - alpha) * bp;
                         float w = (delta && (R.flags & DL_RENDER_FIX_POINT_LIGHT)) ? 1.f : mis_weight(lpdf, bp);
                         c = mul(mul(scale(tp, w), bv), espec);
                         emit = c.x != 0.f || c.y != 0.f || c.z != 0.f;
@@ -906,7 +905,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 q2.wo = f3(0.f, 0.f, 0.f);
                 q2.eta = 1.f;
                 q2.measure = M_UNKNOWN;
-                if (kGuided) {
+                if (use_guide) {
                     // one-sample MIS between the learned mixture and the BSDF
                     float3 fcos_over_p;
                     if (g.next_float() < alpha) {
@@ -945,7 +944,9 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     nr.d = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
                     P.ray[slot] = nr;
                     cont = true;
-                    record = kGuided && P.grecords != nullptr;
+                    rotate = use_guide && P.grecords != nullptr;
+                    record = rotate && (uint32_t)(splitmix64(pid * 64ull + (unsigned long long)depth) >> 40) <
+                                           P.cnt->pass_keep;
                 }
                 if (emit) {
                     if (done) target = -1 - (int)pid;  // lands in the stored sample
@@ -967,11 +968,12 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                 P.meta[slot] = nmr;
             }
         }
-        // ---- phase 4 (guided): training record of the vertex
+        // ---- phase 4 (guided): training record of the vertex (a hashed
+        // subset of the guided vertices, spread over the whole pass)
         if (kGuided) {
             unsigned long long ri = warp_claim_u32(&P.cnt->guide_next, record);
-            if (record) {
-                int idx = ri < (unsigned long long)P.grecord_cap ? (int)ri : -1;
+            if (rotate) {
+                int idx = record && ri < (unsigned long long)P.grecord_cap ? (int)ri : -1;
                 if (idx >= 0) {
                     GuideRecord rc;
                     for (int k = 0; k < 6; k++) rc.in[k] = in6[k];
@@ -981,7 +983,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
                     rc.pdf = rec_pdf;
                     rc.L = 0.f;
                     rc.pad = 0.f;
-                    P.grecords[idx] = rc;
+                    static_cast<GuideRecord*>(P.cnt->pass_recs)[idx] = rc;
                 }
                 GuideRec ngr;
                 ngr.a = gr.b;
@@ -1264,17 +1266,35 @@ static DevRequest make_request(dl_scene* S, const dl_render_opts& o) {
     return R;
 }
 
-// Wavefront loop over the paths [0, P.total_paths) of one pass, until every
-// path and every shadow ray has finished.  Adds the pass's counters into
-// `acc` and per-kernel times into kms.  `multi`: paths of a request table.
+// The values that change from pass to pass live in the device counters (set
+// after their reset), not in the kernel parameters: one captured graph serves
+// every pass and frame.
+struct PassValues {
+    unsigned long long total;
+    int spp_offset;
+    unsigned keep;
+    void* recs;
+};
+static_assert(sizeof(PassValues) == 24, "pass values layout");
+
+// Wavefront loop over the paths [0, total) of one pass, until every path and
+// every shadow ray has finished.  Adds the pass's counters into `acc` and
+// per-kernel times into kms.  `multi`: paths of a request table.
 static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool multi, bool count_traversal,
-                          double* kms, int64_t& launches, int64_t& iters, RenderCounters& acc) {
+                          double* kms, int64_t& launches, int64_t& iters, RenderCounters& acc,
+                          unsigned long long total, int spp_offset, unsigned keep, void* recs = nullptr) {
     cudaStream_t st = ctx->stream;
     RenderBuffers& B = ctx->render;
     const TuneParams tp = ctx->tune;
     const int batch = tp.iters_per_graph;
-    const unsigned long long total = P.total_paths;
     DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
+    B.host_pass.ensure(sizeof(PassValues));
+    PassValues* pv = B.host_pass.as<PassValues>();
+    pv->total = total;
+    pv->spp_offset = spp_offset;
+    pv->keep = keep;
+    pv->recs = recs;
+    DL_CUDA(cudaMemcpyAsync(&P.cnt->pass_total, pv, sizeof(PassValues), cudaMemcpyHostToDevice, st));
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     const bool timing = ctx->kernel_timing;
     const bool use_graph = !timing && !count_traversal;
@@ -1435,17 +1455,16 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
     DL_CUDA(cudaEventRecord(ctx->ev0, st));
     unsigned long long invalid = 0;
     if (P.mode == 1) {
-        P.total_paths = (unsigned long long)li_n;
-        run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc);
+        run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc, (unsigned long long)li_n, 0,
+                      1u << 24);
     } else {
         FilmParams F = film_params(cam, P.r0, o.filter, d_film, P.samples, B.invalid.as<unsigned long long>());
         DL_CUDA(cudaMemsetAsync(F.invalid, 0, sizeof(unsigned long long), st));
         dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
         for (int s0 = 0; s0 < spp; s0 += chunk_spp) {
             int ns = std::min(chunk_spp, spp - s0);
-            P.r0.spp_offset = o.spp_offset + s0;
-            P.total_paths = npix * (unsigned long long)ns;
-            run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc);
+            run_wavefront(ctx, P, cap, false, count_traversal, kms, launches, iters, acc,
+                          npix * (unsigned long long)ns, o.spp_offset + s0, 1u << 24);
             F.nspp = ns;
             F.s_first = o.spp_offset + s0;
             F.accumulate = s0 > 0;
@@ -1492,16 +1511,22 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
     P.gnet.w16 = G->w16.as<__half>();
     P.gnet.w32 = G->w32.as<float>();
     P.gnet.fraction = G->cfg.guide_fraction;
+    P.gnet.max_depth = G->cfg.max_guided_depth;
     P.grec = B.grec.as<GuideRec>();
     const int64_t rec_cap = std::min<int64_t>((int64_t)G->cfg.batch * std::max(1, G->cfg.steps_per_pass), 1 << 23);
+    GuideRecord* rec_half[2] = {nullptr, nullptr};
     if (train) {
-        G->pass_recs.ensure((size_t)rec_cap * sizeof(GuideRecord));
-        P.grecords = G->pass_recs.as<GuideRecord>();
+        // two halves: pass k writes half k % 2 while the training stream
+        // learns from the other half (the previous pass)
+        G->pass_recs.ensure(2 * (size_t)rec_cap * sizeof(GuideRecord));
+        rec_half[0] = G->pass_recs.as<GuideRecord>();
+        rec_half[1] = rec_half[0] + rec_cap;
+        P.grecords = rec_half[0];  // non-null: the kernels write records
         P.grecord_cap = (int)rec_cap;
     }
     double kms[4] = {0, 0, 0, 0};
     int64_t launches = 0, iters = 0, records = 0;
-    double train_ms = 0.0;
+    float train_ms = 0.f;
     RenderCounters acc;
     std::memset(&acc, 0, sizeof(acc));
     DL_CUDA(cudaEventRecord(ctx->ev0, st));
@@ -1510,12 +1535,24 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
     dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
     RenderCounters* hc = B.host_counters.as<RenderCounters>();
     int done = 0;
+    bool trained[2] = {false, false};
+    double guided_per_sample = 2.0 * (double)npix;  // guided vertices per sample per pixel: first guess
+    cudaStream_t ts = G->train_stream;
     for (int pass = 0; done < spp; pass++) {
         int ns = std::min(std::min(pass == 0 ? 1 : (1 << (pass - 1)), spp - done), chunk_spp);
-        P.r0.spp_offset = o.spp_offset + done;
-        P.total_paths = npix * (unsigned long long)ns;
-        run_wavefront(ctx, P, cap, false, false, kms, launches, iters, acc);
-        const int64_t nrec = train ? std::min<int64_t>(hc->guide_next, rec_cap) : 0;
+        // keep about rec_cap of the pass's guided vertices, spread over it
+        const double expect = guided_per_sample * ns;
+        const double frac = std::min(1.0, 0.9 * (double)rec_cap / std::max(expect, 1.0));
+        const unsigned keep = (unsigned)std::max(1.0, frac * (double)(1u << 24));
+        const int half = pass & 1;
+        // the half this pass writes must be free of the training that read it
+        if (train && trained[half]) DL_CUDA(cudaStreamWaitEvent(st, G->train_done[half], 0));
+        run_wavefront(ctx, P, cap, false, false, kms, launches, iters, acc, npix * (unsigned long long)ns,
+                      o.spp_offset + done, keep, rec_half[half]);
+        const int64_t claimed = train ? (int64_t)hc->guide_next : 0;
+        const int64_t nrec = std::min<int64_t>(claimed, rec_cap);
+        if (train && claimed > 0)
+            guided_per_sample = (double)claimed / ((double)keep / (double)(1u << 24)) / ns;
         F.nspp = ns;
         F.s_first = o.spp_offset + done;
         F.accumulate = done > 0;
@@ -1523,20 +1560,34 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
         launches += 1;
         DL_CUDA(cudaGetLastError());
         done += ns;
-        if (train && nrec >= 16 && done < spp) {
-            auto h0 = std::chrono::steady_clock::now();
-            const int64_t bs = std::min<int64_t>(G->cfg.batch, nrec);
-            for (int k = 0; k < G->cfg.steps_per_pass; k++) {
-                int64_t off = ((int64_t)k * bs) % nrec;
-                int64_t cnt = std::min<int64_t>(bs, nrec - off);
-                DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, kGuideParams * 4, st));
-                guide_gradient(G, P.grecords + off, cnt);
-                guide_adam(G);
+        const int steps = G->cfg.steps_per_pass;
+        if (train && nrec >= 16 * (int64_t)std::max(1, steps) && done < spp) {
+            // Adam steps on this pass's records, on the training stream: the
+            // next pass renders meanwhile with the network as it changes (its
+            // kernels sample and evaluate the same lobes, so every sample
+            // stays unbiased).  Step k trains on records k, k + steps, ...:
+            // every step sees the whole image.
+            DL_CUDA(cudaEventRecord(G->pass_done[half], st));
+            DL_CUDA(cudaStreamWaitEvent(ts, G->pass_done[half], 0));
+            DL_CUDA(cudaEventRecord(G->t0, ts));
+            for (int k = 0; k < steps; k++) {
+                const int64_t cnt = (nrec - k + steps - 1) / steps;
+                DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, kGuideParams * 4, ts));
+                guide_gradient(G, rec_half[half] + k, cnt, steps, ts);
+                guide_adam(G, ts);
             }
-            DL_CUDA(cudaStreamSynchronize(st));
-            train_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+            DL_CUDA(cudaEventRecord(G->t1, ts));
+            DL_CUDA(cudaEventRecord(G->train_done[half], ts));
+            trained[half] = true;
         }
         records += nrec;
+    }
+    if (train && (trained[0] || trained[1])) {
+        // the render ends when its last training round has ended
+        DL_CUDA(cudaEventRecord(G->pass_done[0], ts));
+        DL_CUDA(cudaStreamWaitEvent(st, G->pass_done[0], 0));
+        DL_CUDA(cudaStreamSynchronize(ts));
+        DL_CUDA(cudaEventElapsedTime(&train_ms, G->t0, G->t1));  // the last round's device time
     }
     unsigned long long* hinv =
         reinterpret_cast<unsigned long long*>(B.host_counters.as<char>() + sizeof(RenderCounters));
@@ -1559,13 +1610,13 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
     std::vector<int> done(n, 0);
     unsigned long long all = 0;
     for (int r = 0; r < n; r++)
-        all += (unsigned long long)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h * items[r].opts.spp;
+        all += (unsigned long long)items[r].cam.w * items[r].cam.h * items[r].opts.spp;
     const unsigned long long budget = kSampleBufferBytes / 16;
     // slice of request r per pass: its share of the budget, at least one sample
     std::vector<int> slice(n);
     unsigned long long max_pass = 0;
     for (int r = 0; r < n; r++) {
-        const unsigned long long npix = (unsigned long long)items[r].scene->dev.cam.w * items[r].scene->dev.cam.h;
+        const unsigned long long npix = (unsigned long long)items[r].cam.w * items[r].cam.h;
         double share = all <= budget ? 1.0 : (double)budget / (double)all;
         slice[r] = std::max(1, std::min(items[r].opts.spp, (int)(items[r].opts.spp * share)));
         max_pass += npix * (unsigned long long)slice[r];
@@ -1597,10 +1648,10 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
         unsigned long long first = 0;
         for (int r = 0; r < n; r++) {
             if (done[r] >= items[r].opts.spp) continue;
-            const dl_scene* S = items[r].scene;
-            const unsigned long long npix = (unsigned long long)S->dev.cam.w * S->dev.cam.h;
+            const unsigned long long npix = (unsigned long long)items[r].cam.w * items[r].cam.h;
             ns[na] = std::min(slice[r], items[r].opts.spp - done[r]);
             DevRequest R = make_request(items[r].scene, items[r].opts);
+            R.sc.cam = items[r].cam;
             R.pid_first = first;
             R.spp_offset = items[r].opts.spp_offset + done[r];
             hreq[na] = R;
@@ -1612,11 +1663,10 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
         // the pass's request table; the copy is ordered before the pass's kernels
         DL_CUDA(cudaMemcpyAsync(B.requests.ptr, hreq, sizeof(DevRequest) * na, cudaMemcpyHostToDevice, st));
         P.num_reqs = na;
-        P.total_paths = first;
-        run_wavefront(ctx, P, cap, true, count_traversal, kms, launches, iters, acc);
+        run_wavefront(ctx, P, cap, true, count_traversal, kms, launches, iters, acc, first, 0, 1u << 24);
         for (int a = 0; a < na; a++) {
             const int r = active[a];
-            const DevCamera& cam = items[r].scene->dev.cam;
+            const DevCamera& cam = items[r].cam;
             FilmParams F = film_params(cam, hreq[a], items[r].opts.filter, items[r].d_film,
                                        P.samples + hreq[a].pid_first, d_invalid);
             F.nspp = ns[a];
@@ -1677,10 +1727,17 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     P.xys = d_xys;
     P.li_L = d_L;
     P.li_pos = d_pos;
-    P.total_paths = (unsigned long long)li_n;
     int64_t cap = std::min<int64_t>(slots, ((li_n + 31) / 32) * 32);
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     cudaError_t e = cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st);
+    if (e != cudaSuccess) return e;
+    // pass values from the stack (a pageable copy: staged before it returns)
+    PassValues pv;
+    pv.total = (unsigned long long)li_n;
+    pv.spp_offset = 0;
+    pv.keep = 1u << 24;
+    pv.recs = nullptr;
+    e = cudaMemcpyAsync(&P.cnt->pass_total, &pv, sizeof(pv), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
     k_init<false><<<sms * 16, 128, 0, st>>>(P, (int)cap);
     RenderCounters hc;
@@ -1701,10 +1758,13 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
 }
 
 void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb) {
-    const DevCamera& cam = S->dev.cam;
+    resolve_film_cam(S->dev.cam, S->ctx->stream, d_film, filter, d_rgb);
+}
+
+void resolve_film_cam(const DevCamera& cam, cudaStream_t st, const float* d_film, int filter, float* d_rgb) {
     int b = filter == DL_FILTER_BOX ? 0 : 2;
     int n = cam.w * cam.h;
-    k_resolve<<<(n + 255) / 256, 256, 0, S->ctx->stream>>>(reinterpret_cast<const float4*>(d_film),
+    k_resolve<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4*>(d_film),
                                                          cam.w + 2 * b, b, cam.w, cam.h, d_rgb);
     DL_CUDA(cudaGetLastError());
 }

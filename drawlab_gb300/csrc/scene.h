@@ -24,15 +24,17 @@ struct BatchItem {
     dl_scene* scene;
     dl_render_opts opts;
     float* d_film;
+    DevCamera cam;   // the scene's camera or the request's override
 };
+void resolve_film_cam(const DevCamera& cam, cudaStream_t st, const float* d_film, int filter, float* d_rgb);
 void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_traversal);
 
 // Learned guiding (guide.cu).
 constexpr int kGuideParams = 16560;
 void guide_init_params(uint64_t seed, std::vector<float>& w);
 void guide_upload_params(dl_guide* G, const float* host);
-void guide_gradient(dl_guide* G, const void* d_recs, int64_t n);
-void guide_adam(dl_guide* G);
+void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cudaStream_t st);
+void guide_adam(dl_guide* G, cudaStream_t st);
 float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps);
 void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n);
 // Guided progressive render into d_film (render.cu).

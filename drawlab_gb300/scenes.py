@@ -573,3 +573,82 @@ def guiding_room(width: int = 1920, height: int = 1080, spp: int = 16, max_depth
     s.camera = Camera(width=width, height=height, eye=(0.0, 1.6, 2.7), lookat=(0.0, 1.0, -3.0),
                       up=(0.0, 1.0, 0.0), fov=60.0)
     return s
+
+
+def _random_material(rng) -> Material:
+    kind = int(rng.integers(0, 5))
+    if kind == 0:
+        return Material(type=abi.DL_MAT_DIFFUSE, albedo=tuple(rng.uniform(0.1, 0.9, 3)))
+    if kind == 1:
+        return Material(type=abi.DL_MAT_MIRROR)
+    if kind == 2:
+        return Material(type=abi.DL_MAT_DIELECTRIC, int_ior=1.5, ext_ior=1.000277)
+    if kind == 3:
+        a = float(rng.uniform(0.05, 0.5))
+        return Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1), alpha=(a, a))
+    ax, ay = (float(v) for v in rng.uniform(0.02, 0.4, 2))
+    return Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0, 0, 0), specular=(1, 1, 1), alpha=(ax, ay))
+
+
+def batch_scene(triangles: int, seed: int, env: np.ndarray | None) -> SceneData:
+    """A scene of about `triangles` triangles: a displaced-grid ground (half
+    the budget) and level-3/4 icospheres with random materials (the other
+    half), lit by `env` (the procedural sky) or by two quad area lights."""
+    rng = np.random.default_rng(seed)
+    s = SceneData("batch_%d" % triangles, spp=16, max_depth=8, rr_depth=3)
+    n = max(4, int(math.sqrt(max(triangles // 2, 32) / 2)))
+    P, F, N = displaced_grid((0.0, 0.0, 0.0), (20.0, 20.0), n, 1.0, seed=seed)
+    s.add_mesh(Mesh(P, F, N, material=s.add_material(Material(albedo=tuple(rng.uniform(0.3, 0.7, 3))))))
+    level = 4 if triangles >= 200_000 else 3
+    per = 20 * 4 ** level
+    count = max(1, (triangles - 2 * n * n) // per)
+    for k in range(count):
+        r = float(rng.uniform(0.2, 0.8))
+        x, z = (float(v) for v in rng.uniform(-9.0, 9.0, 2))
+        mi = s.add_material(_random_material(rng))
+        p, f, nn = sphere_mesh(level, (x, 1.0 + r, z), r)
+        s.add_mesh(Mesh(p, f, nn, material=mi))
+    if env is not None:
+        s.lights.append(Light(type=abi.DL_LIGHT_ENVMAP, env_rgb=env, env_scale=1.0, env_visual=1))
+    else:
+        black = s.add_material(Material(albedo=(0.0, 0.0, 0.0)))
+        for k in range(2):
+            L = float(rng.uniform(5.0, 30.0))
+            cx, cz = (float(v) for v in rng.uniform(-6.0, 6.0, 2))
+            p, f, nn = rectangle((cx - 1.5, 8.0, cz - 1.5), (3.0, 0, 0), (0, 0, 3.0))
+            li = s.add_mesh(Mesh(p, f, nn, material=black))
+            s.add_area_light(li, (L, L, L))
+    s.camera = Camera(width=256, height=256, eye=(0.0, 7.0, 16.0), lookat=(0.0, 0.5, 0.0), up=(0.0, 1.0, 0.0),
+                      fov=45.0)
+    return s
+
+
+BATCH_RESOLUTIONS = [(128, 128), (256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+BATCH_SPP = [4, 16, 64, 256]
+BATCH_TRIANGLES = [1_000, 4_000, 16_000, 64_000, 256_000, 512_000, 1_000_000, 2_000_000]
+
+
+def batch_workload(seed: int = 4, num_requests: int = 64, env_width: int = 2048, env_height: int = 1024,
+                   triangles=None, resolutions=None, spp_choices=None):
+    """The batched-rendering workload: `num_requests` requests drawn from
+    `seed` -- a scene of 1k-2M triangles (half of the scenes lit by the
+    procedural 2048x1024 sky with its 0.5-degree 1e4 sun), a resolution from
+    {128^2 .. 1920x1080}, spp from {4, 16, 64, 256}, a camera orbiting the
+    scene.  Returns (scenes, requests): requests are (scene index, spp,
+    Camera)."""
+    rng = np.random.default_rng(seed)
+    tris = triangles or BATCH_TRIANGLES
+    sky = sky_envmap(env_width, env_height, sun_peak=1.0e4, sun_radius_deg=0.5)
+    scene_list = [batch_scene(t, seed * 100 + k, sky if k % 2 == 0 else None) for k, t in enumerate(tris)]
+    reqs = []
+    res = resolutions or BATCH_RESOLUTIONS
+    sppc = spp_choices or BATCH_SPP
+    for _ in range(num_requests):
+        si = int(rng.integers(0, len(scene_list)))
+        w, h = res[int(rng.integers(0, len(res)))]
+        spp = int(sppc[int(rng.integers(0, len(sppc)))])
+        a = float(rng.uniform(0, 2 * math.pi))
+        cam = Camera(width=w, height=h, eye=(16.0 * math.sin(a), 7.0, 16.0 * math.cos(a)), lookat=(0.0, 0.5, 0.0),
+                     up=(0.0, 1.0, 0.0), fov=45.0)
+        reqs.append((si, spp, cam))
+    return scene_list, reqs

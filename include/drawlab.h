@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 3
+#define DL_ABI_VERSION 4
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -282,6 +282,8 @@ typedef struct dl_request {
     dl_render_opts opts;
     float* rgb;
     float* film_device;
+    const dl_camera_desc* camera;  /* NULL: the scene's camera; else this one
+                                      (its resolution sizes the outputs) */
 } dl_request;
 
 /* Render many requests -- of different scenes, resolutions and sample
@@ -324,7 +326,7 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
  * extra technique in one-sample MIS with BSDF sampling (the estimator stays
  * unbiased; BSDF + NEE remains the fallback).  No reference counterpart.
  *
- * Network: encoding sin/cos(2^k pi x), k < 12, of the 6 inputs (144
+ * Network: encoding sin/cos(2^(k-3) pi x), k < 12, of the 6 inputs (144
  * features) -> 64 ReLU -> 64 ReLU -> 40 outputs = per lobe (mean direction
  * m (3, normalised), log kappa (clamped to [-3, 8]), weight logit (softmax)).
  * FP16 weights and activations, FP32 accumulation, on the tensor cores.
@@ -333,10 +335,12 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
 #define DL_GUIDE_PARAMS 16560
 typedef struct dl_guide dl_guide;
 typedef struct dl_guide_config {
-    float learning_rate;     /* Adam step size (1e-3) */
+    float learning_rate;     /* Adam step size (2e-3) */
     float guide_fraction;    /* probability of sampling the learned proposal at a guided vertex (0.5) */
-    int32_t batch;           /* training records per Adam step (65536) */
-    int32_t steps_per_pass;  /* Adam steps after each pass of dl_render_guided (8) */
+    int32_t batch;           /* training records per Adam step (32768) */
+    int32_t steps_per_pass;  /* Adam steps after each pass of dl_render_guided (16) */
+    int32_t max_guided_depth; /* vertices at this depth or deeper sample the BSDF alone (6) */
+    int32_t reserved;
     uint64_t seed;           /* initial weights */
 } dl_guide_config;
 int dl_guide_default_config(dl_guide_config* cfg);
@@ -348,18 +352,21 @@ int dl_guide_set_params(dl_guide* guide, const float* params);
 int dl_guide_forward(dl_guide* guide, int64_t n, const float* inputs, float* outputs);
 /* Training records, 12 floats each: position in [0,1]^3 (3), normal (3),
  * sampled direction (3), its sampling pdf, radiance estimate along it, 0.
- * Loss: -(1/n) sum (L/p) / mean(L/p) log q(direction).  dl_guide_gradient
+ * Loss: -(1/n) sum min((L/p) / mean(L/p), 20) log q(direction).  dl_guide_gradient
  * returns the gradient of that loss (DL_GUIDE_PARAMS floats) and the loss
  * without updating; dl_guide_train runs `steps` Adam steps on the batch. */
 int dl_guide_gradient(dl_guide* guide, int64_t n, const float* records, float* grad, float* loss);
 int dl_guide_train(dl_guide* guide, int64_t n, const float* records, int32_t steps, float* loss);
 
 /* Progressive guided render (as dl_render, image to host): passes of 1, 1,
- * 2, 4, ... samples per pixel; with `train` set, every pass writes training
- * records at its guided vertices (diffuse, Beckmann, GGX surfaces; radiance
- * gathered later on the path credited to the two most recent ones) and the
- * guide takes steps_per_pass Adam steps on them before the next pass.  With
- * `train` 0 the network is frozen.  All samples add to one film. */
+ * 2, 4, ... samples per pixel.  Guided vertices are those on diffuse,
+ * Beckmann and GGX surfaces shallower than max_guided_depth.  With `train`
+ * set, a hashed subset of each pass's guided vertices -- about batch x
+ * steps_per_pass of them, spread over the whole image -- become training
+ * records (radiance gathered later on the path is credited to the two most
+ * recent ones) and the guide takes steps_per_pass Adam steps on interleaved
+ * subsets of them before the next pass.  With `train` 0 the network is
+ * frozen.  All samples add to one film. */
 int dl_render_guided(dl_scene* scene, const dl_render_opts* opts, dl_guide* guide, int32_t train, float* rgb_out);
 
 /* --------------------------------------------------------------- statistics */
@@ -381,7 +388,8 @@ typedef struct dl_stats {
     double retire_ms;          /* the miss kernel (envmap, sample store, new camera paths) */
     int64_t kernel_launches;   /* kernels launched by the last render */
     int64_t guide_records;     /* training records written by the last guided render */
-    double guide_train_ms;     /* host-timed training of the last guided render */
+    double guide_train_ms;     /* device time of the last training round of the last guided
+                                  render (rounds overlap the next pass's rendering) */
 } dl_stats;
 
 /* Enable (1) or disable (0) per-kernel event timing on a context. */

@@ -36,9 +36,9 @@ def _h(x, fp16):
 
 
 def encode(inp, fp16=True):
-    """inp (n, 6) -> (n, 144): per scalar, (sin, cos)(2^k pi x) for k < 12."""
+    """inp (n, 6) -> (n, 144): per scalar, (sin, cos)(2^(k-3) pi x) for k < 12."""
     inp = np.asarray(inp, np.float64)
-    k = (2.0 ** np.arange(N_FREQ)) * np.pi
+    k = (2.0 ** (np.arange(N_FREQ) - 3)) * np.pi
     a = inp[:, :, None] * k[None, None, :]                     # (n, 6, 12)
     e = np.stack([np.sin(a), np.cos(a)], axis=-1).reshape(len(inp), N_ENC)
     return _h(e, fp16)
@@ -83,13 +83,18 @@ def mixture_pdf(o, w):
     return (lam * vmf_pdf(mu, kappa, np.asarray(w, np.float64))).sum(-1)
 
 
+CLAMP = 20.0
+
+
 def loss_and_dout(o, rec):
-    """Loss of records `rec` (n, 12) and dLoss/do (n, 40) for outputs o."""
+    """Loss of records `rec` (n, 12) and dLoss/do (n, 40) for outputs o.
+    Record weights L/p are normalised by their batch mean and clamped at
+    CLAMP times it."""
     n = len(rec)
     L, pdf, w = rec[:, 10], rec[:, 9], rec[:, 6:9]
     ratio = np.where(pdf > 0, L / np.where(pdf > 0, pdf, 1.0), 0.0)
-    mean = ratio.sum() / n
-    scale = np.where((pdf > 0) & (mean > 0), ratio / mean / n if mean > 0 else 0.0, 0.0)
+    mean = np.float32(np.float32(ratio.astype(np.float32).sum()) / np.float32(n)) if n else 0.0
+    scale = np.where((pdf > 0) & (mean > 0), np.minimum(ratio / mean if mean > 0 else 0.0, CLAMP) / n, 0.0)
     mu, kappa, lam, inv_len, clamped = decode(o)
     pj = lam * vmf_pdf(mu, kappa, w)
     q = pj.sum(-1)

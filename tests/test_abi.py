@@ -52,7 +52,7 @@ def test_struct_sizes_match_header():
 
 
 STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts", "dl_request",
-           "dl_tune_params",
+           "dl_tune_params", "dl_guide_config",
            "dl_scene_info", "dl_stats", "dl_traversal_counts"]
 
 

@@ -74,3 +74,17 @@ def test_batch_arguments_are_checked(ctx):
     with pytest.raises(api.DrawlabError):
         ctx.render_batch([(s, abi.make_opts(spp=0))])
     assert ctx.render_batch([]) == []
+
+
+def test_camera_override_equals_a_scene_with_that_camera(ctx):
+    base = scenes.cornell(width=48, height=40)
+    cam = scenes.Camera(width=64, height=32, eye=(0.3, 0.1, 3.5), lookat=(0.0, -0.2, 0.0), up=(0.0, 1.0, 0.0),
+                        fov=35.0)
+    other = scenes.cornell(width=48, height=40)
+    other.camera = cam
+    sa = api.Scene.from_data(ctx, base)
+    sb = api.Scene.from_data(ctx, other)
+    o = abi.make_opts(spp=4, max_depth=5, seed=12)
+    img, = ctx.render_batch([(sa, o, cam)])
+    assert img.shape == (32, 64, 3)
+    np.testing.assert_array_equal(img, sb.render(o))

@@ -62,18 +62,26 @@ def test_training_changes_the_network(ctx):
 
 
 def test_guided_beats_plain_at_equal_time(ctx):
+    # relMSE against a 16k-spp plain reference, guided (256 spp, training
+    # included in its time) vs plain with the same device time.  Single
+    # renders of this sun-lit room are firefly-dominated (a few samples near
+    # the sun's edge), so the comparison uses the relMSE without the 0.1 %
+    # largest per-pixel errors, median over three independent runs.
     W, H = 96, 54
     gs = api.Scene.from_data(ctx, room(W, H, grid=32))
     ref = gs.render(abi.make_opts(spp=16384, max_depth=12, seed=100))
-    spp_g = 256
-    g = api.Guide(ctx, seed=11)
-    img_g = gs.render_guided(abi.make_opts(spp=spp_g, max_depth=12, seed=7), g)
-    t_g = ctx.stats().render_ms
-    gs.render(abi.make_opts(spp=64, max_depth=12, seed=8))
-    t_p64 = ctx.stats().render_ms
-    spp_p = max(1, int(round(64 * t_g / t_p64)))
-    img_p = gs.render(abi.make_opts(spp=spp_p, max_depth=12, seed=9))
-    e_g, e_p = metrics.relmse(img_g, ref), metrics.relmse(img_p, ref)
-    print("equal time: guided %d spp %.1f ms relMSE %.4g | plain %d spp relMSE %.4g | ratio %.2f"
-          % (spp_g, t_g, e_g, spp_p, e_p, e_p / e_g))
-    assert e_g < e_p
+    eg, ep, rg, rp = [], [], [], []
+    for rep in range(3):
+        g = api.Guide(ctx, seed=11 + rep)
+        img_g = gs.render_guided(abi.make_opts(spp=256, max_depth=12, seed=7 + rep), g)
+        t_g = ctx.stats().render_ms
+        gs.render(abi.make_opts(spp=64, max_depth=12, seed=8))
+        spp_p = max(1, int(round(64 * t_g / ctx.stats().render_ms)))
+        img_p = gs.render(abi.make_opts(spp=spp_p, max_depth=12, seed=9 + rep))
+        eg.append(metrics.relmse(img_g, ref))
+        ep.append(metrics.relmse(img_p, ref))
+        rg.append(metrics.relmse_robust(img_g, ref))
+        rp.append(metrics.relmse_robust(img_p, ref))
+    print("equal time relMSE: guided %s plain %s | robust: guided %s plain %s ratio %.2f"
+          % (np.round(eg, 4), np.round(ep, 4), np.round(rg, 4), np.round(rp, 4), np.median(rp) / np.median(rg)))
+    assert np.median(rg) < np.median(rp)
