@@ -413,7 +413,7 @@ def run_guided(args):
     ctx = api.Context(local)
     small = api.Scene.from_data(ctx, scenes.guiding_room(width=480, height=270))
     ref = small.render(abi.make_opts(spp=16384, max_depth=12, seed=1000))
-    spp_g = 64
+    spp_g = 256
     results = []
     for rep in range(max(1, args.steps)):
         g = api.Guide(ctx, seed=40 + rep)
