@@ -509,6 +509,7 @@ int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out)
         const size_t pb = dl::kGuideParams * 4;
         for (dl::DevBuf* b : {&G->w32, &G->grad, &G->m, &G->v}) b->ensure(pb);
         G->w16.ensure(dl::kGuideParams * 2);
+        G->image.ensure(dl::kGuideImageBytes);
         G->scratch.ensure(256);
         DL_CUDA(cudaStreamCreateWithFlags(&G->train_stream, cudaStreamNonBlocking));
         for (int k = 0; k < 2; k++) {
@@ -569,7 +570,11 @@ int dl_guide_forward(dl_guide* G, int64_t n, const float* inputs, float* outputs
         DL_CUDA(cudaMemcpyAsync(G->io_in.ptr, inputs, (size_t)n * 24, cudaMemcpyHostToDevice, ctx->stream));
         dl::guide_forward(G, G->io_in.as<float>(), G->io_out.as<float>(), n);
         DL_CUDA(cudaMemcpyAsync(outputs, G->io_out.ptr, (size_t)n * 160, cudaMemcpyDeviceToHost, ctx->stream));
+        unsigned err = 0;
+        DL_CUDA(cudaMemcpyAsync(&err, G->scratch.as<char>() + dl::kGuideErrOffset, 4, cudaMemcpyDeviceToHost,
+                                ctx->stream));
         DL_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (err) throw dl::Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in the network kernel");
     });
 }
 

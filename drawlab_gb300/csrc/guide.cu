@@ -14,43 +14,52 @@
 //                        sums
 //   k_guide_wgrad        weight gradients dW = dY^T Z over the batch
 //                        (mma.sync, K = batch rows)
-//   k_guide_adam         Adam on the fp32 master weights, fp16 copy
+//   k_guide_adam         Adam on the fp32 master weights; refreshes the fp16
+//                        copy and the tensor cores' weight image
+// Inference (k_guide_infer, and the guided material kernels in render.cu)
+// runs on tcgen05 (guide_tc.cuh).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "guide.cuh"
+#include "guide_tc.cuh"
 #include "internal.h"
 #include "scene.h"
 
 namespace dl {
 
 // ------------------------------------------------------------- inference
-constexpr int kInferWarps = 4;
+static_assert(kGImgBytes == kGuideImageBytes, "image size");
 
-__global__ void __launch_bounds__(32 * kInferWarps) k_guide_infer(const __half* w16, const float* w32,
-                                                                  const float* in, float* out, int n) {
-    __shared__ GuideTile tiles[kInferWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    GuideTile& T = tiles[warp];
-    const int ntiles = (n + 15) / 16;
-    for (int tile = blockIdx.x * kInferWarps + warp; tile < ntiles; tile += gridDim.x * kInferWarps) {
-        const int r = tile * 16 + (lane & 15);
-        if (lane < 16) {
-            float x[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (r < n)
-                for (int i = 0; i < 6; i++) x[i] = in[6 * (size_t)r + i];
-            encode_input(x, T.x + lane * kGXs);
+// Raw network outputs (40 per row) of n input rows, 128 rows per tile on
+// the tensor cores.
+__global__ void __launch_bounds__(kTcRows) k_guide_infer(const void* image, const float* in, float* out, int n,
+                                                          unsigned* err) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    GuideTcSmem& S = *reinterpret_cast<GuideTcSmem*>(dyn_smem);
+    const int ntiles = (n + kTcRows - 1) / kTcRows;
+    if ((int)blockIdx.x >= ntiles) return;
+    uint32_t phase = 0;
+    bool ok = guide_tc_begin(S, image, err);
+    for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        const int r = tile * kTcRows + threadIdx.x;
+        float x[kGIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (r < n)
+            for (int i = 0; i < kGIn; i++) x[i] = in[(size_t)kGIn * r + i];
+        __syncthreads();  // the previous tile's outputs have been read
+        encode_row_tc(x, S.act, threadIdx.x);
+        ok = guide_tc_forward(S, phase, err);
+        if (ok && r < n) {
+            const float* o = tc_out_row(S, threadIdx.x);
+            for (int j = 0; j < kGOut; j++) out[(size_t)r * kGOut + j] = o[j];
         }
-        __syncwarp();
-        forward16(T, w16, w32, lane);
-        if (lane < 16 && r < n)
-            for (int j = 0; j < kGOut; j++) out[(size_t)r * kGOut + j] = T.o[lane * kGOs + j];
-        __syncwarp();
     }
+    guide_tc_end(S, phase);
 }
 
 // -------------------------------------------------------------- training
@@ -266,8 +275,8 @@ __global__ void k_guide_wgrad(const __half* dY, int ldy, const __half* Z, int ld
 
 // Adam on the fp32 master copy; refreshes the fp16 copy and clears the
 // gradient.  The padding rows of layer 3 stay zero.
-__global__ void k_guide_adam(float* w32, __half* w16, float* grad, float* m, float* v, float lr, float b1, float b2,
-                             float c1, float c2, float eps) {
+__global__ void k_guide_adam(float* w32, __half* w16, unsigned char* image, float* grad, float* m, float* v, float lr,
+                             float b1, float b2, float c1, float c2, float eps) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kGParams; i += gridDim.x * blockDim.x) {
         const bool pad = (i >= kGW3 + kGOut * kGHid && i < kGB3) || i >= kGB3 + kGOut;
         if (!pad) {
@@ -281,13 +290,16 @@ __global__ void k_guide_adam(float* w32, __half* w16, float* grad, float* m, flo
             w32[i] = 0.f;
         }
         w16[i] = __float2half_rn(w32[i]);
+        write_image(image, i, w32[i]);
         grad[i] = 0.f;
     }
 }
 
-__global__ void k_guide_to_half(const float* w32, __half* w16) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kGParams; i += gridDim.x * blockDim.x)
+__global__ void k_guide_to_half(const float* w32, __half* w16, unsigned char* image) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kGParams; i += gridDim.x * blockDim.x) {
         w16[i] = __float2half_rn(w32[i]);
+        write_image(image, i, w32[i]);
+    }
 }
 
 // ------------------------------------------------------------------ host
@@ -330,7 +342,7 @@ void guide_init_params(uint64_t seed, std::vector<float>& w) { init_params(seed,
 void guide_upload_params(dl_guide* G, const float* host) {
     cudaStream_t st = G->ctx->stream;
     DL_CUDA(cudaMemcpyAsync(G->w32.ptr, host, kGParams * 4, cudaMemcpyHostToDevice, st));
-    k_guide_to_half<<<64, 256, 0, st>>>(G->w32.as<float>(), G->w16.as<__half>());
+    k_guide_to_half<<<64, 256, 0, st>>>(G->w32.as<float>(), G->w16.as<__half>(), G->image.as<unsigned char>());
     DL_CUDA(cudaGetLastError());
 }
 
@@ -372,7 +384,8 @@ void guide_adam(dl_guide* G, cudaStream_t st) {
     G->step += 1;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)G->step), c2 = 1.f - std::pow(b2, (float)G->step);
-    k_guide_adam<<<64, 256, 0, st>>>(G->w32.as<float>(), G->w16.as<__half>(), G->grad.as<float>(),
+    k_guide_adam<<<64, 256, 0, st>>>(G->w32.as<float>(), G->w16.as<__half>(), G->image.as<unsigned char>(),
+                                     G->grad.as<float>(),
                                      G->m.as<float>(), G->v.as<float>(), G->cfg.learning_rate, b1, b2, c1, c2,
                                      1e-8f);
     DL_CUDA(cudaGetLastError());
@@ -393,11 +406,32 @@ float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps) {
     return loss;
 }
 
+// Blocks of k_guide_infer resident at once on one SM, from its registers and
+// shared memory; the first call raises the kernel's shared-memory limit.
+static int infer_blocks_per_sm() {
+    DL_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(GuideTcSmem)));
+    DL_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int dev = 0;
+    DL_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    DL_CUDA(cudaGetDeviceProperties(&prop, dev));
+    cudaFuncAttributes fa;
+    DL_CUDA(cudaFuncGetAttributes(&fa, k_guide_infer));
+    const int regs_per_warp = ((fa.numRegs + 7) / 8) * 8 * 32;
+    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcRows / 32));
+    const size_t smem = sizeof(GuideTcSmem) + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
+    return std::max(1, std::min(by_regs, (int)(prop.sharedMemPerMultiprocessor / smem)));
+}
+
 void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n) {
-    const int64_t ntiles = (n + 15) / 16;
-    const int blocks = (int)std::min<int64_t>((ntiles + kInferWarps - 1) / kInferWarps, 152 * 16);
-    k_guide_infer<<<blocks, 32 * kInferWarps, 0, G->ctx->stream>>>(G->w16.as<__half>(), G->w32.as<float>(), d_in,
-                                                                   d_out, (int)n);
+    static const int per_sm = infer_blocks_per_sm();
+    cudaStream_t st = G->ctx->stream;
+    unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
+    DL_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
+    const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
+    const int blocks = (int)std::min<int64_t>(ntiles, (int64_t)G->ctx->num_sms * per_sm);
+    k_guide_infer<<<blocks, kTcRows, sizeof(GuideTcSmem), st>>>(G->image.ptr, d_in, d_out, (int)n, err);
     DL_CUDA(cudaGetLastError());
 }
 

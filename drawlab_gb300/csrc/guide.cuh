@@ -4,7 +4,8 @@
 // guided material kernels) and by the training kernels (guide.cu).
 //
 // Network (FP16 weights and activations, FP32 accumulation on the tensor
-// cores with mma.sync m16n8k16):
+// cores: inference with tcgen05.mma in guide_tc.cuh, the training kernels of
+// guide.cu with mma.sync m16n8k16):
 //   input   6 scalars: position scaled to [0, 1]^3 by the scene bounds,
 //           shading normal in [-1, 1]^3
 //   encode  sin / cos (2^(k-3) pi x), k = 0..11, for each scalar: 144 features
@@ -59,10 +60,10 @@ struct GuideRecord {   // one training sample, 48 bytes
 static_assert(sizeof(GuideRecord) == 48, "record layout");
 
 struct GuideNet {
-    const __half* w16;   // kGParams halves
-    const float* w32;    // fp32 master (the biases are read from it)
+    const void* image;   // the weight image of the tensor-core kernels (guide_tc.cuh)
     float fraction;      // probability of sampling the learned proposal
     int max_depth;       // vertices at depth >= max_depth sample the BSDF alone
+    int blocks;          // grid of the guided material kernels (host side)
 };
 
 // ------------------------------------------------------------- encoding
@@ -70,19 +71,27 @@ struct GuideNet {
 // down to 1/128): exact sincospi at k = 0, 4, 8, double-angle steps in
 // between (at most three, error ~1e-6).
 constexpr int kGFreqShift = 3;
-__device__ __forceinline__ void encode_scalar(float x, __half* out) {
+__device__ __forceinline__ void encode_scalar_h2(float x, __half2* out) {
 #pragma unroll
     for (int k0 = 0; k0 < kGFreq; k0 += 4) {
         float s, c;
         sincospif(x * ((float)(1 << k0) / (float)(1 << kGFreqShift)), &s, &c);
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            out[2 * (k0 + k)] = __float2half_rn(s);
-            out[2 * (k0 + k) + 1] = __float2half_rn(c);
+            out[k0 + k] = __floats2half2_rn(s, c);  // (sin, cos): sin at the lower address
             float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
             s = s2;
             c = c2;
         }
+    }
+}
+__device__ __forceinline__ void encode_scalar(float x, __half* out) {
+    __half2 h[kGFreq];
+    encode_scalar_h2(x, h);
+#pragma unroll
+    for (int k = 0; k < kGFreq; k++) {
+        out[2 * k] = __low2half(h[k]);
+        out[2 * k + 1] = __high2half(h[k]);
     }
 }
 
@@ -165,19 +174,6 @@ __device__ __forceinline__ void layer16(const __half* in, int ldi, const __half*
     }
 }
 
-// Forward pass of the 16 rows in `T.x` (encodings already written): the
-// network output lands in T.o; the layer-1 / layer-2 activations stay in
-// T.h / T.x for a backward pass.  Weights: halves `w16`; biases: floats
-// `bias` at the same offsets as in the parameter layout.
-__device__ __forceinline__ void forward16(GuideTile& T, const __half* w16, const float* bias, int lane) {
-    layer16<kGEnc, kGHid, true>(T.x, kGXs, w16 + kGW1, bias + kGB1, T.h, kGHs, nullptr, 0, lane);
-    __syncwarp();
-    layer16<kGHid, kGHid, true>(T.h, kGHs, w16 + kGW2, bias + kGB2, T.x, kGXs, nullptr, 0, lane);
-    __syncwarp();
-    layer16<kGHid, kGOutPad, false>(T.x, kGXs, w16 + kGW3, bias + kGB3, nullptr, 0, T.o, kGOs, lane);
-    __syncwarp();
-}
-
 // -------------------------------------------------------------- mixture
 struct VmfLobe {
     float3 mu;
@@ -220,29 +216,76 @@ __device__ __forceinline__ float vmf_pdf(float3 mu, float kappa, float3 w) {
     return kappa / (2.f * kPiF * (-expm1f(-2.f * kappa))) * expf(kappa * (d - 1.f));
 }
 
-__device__ __forceinline__ float mixture_pdf(const VmfLobe* L, float3 w) {
+// Decoded lobes as the renderer stores them: 8 x {mu.x, mu.y, mu.z, k, c,
+// lambda} floats, with k = kappa (0 for kappa < 1e-4: the uniform sphere)
+// and c = lambda times the lobe's normalisation, so that
+//   q(w) = sum_j c_j exp(k_j (mu_j . w - 1)).
+constexpr int kGLobeFloats = 6;
+constexpr int kGStoredLobes = kGLobes * kGLobeFloats;  // 48
+
+// Decodes the 40 network outputs at `o` in place into the stored form (48
+// floats from `o`; lobes in descending order, so lobe j's outputs
+// [5j, 5j + 5) are read before its stored floats [6j, 6j + 6) are written).
+__device__ __forceinline__ void decode_lobes_inplace(float* o) {
+    float mx = -1e30f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) mx = fmaxf(mx, o[5 * j + 4]);
+    float sum = 0.f;
+#pragma unroll
+    for (int j = kGLobes - 1; j >= 0; j--) {
+        const float m0 = o[5 * j], m1 = o[5 * j + 1], m2 = o[5 * j + 2], lk = o[5 * j + 3], lg = o[5 * j + 4];
+        const float len = sqrtf(m0 * m0 + m1 * m1 + m2 * m2);
+        float3 mu = f3(0.f, 0.f, 1.f);
+        if (len > 1e-6f) mu = f3(m0 / len, m1 / len, m2 / len);
+        const float kappa = expf(fminf(fmaxf(lk, kGLogKappaMin), kGLogKappaMax));
+        const float lam = expf(lg - mx);
+        sum += lam;
+        const bool uniform = kappa < 1e-4f;
+        const float norm = uniform ? 0.25f * kInvPiF : kappa / (2.f * kPiF * (-expm1f(-2.f * kappa)));
+        o[6 * j] = mu.x;
+        o[6 * j + 1] = mu.y;
+        o[6 * j + 2] = mu.z;
+        o[6 * j + 3] = uniform ? 0.f : kappa;
+        o[6 * j + 4] = lam * norm;
+        o[6 * j + 5] = lam;
+    }
+    const float inv = 1.f / sum;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) {
+        o[6 * j + 4] *= inv;
+        o[6 * j + 5] *= inv;
+    }
+}
+
+__device__ __forceinline__ float stored_mixture_pdf(const float* lob, float3 w) {
     float p = 0.f;
 #pragma unroll
-    for (int j = 0; j < kGLobes; j++) p += L[j].lambda * vmf_pdf(L[j].mu, L[j].kappa, w);
+    for (int j = 0; j < kGLobes; j++) {
+        const float* l = lob + kGLobeFloats * j;
+        const float d = l[0] * w.x + l[1] * w.y + l[2] * w.z;
+        p += l[4] * __expf(l[3] * (d - 1.f));
+    }
     return p;
 }
 
 // Sample a direction: lobe by its weight (u0), then the vMF lobe (Jakob's
-// stable inversion of the cosine's distribution, u = (u1, u2)).
-__device__ __forceinline__ float3 mixture_sample(const VmfLobe* L, float u0, float2 u) {
+// stable inversion of the cosine's distribution, u = (u1, u2)); k = 0 lobes
+// are uniform over the sphere.
+__device__ __forceinline__ float3 stored_mixture_sample(const float* lob, float u0, float2 u) {
     int j = kGLobes - 1;
     float acc = 0.f;
 #pragma unroll
     for (int i = 0; i < kGLobes - 1; i++) {
-        acc += L[i].lambda;
+        acc += lob[kGLobeFloats * i + 5];
         if (u0 < acc) {
             j = i;
             break;
         }
     }
-    const float k = L[j].kappa;
+    const float* l = lob + kGLobeFloats * j;
+    const float k = l[3];
     float w;
-    if (k < 1e-4f) {
+    if (k == 0.f) {
         w = 2.f * u.x - 1.f;
     } else {
         w = 1.f + logf(u.x + (1.f - u.x) * expf(-2.f * k)) / k;
@@ -251,40 +294,9 @@ __device__ __forceinline__ float3 mixture_sample(const VmfLobe* L, float u0, flo
     float v = sqrtf(fmaxf(0.f, 1.f - w * w));
     float s, c;
     sincospif(2.f * u.y, &s, &c);
-    Frame f = make_onb(L[j].mu);
+    Frame f = make_onb(f3(l[0], l[1], l[2]));
     float3 loc = f3(v * c, v * s, w);
     return normalize(to_world(f, loc));
-}
-
-// Decoded lobes stored as 8 x {mu.x, mu.y, mu.z, kappa, lambda} floats.
-__device__ __forceinline__ void store_lobes(const VmfLobe* L, float* dst) {
-#pragma unroll
-    for (int j = 0; j < kGLobes; j++) {
-        dst[5 * j] = L[j].mu.x;
-        dst[5 * j + 1] = L[j].mu.y;
-        dst[5 * j + 2] = L[j].mu.z;
-        dst[5 * j + 3] = L[j].kappa;
-        dst[5 * j + 4] = L[j].lambda;
-    }
-}
-
-__device__ __forceinline__ float stored_mixture_pdf(const float* lob, float3 w) {
-    float p = 0.f;
-#pragma unroll
-    for (int j = 0; j < kGLobes; j++)
-        p += lob[5 * j + 4] * vmf_pdf(f3(lob[5 * j], lob[5 * j + 1], lob[5 * j + 2]), lob[5 * j + 3], w);
-    return p;
-}
-
-__device__ __forceinline__ float3 stored_mixture_sample(const float* lob, float u0, float2 u) {
-    VmfLobe L[kGLobes];
-#pragma unroll
-    for (int j = 0; j < kGLobes; j++) {
-        L[j].mu = f3(lob[5 * j], lob[5 * j + 1], lob[5 * j + 2]);
-        L[j].kappa = lob[5 * j + 3];
-        L[j].lambda = lob[5 * j + 4];
-    }
-    return mixture_sample(L, u0, u);
 }
 
 // Network input of a shading point: position scaled into [0, 1]^3 by the

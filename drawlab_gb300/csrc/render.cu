@@ -37,6 +37,7 @@
 
 #include "device.cuh"
 #include "guide.cuh"
+#include "guide_tc.cuh"
 #include "internal.h"
 #include "scene.h"
 
@@ -755,18 +756,14 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 // to the stored sample when traced.  Mirror and dielectric still draw the NEE
 // sample (their eval and pdf are zero: no contribution, no shadow ray).
 //
-// kGuided (diffuse, Beckmann, GGX in a guided render): the warp evaluates the
-// guiding network for its 32 shading points on the tensor cores (two 16-row
-// tiles), and each path samples its next direction by one-sample MIS between
-// the learned vMF mixture (probability `fraction`) and the BSDF, weighting
-// by f cos / (fraction q + (1 - fraction) p_bsdf); NEE's MIS weight uses the
+// kGuided (diffuse, Beckmann, GGX in a guided render): 128-thread blocks take
+// 128 queued hits at a time and evaluate the guiding network for them on the
+// tensor cores (guide_tc.cuh: tcgen05.mma, accumulators in tensor memory);
+// each path samples its next direction by one-sample MIS between the learned
+// vMF mixture (probability `fraction`) and the BSDF, weighting by
+// f cos / (fraction q + (1 - fraction) p_bsdf); NEE's MIS weight uses the
 // same combined pdf.  The vertex becomes a training record.
-constexpr int kGuidedWarps = 2;  // 64-thread blocks for the guided kernels
-struct GuideWarpSmem {
-    GuideTile tile;
-    float lobes[32 * kGOut];
-};
-constexpr size_t kGuidedSmem = sizeof(GuideWarpSmem) * kGuidedWarps;
+constexpr size_t kGuidedSmem = sizeof(GuideTcSmem);
 
 template <int T, bool kMulti, bool kGuided>
 __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
@@ -774,8 +771,17 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
     const int q = p ^ 1;
     const int lane = lane_id();
     const int n = P.cnt->mat[p][T].n;
-    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
-        int i = i0 + lane;
+    // guided: the block walks whole 128-row tiles (every thread takes part in
+    // the network's block-wide steps); otherwise each warp walks 32 rows
+    constexpr int kSpan = kGuided ? kTcRows : 32;
+    uint32_t mma_phase = 0;
+    bool net_ok = false;
+    if (kGuided) {
+        if ((int)blockIdx.x * kTcRows >= n) return;
+        net_ok = guide_tc_begin(*reinterpret_cast<GuideTcSmem*>(dyn_smem), P.gnet.image, &P.cnt->err);
+    }
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~(kSpan - 1); i0 < n; i0 += gridDim.x * blockDim.x) {
+        int i = i0 + (kGuided ? (int)threadIdx.x : lane);
         bool active = i < n;
         int slot = active ? P.mat_q[T][i] : 0;
         bool cont = false, emit = false, done = false;
@@ -837,27 +843,22 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             }
             if (!done && R.max_depth > 0 && depth >= R.max_depth) done = true;
         }
-        // ---- phase 2 (guided): the network on the warp's shading points
+        // ---- phase 2 (guided): the network on the block's 128 shading points
         const bool sampling = active && !done;
-        const bool use_guide = kGuided && sampling && depth < P.gnet.max_depth;
+        bool use_guide = kGuided && sampling && depth < P.gnet.max_depth;
         float in6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         float* lob = nullptr;
         if (kGuided) {
-            GuideWarpSmem& W = reinterpret_cast<GuideWarpSmem*>(dyn_smem)[threadIdx.x >> 5];
-            lob = W.lobes + lane * kGOut;
+            GuideTcSmem& S = *reinterpret_cast<GuideTcSmem*>(dyn_smem);
+            lob = tc_out_row(S, threadIdx.x);
             if (use_guide) guide_input(request<kMulti>(P, rid).sc, h.p, normalize(h.sh.n), in6);
-            for (int half = 0; half < 2; half++) {
-                if (!__any_sync(0xffffffffu, use_guide && (lane >> 4) == half)) continue;
-                if ((lane >> 4) == half) encode_input(in6, W.tile.x + (lane & 15) * kGXs);
-                __syncwarp();
-                forward16(W.tile, P.gnet.w16, P.gnet.w32, lane);
-                if ((lane >> 4) == half && use_guide) {
-                    VmfLobe L[kGLobes];
-                    decode_lobes(W.tile.o + (lane & 15) * kGOs, L);
-                    store_lobes(L, lob);
-                }
-                __syncwarp();
+            // (also the barrier after which the previous tile's lobes are dead)
+            if (__syncthreads_or(use_guide) && net_ok) {
+                encode_row_tc(in6, S.act, threadIdx.x);
+                net_ok = guide_tc_forward(S, mma_phase, &P.cnt->err);
             }
+            if (!net_ok) use_guide = false;  // a wait ran out: sample the BSDF alone
+            if (use_guide) decode_lobes_inplace(lob);
         }
         // ---- phase 3: NEE and the next direction
         bool record = false, rotate = false;
@@ -1002,6 +1003,7 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
         int e = warp_push(&P.cnt->ext[q], push);
         if (push) P.ext_q[q][e] = slot;
     }
+    if (kGuided) guide_tc_end(*reinterpret_cast<GuideTcSmem*>(dyn_smem), mma_phase);
 }
 
 // Film accumulation as a gather (the reference splats each sample with
@@ -1162,13 +1164,14 @@ size_t RenderBuffers::device_bytes() const {
 
 constexpr int kKernelsPerIteration = 8;
 
-// The material kernel of type T: guided (64-thread blocks, the network's
-// tiles in dynamic shared memory) for the non-delta BSDFs of a guided render.
+// The material kernel of type T: guided (the network's tiles and weights in
+// dynamic shared memory, as many blocks as fit at once) for the non-delta
+// BSDFs of a guided render.
 template <int T, bool kMulti>
 static void launch_material(const RenderParams& P, int p, cudaStream_t st, int wb, int th) {
     constexpr bool kCanGuide = !kMulti && T != MAT_MIRROR && T != MAT_DIELECTRIC;
     if (kCanGuide && P.guided)
-        k_material<T, false, true><<<wb * (th / (32 * kGuidedWarps)), 32 * kGuidedWarps, kGuidedSmem, st>>>(P, p);
+        k_material<T, false, true><<<P.gnet.blocks, kTcRows, kGuidedSmem, st>>>(P, p);
     else
         k_material<T, kMulti, false><<<wb, th, 0, st>>>(P, p);
 }
@@ -1362,6 +1365,7 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool mu
                     kms[j] += ms;
                 }
         }
+        if (hc->err & kErrTensorWait) throw Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in a guided kernel");
         if (hc->err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         if (hc->ext[0] == 0 && hc->shadow[0] == 0 && hc->next_path >= total) break;
         if (iters > 1000000) throw Error(DL_ERR_TIMEOUT, "render did not converge");
@@ -1489,6 +1493,34 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
 // Adam steps on consecutive batches, and the next pass samples with the
 // updated network.  All passes add to one film: each sample is an unbiased
 // estimate whichever network drew it.
+// Blocks of a guided material launch: as many as are resident at once (each
+// loads the weights once and walks tiles), from the SM's registers and
+// shared memory.  The first call raises the kernels' dynamic shared-memory
+// limit (before any graph capture).
+template <int T>
+static int guided_resident_blocks() {
+    auto* fn = k_material<T, false, true>;
+    DL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGuidedSmem));
+    DL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int dev = 0;
+    DL_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    DL_CUDA(cudaGetDeviceProperties(&prop, dev));
+    cudaFuncAttributes fa;
+    DL_CUDA(cudaFuncGetAttributes(&fa, fn));
+    const int regs_per_warp = ((fa.numRegs + 7) / 8) * 8 * 32;
+    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcRows / 32));
+    const size_t smem = kGuidedSmem + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
+    const int by_smem = (int)(prop.sharedMemPerMultiprocessor / smem);
+    return std::max(1, std::min(by_regs, by_smem));
+}
+static int guided_blocks(int sms) {
+    static const int per_sm = std::min(std::min(guided_resident_blocks<MAT_DIFFUSE>(),
+                                                guided_resident_blocks<MAT_MICROFACET>()),
+                                       guided_resident_blocks<MAT_ANISO_GGX>());
+    return sms * per_sm;
+}
+
 void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_film, bool train) {
     dl_context* ctx = S->ctx;
     cudaStream_t st = ctx->stream;
@@ -1508,8 +1540,8 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
     B.samples.ensure((size_t)npix * chunk_spp * 16);
     P.samples = B.samples.as<float4>();
     P.guided = 1;
-    P.gnet.w16 = G->w16.as<__half>();
-    P.gnet.w32 = G->w32.as<float>();
+    P.gnet.image = G->image.ptr;
+    P.gnet.blocks = guided_blocks(ctx->num_sms);
     P.gnet.fraction = G->cfg.guide_fraction;
     P.gnet.max_depth = G->cfg.max_guided_depth;
     P.grec = B.grec.as<GuideRec>();

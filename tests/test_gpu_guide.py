@@ -21,12 +21,15 @@ def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-def test_forward_matches_oracle(ctx):
+@pytest.mark.parametrize("n", [1, 37, 128, 1000, 100000])
+def test_forward_matches_oracle(ctx, n):
+    """tcgen05 inference (128-row tiles; a ragged last tile, many tiles per
+    block) against the oracle."""
     g = api.Guide(ctx)
     p = random_params(5).astype(np.float32)
     g.set_params(p)
     np.testing.assert_array_equal(g.params(), p)
-    inp = random_records(1000, 6)[:, :6]
+    inp = random_records(n, 6)[:, :6]
     out = g.forward(inp)
     want, _ = go.forward(p.astype(np.float64), inp, fp16=True)
     # fp16 activations: agreement to fp16-accumulation level
