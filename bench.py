@@ -61,6 +61,63 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def tensor_peak():
+    """Dense fp16/bf16 tensor peak (TFLOP/s) for a kernel timed alone."""
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if "bf16_tflops" in d:
+            return d["bf16_tflops"], "measured"
+    return 1900.0, "fallback"
+
+
+# Multiply-adds per row of the guiding network: 144x64 + 64x64 + 64x48
+# (forward), 48x64 + 64x64 (backward through layers 3 and 2), and the
+# weight gradients (as many as the forward).
+NET_MAC_FWD = 144 * 64 + 64 * 64 + 64 * 48
+NET_MAC_TRAIN = NET_MAC_FWD + (48 * 64 + 64 * 64) + NET_MAC_FWD
+
+
+def network_roofline(ctx, api):
+    """Device time of the network kernels alone (dl_guide_forward on 4M rows;
+    dl_guide_gradient on one 32768-record training batch), as FLOP/s against
+    the measured tensor peak and as bytes/s against HBM."""
+    tpk, tkind = tensor_peak()
+    hbm, hkind = peaks()
+    rng = np.random.default_rng(3)
+    g = api.Guide(ctx, seed=5)
+    n = 1 << 22
+    inp = np.concatenate([rng.uniform(0, 1, (n, 3)), rng.normal(size=(n, 3))], axis=1).astype(np.float32)
+    inp[:, 3:] /= np.linalg.norm(inp[:, 3:], axis=1, keepdims=True)
+    times = []
+    for _ in range(4):
+        g.forward(inp)
+        times.append(ctx.stats().guide_ms)
+    t_inf = float(np.median(times[1:]))
+    nb = 32768
+    rec = np.zeros((nb, 12), np.float32)
+    rec[:, :6] = inp[:nb]
+    w = rng.normal(size=(nb, 3))
+    rec[:, 6:9] = w / np.linalg.norm(w, axis=1, keepdims=True)
+    rec[:, 9] = rng.uniform(0.05, 2.0, nb)
+    rec[:, 10] = rng.uniform(0.0, 3.0, nb)
+    times = []
+    for _ in range(6):
+        g.gradient(rec)
+        times.append(ctx.stats().guide_ms)
+    t_tr = float(np.median(times[1:]))
+    inf_tf = 2.0 * NET_MAC_FWD * n / (t_inf * 1e-3) / 1e12
+    tr_tf = 2.0 * NET_MAC_TRAIN * nb / (t_tr * 1e-3) / 1e12
+    inf_gbs = (24 + 160) * n / (t_inf * 1e-3) / 1e9
+    return {"inference": {"kernel": "k_guide_infer (tcgen05)", "rows": n, "ms": t_inf, "tflops": inf_tf,
+                          "frac_tensor": inf_tf / tpk, "gbs": inf_gbs, "frac_hbm": inf_gbs / hbm,
+                          "bytes_per_row": 184, "flop_per_row": 2 * NET_MAC_FWD},
+            "training_batch": {"kernels": "k_guide_weight_sum + k_guide_fwd_bwd + k_guide_wgrad", "rows": nb,
+                               "ms": t_tr, "tflops": tr_tf, "frac_tensor": tr_tf / tpk,
+                               "flop_per_row": 2 * NET_MAC_TRAIN},
+            "peak_tflops": tpk, "peak_kind": tkind, "hbm_peak": hbm, "hbm_kind": hkind}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -402,17 +459,21 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+REF_SPP = 65536  # plain reference of the equal-time comparison
+
+
 def run_guided(args):
     """Learned guiding at equal time on the window-lit room (2M triangles,
-    depth 12): relMSE of guided vs plain against a 16k-spp plain reference at
-    480x270; throughput of the guided render at 1920x1080."""
+    depth 12): relMSE of guided vs plain against a 64k-spp plain reference at
+    480x270; throughput of the guided render at 1920x1080; the network
+    kernels against the tensor-core peak."""
     local = _device_setup()
     if local is None:
         return
     from drawlab_gb300 import abi, api, metrics, scenes
     ctx = api.Context(local)
     small = api.Scene.from_data(ctx, scenes.guiding_room(width=480, height=270))
-    ref = small.render(abi.make_opts(spp=16384, max_depth=12, seed=1000))
+    ref = small.render(abi.make_opts(spp=REF_SPP, max_depth=12, seed=1000))
     spp_g = 256
     results = []
     for rep in range(max(1, args.steps)):
@@ -442,13 +503,14 @@ def run_guided(args):
         st = ctx.stats()
     ck = clocks.summary()
     samples = 1920 * 1080 * 16
+    net = network_roofline(ctx, api)
     line = {"metric": "relMSE ratio plain/guided at equal time (window-lit room, 2M triangles)",
             "value": e_p / e_g, "unit": "x (median over runs)", "n_gpus": 1, "steps": len(results), "warmup": args.warmup,
             "ms_per_step": float(np.mean([r[2] for r in results])), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network fp16 in, fp32 accumulate)",
             "data": "synthetic (procedural room and sky)",
             "config": {"workload": "guided", "triangles": 1960090, "relmse_resolution": "480x270",
-                       "reference": "plain, 16384 spp", "guided_spp": spp_g, "max_depth": 12,
+                       "reference": "plain, %d spp" % REF_SPP, "guided_spp": spp_g, "max_depth": 12,
                        "l2_flush": "inputs larger than L2 (BVH + samples)"},
             "relmse": {"guided": e_g, "plain": e_p, "runs": [
                 {"guided": r[0], "plain": r[1], "guided_ms": r[2], "plain_ms": r[3], "plain_spp": r[4],
@@ -457,6 +519,7 @@ def run_guided(args):
                               "note": "relMSE without the 0.1 % largest per-pixel errors (sun-edge fireflies)"},
             "guided_1080p": {"samples_per_s": samples / (st.render_ms / 1e3), "ms": st.render_ms,
                              "records": st.guide_records, "train_ms": st.guide_train_ms},
+            "network": net,
             "gpu_launches": st.kernel_launches,
             "e2e": {"value": samples / wall, "unit": "samples/s (guided 1080p, 16 spp)", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 1920 * 1080 * 12, "call": "dl_render_guided"},

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 4
+DL_ABI_VERSION = 5
 
 # status
 DL_OK = 0
@@ -144,6 +144,7 @@ class dl_stats(C.Structure):
         ("kernel_launches", C.c_int64),
         ("guide_records", C.c_int64),
         ("guide_train_ms", C.c_double),
+        ("guide_ms", C.c_double),
     ]
 
 

@@ -568,13 +568,18 @@ int dl_guide_forward(dl_guide* G, int64_t n, const float* inputs, float* outputs
         G->io_in.ensure((size_t)n * 6 * 4);
         G->io_out.ensure((size_t)n * 40 * 4);
         DL_CUDA(cudaMemcpyAsync(G->io_in.ptr, inputs, (size_t)n * 24, cudaMemcpyHostToDevice, ctx->stream));
+        DL_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
         dl::guide_forward(G, G->io_in.as<float>(), G->io_out.as<float>(), n);
+        DL_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
         DL_CUDA(cudaMemcpyAsync(outputs, G->io_out.ptr, (size_t)n * 160, cudaMemcpyDeviceToHost, ctx->stream));
         unsigned err = 0;
         DL_CUDA(cudaMemcpyAsync(&err, G->scratch.as<char>() + dl::kGuideErrOffset, 4, cudaMemcpyDeviceToHost,
                                 ctx->stream));
         DL_CUDA(cudaStreamSynchronize(ctx->stream));
         if (err) throw dl::Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in the network kernel");
+        float ms = 0.f;
+        DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        ctx->stats.guide_ms = ms;
     });
 }
 
@@ -586,13 +591,18 @@ int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad,
         G->recs.ensure((size_t)n * 48);
         DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
+        DL_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
         dl::guide_gradient(G, G->recs.ptr, n, 1, ctx->stream);
+        DL_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
         DL_CUDA(cudaMemcpyAsync(grad, G->grad.ptr, dl::kGuideParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
         float l = 0.f;
         DL_CUDA(cudaMemcpyAsync(&l, G->scratch.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
         DL_CUDA(cudaStreamSynchronize(ctx->stream));
         if (loss) *loss = l;
+        float ms = 0.f;
+        DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        ctx->stats.guide_ms = ms;
     });
 }
 

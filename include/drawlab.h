@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 4
+#define DL_ABI_VERSION 5
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -390,6 +390,8 @@ typedef struct dl_stats {
     int64_t guide_records;     /* training records written by the last guided render */
     double guide_train_ms;     /* device time of the last training round of the last guided
                                   render (rounds overlap the next pass's rendering) */
+    double guide_ms;           /* device time of the network kernels of the last
+                                  dl_guide_forward / dl_guide_gradient call */
 } dl_stats;
 
 /* Enable (1) or disable (0) per-kernel event timing on a context. */

@@ -63,10 +63,11 @@ def test_training_changes_the_network(ctx):
 
 def test_guided_beats_plain_at_equal_time(ctx):
     # relMSE against a 16k-spp plain reference, guided (256 spp, training
-    # included in its time) vs plain with the same device time.  Single
-    # renders of this sun-lit room are firefly-dominated (a few samples near
-    # the sun's edge), so the comparison uses the relMSE without the 0.1 %
-    # largest per-pixel errors, median over three independent runs.
+    # included in its time) vs plain with the same device time, medians over
+    # three independent runs.  Plain renders of this sun-lit room are
+    # firefly-dominated (a few samples near the sun's edge); the guided ones
+    # must have at least 2x lower relMSE, and also win on the relMSE without
+    # the 0.1 % largest per-pixel errors.
     W, H = 96, 54
     gs = api.Scene.from_data(ctx, room(W, H, grid=32))
     ref = gs.render(abi.make_opts(spp=16384, max_depth=12, seed=100))
@@ -84,4 +85,5 @@ def test_guided_beats_plain_at_equal_time(ctx):
         rp.append(metrics.relmse_robust(img_p, ref))
     print("equal time relMSE: guided %s plain %s | robust: guided %s plain %s ratio %.2f"
           % (np.round(eg, 4), np.round(ep, 4), np.round(rg, 4), np.round(rp, 4), np.median(rp) / np.median(rg)))
+    assert np.median(ep) > 2.0 * np.median(eg), (np.median(ep), np.median(eg))
     assert np.median(rg) < np.median(rp)
