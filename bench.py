@@ -112,7 +112,7 @@ def network_roofline(ctx, api):
     return {"inference": {"kernel": "k_guide_infer (tcgen05)", "rows": n, "ms": t_inf, "tflops": inf_tf,
                           "frac_tensor": inf_tf / tpk, "gbs": inf_gbs, "frac_hbm": inf_gbs / hbm,
                           "bytes_per_row": 184, "flop_per_row": 2 * NET_MAC_FWD},
-            "training_batch": {"kernels": "k_guide_weight_sum + k_guide_fwd_bwd + k_guide_wgrad", "rows": nb,
+            "training_batch": {"kernels": "k_guide_weight_sum + k_guide_train_tc (tcgen05)", "rows": nb,
                                "ms": t_tr, "tflops": tr_tf, "frac_tensor": tr_tf / tpk,
                                "flop_per_row": 2 * NET_MAC_TRAIN},
             "peak_tflops": tpk, "peak_kind": tkind, "hbm_peak": hbm, "hbm_kind": hkind}

@@ -492,6 +492,20 @@ int dl_guide_default_config(dl_guide_config* cfg) {
     return DL_OK;
 }
 
+namespace {
+// The guide's error word: a tensor-core wait in a training or network
+// kernel that ran out sets it.
+void guide_err_reset(dl_guide* G, cudaStream_t st) {
+    DL_CUDA(cudaMemsetAsync(G->scratch.as<char>() + dl::kGuideErrOffset, 0, 4, st));
+}
+void guide_err_check(dl_guide* G, cudaStream_t st) {
+    unsigned err = 0;
+    DL_CUDA(cudaMemcpyAsync(&err, G->scratch.as<char>() + dl::kGuideErrOffset, 4, cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    if (err) throw dl::Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in a network kernel");
+}
+}  // namespace
+
 int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out) {
     if (!ctx) return DL_ERR_INVALID_ARG;
     dl_guide* G = nullptr;
@@ -591,6 +605,7 @@ int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad,
         G->recs.ensure((size_t)n * 48);
         DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
+        guide_err_reset(G, ctx->stream);
         DL_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
         dl::guide_gradient(G, G->recs.ptr, n, 1, ctx->stream);
         DL_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -599,6 +614,7 @@ int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad,
         DL_CUDA(cudaMemcpyAsync(&l, G->scratch.as<float>() + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
         DL_CUDA(cudaStreamSynchronize(ctx->stream));
+        guide_err_check(G, ctx->stream);
         if (loss) *loss = l;
         float ms = 0.f;
         DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
@@ -614,7 +630,9 @@ int dl_guide_train(dl_guide* G, int64_t n, const float* records, int32_t steps, 
         need(steps >= 0 && steps <= 100000, "steps out of range");
         G->recs.ensure((size_t)n * 48);
         DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
+        guide_err_reset(G, ctx->stream);
         float l = dl::guide_train(G, G->recs.ptr, n, steps);
+        guide_err_check(G, ctx->stream);
         if (loss) *loss = l;
     });
 }
@@ -630,7 +648,9 @@ int dl_render_guided(dl_scene* S, const dl_render_opts* opts, dl_guide* G, int32
         size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;
         ctx->render.film.ensure((size_t)nf * 4);
         ctx->render.rgb.ensure(nrgb * 4);
+        guide_err_reset(G, ctx->stream);
         dl::render_guided(S, *opts, G, ctx->render.film.as<float>(), train != 0);
+        guide_err_check(G, ctx->stream);
         dl::resolve_film(S, ctx->render.film.as<float>(), opts->filter, ctx->render.rgb.as<float>());
         DL_CUDA(cudaMemcpyAsync(rgb_out, ctx->render.rgb.ptr, nrgb * 4, cudaMemcpyDeviceToHost, ctx->stream));
         DL_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -1,5 +1,5 @@
 // Training and inference of the learned path-guiding proposal (guide.cuh)
-// on the tensor cores, and the dl_guide C ABI.
+// on the fifth-generation tensor cores, and the dl_guide C ABI.
 //
 // One training step on a batch of n records {position, normal, sampled
 // direction w, its sampling pdf p, radiance estimate L along w}:
@@ -7,17 +7,12 @@
 // (an estimate of the KL divergence from the normalised incident radiance to
 // the mixture q, up to a constant), then one Adam update.  Kernels:
 //   k_guide_weight_sum   mean(L / p) over the batch
-//   k_guide_fwd_bwd      per 16-row tile: encoding, forward (mma.sync),
-//                        dLoss/dOutput, backward through layers 3 and 2
-//                        (mma.sync); stores the fp16 activations and output
-//                        gradients of every row, bias gradients by column
-//                        sums
-//   k_guide_wgrad        weight gradients dW = dY^T Z over the batch
-//                        (mma.sync, K = batch rows)
+//   k_guide_train_tc     forward, loss gradient, backward and the weight and
+//                        bias gradients of the whole batch (tcgen05.mma)
 //   k_guide_adam         Adam on the fp32 master weights; refreshes the fp16
 //                        copy and the tensor cores' weight image
 // Inference (k_guide_infer, and the guided material kernels in render.cu)
-// runs on tcgen05 (guide_tc.cuh).
+// runs on tcgen05 too (guide_tc.cuh).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -34,7 +29,7 @@
 namespace dl {
 
 // ------------------------------------------------------------- inference
-static_assert(kGImgBytes == kGuideImageBytes, "image size");
+static_assert(kGImgTrainBytes == kGuideImageBytes, "image size");
 
 // Raw network outputs (40 per row) of n input rows, 128 rows per tile on
 // the tensor cores.
@@ -63,26 +58,10 @@ __global__ void __launch_bounds__(kTcRows) k_guide_infer(const void* image, cons
 }
 
 // -------------------------------------------------------------- training
-constexpr int kTrainWarps = 2;
 // Record weights L/p are normalised by their batch mean and clamped at this
 // multiple of it: a few records near the sun would otherwise carry the
 // whole gradient of a batch.
 constexpr float kGTargetClamp = 20.f;
-struct TrainTile {
-    GuideTile f;                 // x: encoding, then layer-2 output; h: layer-1 output; o: output
-    __half d0[16 * kGHs];        // dLoss / dOutput (48 used)
-    __half d2[16 * kGHs];        // dLoss / d(layer-2 output)
-};
-
-// Activations of the batch kept for the weight gradients (halves, row-major).
-struct TrainActs {
-    __half* x;    // [n][144] encoding
-    __half* h1;   // [n][64]
-    __half* h2;   // [n][64]
-    __half* d0;   // [n][48]
-    __half* d2;   // [n][64]
-    __half* d1;   // [n][64]
-};
 
 __global__ void k_guide_weight_sum(const GuideRecord* s, int n, int stride, float* sum) {
     float acc = 0.f;
@@ -92,54 +71,6 @@ __global__ void k_guide_weight_sum(const GuideRecord* s, int n, int stride, floa
     }
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
-}
-
-// Column sums over the 16 rows of a C fragment pair, added to g[col], g[col+1].
-__device__ __forceinline__ void add_colsums(float* g, int col, float a0, float a1, int lane) {
-    for (int o = 4; o < 32; o <<= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-    }
-    if ((lane >> 2) == 0) {
-        atomicAdd(g + col, a0);
-        atomicAdd(g + col + 1, a1);
-    }
-}
-
-// dY (16 x N) = (dIn (16 x K) W) masked by act > 0; W row-major [K][N] halves.
-// Writes dY as halves to `out` (smem, stride lds) and `gout` (global, stride N),
-// column sums of the fp32 values into gbias.
-template <int K, int N>
-__device__ __forceinline__ void backward16(const __half* din, int ldi, const __half* W, const __half* act, int lda,
-                                           __half* out, int lds, __half* gout, float* gbias, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < N / 8; nt++) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int ks = 0; ks < K / 16; ks++) {
-            uint32_t a[4], b[2];
-            frag_a(a, din + ks * 16, ldi, lane);
-            frag_b_w(b, W + (ks * 16) * N + nt * 8, N, lane);
-            mma16816(c, a, b);
-        }
-        const int col = nt * 8 + 2 * t;
-        if (!(__half2float(act[g * lda + col]) > 0.f)) c[0] = 0.f;
-        if (!(__half2float(act[g * lda + col + 1]) > 0.f)) c[1] = 0.f;
-        if (!(__half2float(act[(g + 8) * lda + col]) > 0.f)) c[2] = 0.f;
-        if (!(__half2float(act[(g + 8) * lda + col + 1]) > 0.f)) c[3] = 0.f;
-        __half h0 = __float2half_rn(c[0]), h1 = __float2half_rn(c[1]);
-        __half h2 = __float2half_rn(c[2]), h3 = __float2half_rn(c[3]);
-        out[g * lds + col] = h0;
-        out[g * lds + col + 1] = h1;
-        out[(g + 8) * lds + col] = h2;
-        out[(g + 8) * lds + col + 1] = h3;
-        gout[g * N + col] = h0;
-        gout[g * N + col + 1] = h1;
-        gout[(g + 8) * N + col] = h2;
-        gout[(g + 8) * N + col + 1] = h3;
-        add_colsums(gbias, col, c[0] + c[2], c[1] + c[3], lane);
-    }
 }
 
 // The loss of one record and dLoss/dOutput (40 values, scaled by `scale`).
@@ -176,101 +107,318 @@ __device__ __forceinline__ float record_grad(const float* o, const GuideRecord& 
     return -scale * logf(q);
 }
 
-__global__ void __launch_bounds__(32 * kTrainWarps) k_guide_fwd_bwd(const __half* w16, const float* w32,
-                                                                    const GuideRecord* s, int n, int stride,
-                                                                    const float* wsum, float* grad,
-                                                                    TrainActs A, float* loss) {
-    __shared__ TrainTile tiles[kTrainWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    TrainTile& T = tiles[warp];
-    const int ntiles = (n + 15) / 16;
-    const float mean = *wsum / (float)n;
-    float lacc = 0.f;
-    for (int tile = blockIdx.x * kTrainWarps + warp; tile < ntiles; tile += gridDim.x * kTrainWarps) {
-        const int r0 = tile * 16;
-        const int r = r0 + (lane & 15);
-        // rows past the batch are zero inputs with zero loss weight
-        if (lane < 16) {
-            float x[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            if (r < n)
-                for (int i = 0; i < 6; i++) x[i] = s[(size_t)r * stride].in[i];
-            encode_input(x, T.f.x + lane * kGXs);
-            for (int k = 0; k < kGEnc; k++) A.x[(size_t)r * kGEnc + k] = T.f.x[lane * kGXs + k];
-        }
-        __syncwarp();
-        // forward, keeping layer-1 (h) and layer-2 (x) activations
-        layer16<kGEnc, kGHid, true>(T.f.x, kGXs, w16 + kGW1, w32 + kGB1, T.f.h, kGHs, nullptr, 0, lane);
-        __syncwarp();
-        layer16<kGHid, kGHid, true>(T.f.h, kGHs, w16 + kGW2, w32 + kGB2, T.f.x, kGXs, nullptr, 0, lane);
-        __syncwarp();
-        layer16<kGHid, kGOutPad, false>(T.f.x, kGXs, w16 + kGW3, w32 + kGB3, nullptr, 0, T.f.o, kGOs, lane);
-        __syncwarp();
-        if (lane < 16) {
-            float d[kGOut];
-            float sc = 0.f;
-            GuideRecord rec = {};
-            if (r < n) rec = s[(size_t)r * stride];
-            if (r < n && rec.pdf > 0.f && mean > 0.f) sc = fminf(rec.L / rec.pdf / mean, kGTargetClamp) / (float)n;
-            lacc += record_grad(T.f.o + lane * kGOs, rec, sc, d);
-            for (int j = 0; j < kGOutPad; j++) {
-                float v = j < kGOut ? d[j] : 0.f;
-                T.d0[lane * kGHs + j] = __float2half_rn(v);
-                A.d0[(size_t)r * kGOutPad + j] = __float2half_rn(v);
-                if (j < kGOut && v != 0.f) atomicAdd(grad + kGB3 + j, v);
-            }
-            for (int k = 0; k < kGHid; k++) {
-                A.h1[(size_t)r * kGHid + k] = T.f.h[lane * kGHs + k];
-                A.h2[(size_t)r * kGHid + k] = T.f.x[lane * kGXs + k];
-            }
-        }
-        __syncwarp();
-        // backward through layers 3 and 2 (activation buffers hold whole
-        // tiles: rows past the batch carry zero gradients)
-        backward16<kGOutPad, kGHid>(T.d0, kGHs, w16 + kGW3, T.f.x, kGXs, T.d2, kGHs, A.d2 + (size_t)r0 * kGHid,
-                                    grad + kGB2, lane);
-        __syncwarp();
-        backward16<kGHid, kGHid>(T.d2, kGHs, w16 + kGW2, T.f.h, kGHs, T.d0, kGHs, A.d1 + (size_t)r0 * kGHid,
-                                 grad + kGB1, lane);
-        __syncwarp();
-    }
-    for (int o = 16; o; o >>= 1) lacc += __shfl_xor_sync(0xffffffffu, lacc, o);
-    if (lane == 0) atomicAdd(loss, lacc);
+// One training batch on the tensor cores (k_guide_train_tc).  A persistent
+// 128-thread block walks 128-record tiles; per tile, each thread owns one
+// record and every product is a tcgen05.mma issued by thread 0 with the
+// accumulator in tensor memory:
+//   forward   x -> h1 -> h2 -> outputs (3 products, as in inference)
+//   loss      dLoss/dOutput of the thread's record: d0 (fp16)
+//   backward  d2 = (d0 W3) * [h2 > 0],  d1 = (d2 W2) * [h1 > 0]
+//             (B operands W3^T, W2^T from the weight image)
+//   weights   [dW1 | . | g_b1 ; . | dW2 | g_b2] += [d1 | d2]^T [x | h1 | 1]
+//             [g_b3 | dW3] += d0^T [1 | h2]
+// The two weight-gradient products read the activation tiles written for
+// the forward and backward products as MN-major operands (M or N = the
+// features, K = the tile's 128 records) and accumulate over all of the
+// block's tiles in tensor memory; bias gradients come from the columns of
+// ones.  At the end each warp reads its 32 accumulator lanes and adds them
+// to the gradient in global memory.
+//
+// Loss scaling: the fp16 activation gradients leave out the loss's 1/n
+// (with n ~ 3e4 records most of them would be fp16 subnormals); they
+// saturate at the fp16 range, and the 1/n is applied, in fp32, when the
+// accumulators are added to the gradient.
+//
+// Shared memory: the weight image (47,808 B), Z = [x | h1 | 1 | h2] (288
+// halves per record) and D = [d0 | d1 | d2] (176 halves per record), both in
+// the canonical layout.  166 KB per block: one block per SM, and no other
+// tensor-core kernel of this library (70 KB each) fits beside it, so its 512
+// tensor-memory columns are always free.
+constexpr int kZK = 288, kDK = 176;                    // halves per record in Z and D
+constexpr int kZx = 0, kZh1 = 144, kZones = 208, kZh2 = 224;
+constexpr int kDd0 = 0, kDd1 = 48, kDd2 = 112;
+constexpr int kTrainCols = 512;
+constexpr int kAccW12 = 64, kAccW3 = kAccW12 + 224;   // accumulator columns ([0, 64): layer products)
+constexpr float kHalfMax = 65504.f;
+
+struct GuideTrainSmem {
+    __half w[kGImgHalves];
+    float bias[kGImgBiases];
+    __half w2t[kGHid * kGHid];
+    __half w3t[kGHid * kGOutPad];
+    alignas(128) __half z[kTcRows * kZK];
+    alignas(128) __half d[kTcRows * kDK];
+    uint64_t bar_w, bar_mma, bar_g;
+    uint32_t tmem;
+    int fail;
+};
+static_assert(offsetof(GuideTrainSmem, w2t) == kGImgW2T && offsetof(GuideTrainSmem, w3t) == kGImgW3T,
+              "image layout");
+static_assert(sizeof(GuideTrainSmem) > 116 * 1024 + 1024, "one training block per SM");
+static_assert(sizeof(GuideTrainSmem) + sizeof(GuideTcSmem) > 228 * 1024, "no inference block beside it");
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+__device__ __forceinline__ uint32_t pack_h2_sat(float a, float b) {
+    return pack_h2(fminf(fmaxf(a, -kHalfMax), kHalfMax), fminf(fmaxf(b, -kHalfMax), kHalfMax));
 }
 
-// G[m][n] += sum_r dY[r][m] Z[r][n] for m < M, n < N over rows [0, rows):
-// one warp per (m16 x n8 tile, chunk of kWgradRows rows).
-constexpr int kWgradRows = 512;
-
-__global__ void k_guide_wgrad(const __half* dY, int ldy, const __half* Z, int ldz, int M, int N, int rows,
-                              float* G) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int tiles_n = N / 8, tiles = (M / 16) * tiles_n;
-    const int chunks = (rows + kWgradRows - 1) / kWgradRows;
-    if (warp >= tiles * chunks) return;
-    const int tile = warp % tiles, chunk = warp / tiles;
-    const int m0 = (tile / tiles_n) * 16, n0 = (tile % tiles_n) * 8;
-    const int g = lane >> 2, t = lane & 3;
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
-    const int rbeg = chunk * kWgradRows, rend = min(rows, rbeg + kWgradRows);
-    const __half zero = __float2half_rn(0.f);
-    auto ldy_at = [&](int r, int m) { return r < rend ? dY[(size_t)r * ldy + m] : zero; };
-    auto ldz_at = [&](int r, int nn) { return r < rend ? Z[(size_t)r * ldz + nn] : zero; };
-    for (int k0 = rbeg; k0 < rend; k0 += 16) {
-        uint32_t a[4], b[2];
-        // A[m][k] = dY[k][m]
-        a[0] = pack2(ldy_at(k0 + 2 * t, m0 + g), ldy_at(k0 + 2 * t + 1, m0 + g));
-        a[1] = pack2(ldy_at(k0 + 2 * t, m0 + g + 8), ldy_at(k0 + 2 * t + 1, m0 + g + 8));
-        a[2] = pack2(ldy_at(k0 + 2 * t + 8, m0 + g), ldy_at(k0 + 2 * t + 9, m0 + g));
-        a[3] = pack2(ldy_at(k0 + 2 * t + 8, m0 + g + 8), ldy_at(k0 + 2 * t + 9, m0 + g + 8));
-        // B[k][n] = Z[k][n]
-        b[0] = pack2(ldz_at(k0 + 2 * t, n0 + g), ldz_at(k0 + 2 * t + 1, n0 + g));
-        b[1] = pack2(ldz_at(k0 + 2 * t + 8, n0 + g), ldz_at(k0 + 2 * t + 9, n0 + g));
-        mma16816(c, a, b);
+// Bias + ReLU of 64 accumulator columns into Z at feature f0 (fp16);
+// returns the mask of the outputs that are > 0 after rounding.
+__device__ __forceinline__ uint64_t train_hidden_epilogue(GuideTrainSmem& S, uint32_t t, const float* bias, int f0) {
+    const int r = threadIdx.x;
+    uint64_t mask = 0;
+#pragma unroll
+    for (int c0 = 0; c0 < kGHid; c0 += 16) {
+        float v[16];
+        tc::ld_32x32b_x16(t + c0, v);
+        uint32_t p[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            __half2 h = __floats2half2_rn(fmaxf(v[2 * j] + bias[c0 + 2 * j], 0.f),
+                                          fmaxf(v[2 * j + 1] + bias[c0 + 2 * j + 1], 0.f));
+            if (__low2float(h) > 0.f) mask |= 1ull << (c0 + 2 * j);
+            if (__high2float(h) > 0.f) mask |= 1ull << (c0 + 2 * j + 1);
+            p[j] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        *reinterpret_cast<uint4*>(S.z + canon_index(r, f0 + c0, kZK)) = make_uint4(p[0], p[1], p[2], p[3]);
+        *reinterpret_cast<uint4*>(S.z + canon_index(r, f0 + c0 + 8, kZK)) = make_uint4(p[4], p[5], p[6], p[7]);
     }
-    atomicAdd(G + (size_t)(m0 + g) * N + n0 + 2 * t, c[0]);
-    atomicAdd(G + (size_t)(m0 + g) * N + n0 + 2 * t + 1, c[1]);
-    atomicAdd(G + (size_t)(m0 + g + 8) * N + n0 + 2 * t, c[2]);
-    atomicAdd(G + (size_t)(m0 + g + 8) * N + n0 + 2 * t + 1, c[3]);
+    return mask;
+}
+
+// 64 accumulator columns masked by `mask` into D at feature f0 (fp16).
+__device__ __forceinline__ void train_backward_epilogue(GuideTrainSmem& S, uint32_t t, uint64_t mask, int f0) {
+    const int r = threadIdx.x;
+#pragma unroll
+    for (int c0 = 0; c0 < kGHid; c0 += 16) {
+        float v[16];
+        tc::ld_32x32b_x16(t + c0, v);
+        uint32_t p[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float a = (mask >> (c0 + 2 * j)) & 1ull ? v[2 * j] : 0.f;
+            const float b = (mask >> (c0 + 2 * j + 1)) & 1ull ? v[2 * j + 1] : 0.f;
+            p[j] = pack_h2_sat(a, b);
+        }
+        *reinterpret_cast<uint4*>(S.d + canon_index(r, f0 + c0, kDK)) = make_uint4(p[0], p[1], p[2], p[3]);
+        *reinterpret_cast<uint4*>(S.d + canon_index(r, f0 + c0 + 8, kDK)) = make_uint4(p[4], p[5], p[6], p[7]);
+    }
+}
+
+// K-major product of one layer: acc (128 x N) = A (Z or D at feature f0,
+// rows of `a_rowlen` halves) x W^T, W [N][K] at `w` (rows of K halves).
+template <int K, int N>
+__device__ __forceinline__ void train_issue(uint32_t acc, uint32_t a_base, int a_rowlen, int f0, uint32_t w) {
+    constexpr uint32_t idesc = tc::idesc_f16_f32(kTcRows, N);
+    tc::fence_after_sync();
+#pragma unroll
+    for (int ks = 0; ks < K / 16; ks++)
+        tc::mma_f16(acc, tc::smem_desc(a_base + (f0 / 8 + 2 * ks) * 128, 128, a_rowlen * 16),
+                    tc::smem_desc(w + ks * 256, 128, K * 16), idesc, ks > 0 ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(kTcRows) k_guide_train_tc(const void* image, const GuideRecord* s, int n,
+                                                             int stride, const float* wsum, float* grad,
+                                                             float* loss, unsigned* err) {
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    GuideTrainSmem& S = *reinterpret_cast<GuideTrainSmem*>(dyn_smem);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int ntiles = (n + kTcRows - 1) / kTcRows;
+    if ((int)blockIdx.x >= ntiles) return;
+    if (tid == 0) {
+        tc::mbar_init(&S.bar_w, 1);
+        tc::mbar_init(&S.bar_mma, 1);
+        tc::mbar_init(&S.bar_g, 1);
+        S.fail = 0;
+    }
+    if (tid < 32) tc::tmem_alloc(&S.tmem, kTrainCols);
+    {   // the columns of ones (features 208..223 of every record)
+        const uint32_t one2 = pack_h2(1.f, 1.f);
+        *reinterpret_cast<uint4*>(S.z + canon_index(tid, kZones, kZK)) = make_uint4(one2, one2, one2, one2);
+        *reinterpret_cast<uint4*>(S.z + canon_index(tid, kZones + 8, kZK)) = make_uint4(one2, one2, one2, one2);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) tc::bulk_load(S.w, image, kGImgTrainBytes, &S.bar_w);
+    bool failed = !tc::mbar_wait(&S.bar_w, 0, kTcWaitNs);
+    if (failed) {
+        S.fail = 1;
+        atomicOr(err, kErrTensorWait);
+    }
+    uint32_t ph = 0, phg = 0;
+    auto wait = [&](uint64_t* bar, uint32_t& parity) {
+        if (!tc::mbar_wait(bar, parity, kTcWaitNs)) {
+            failed = true;
+            S.fail = 1;
+            atomicOr(err, kErrTensorWait);
+        } else {
+            parity ^= 1u;
+        }
+        tc::fence_after_sync();
+    };
+    const uint32_t T = S.tmem;
+    const uint32_t tl = T + ((uint32_t)(tid & ~31) << 16);  // this warp's lanes, column 0
+    const uint32_t za = tc::smem_addr(S.z), da = tc::smem_addr(S.d), wa = tc::smem_addr(S.w);
+    const float mean = *wsum / (float)n;
+    const float inv_n = 1.f / (float)n;
+    float lacc = 0.f;
+    bool pending = false, first = true;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int r = tile * kTcRows + tid;
+        GuideRecord rec = {};
+        float sc = 0.f;  // the record's loss weight times n
+        if (r < n) {
+            rec = s[(size_t)r * stride];
+            if (rec.pdf > 0.f && mean > 0.f) sc = fminf(rec.L / rec.pdf / mean, kGTargetClamp);
+        }
+        // the previous tile's weight-gradient products read Z and D
+        if (pending) wait(&S.bar_g, phg);
+        pending = false;
+        encode_row_tc(rec.in, S.z, tid, kZK);
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        // forward
+        if (tid == 0) {
+            train_issue<kGEnc, kGHid>(T, za, kZK, kZx, wa + 2 * kGImgW1);
+            tc::commit(&S.bar_mma);
+        }
+        wait(&S.bar_mma, ph);
+        const uint64_t m1 = train_hidden_epilogue(S, tl, S.bias + kGImgB1, kZh1);
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        if (tid == 0) {
+            train_issue<kGHid, kGHid>(T, za, kZK, kZh1, wa + 2 * kGImgW2);
+            tc::commit(&S.bar_mma);
+        }
+        wait(&S.bar_mma, ph);
+        const uint64_t m2 = train_hidden_epilogue(S, tl, S.bias + kGImgB2, kZh2);
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        if (tid == 0) {
+            train_issue<kGHid, kGOutPad>(T, za, kZK, kZh2, wa + 2 * kGImgW3);
+            tc::commit(&S.bar_mma);
+        }
+        wait(&S.bar_mma, ph);
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        tc::fence_after_sync();
+        {   // loss and dLoss/dOutput of this thread's record (times n)
+            float o[kGOutPad];
+#pragma unroll
+            for (int c0 = 0; c0 < kGOutPad; c0 += 16) tc::ld_32x32b_x16(tl + c0, o + c0);
+#pragma unroll
+            for (int j = 0; j < kGOut; j++) o[j] += S.bias[kGImgB3 + j];
+            float dd[kGOut];
+            lacc += record_grad(o, rec, sc, dd);
+#pragma unroll
+            for (int c = 0; c < kGOutPad; c += 8) {
+                uint32_t p[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int k = c + 2 * j;
+                    p[j] = pack_h2_sat(k < kGOut ? dd[k] : 0.f, k + 1 < kGOut ? dd[k + 1] : 0.f);
+                }
+                *reinterpret_cast<uint4*>(S.d + canon_index(tid, kDd0 + c, kDK)) = make_uint4(p[0], p[1], p[2], p[3]);
+            }
+        }
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        // backward through layer 3, then layer 2
+        if (tid == 0) {
+            train_issue<kGOutPad, kGHid>(T, da, kDK, kDd0, wa + kGImgW3T);
+            tc::commit(&S.bar_mma);
+        }
+        wait(&S.bar_mma, ph);
+        train_backward_epilogue(S, tl, m2, kDd2);
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        if (tid == 0) {
+            train_issue<kGHid, kGHid>(T, da, kDK, kDd2, wa + kGImgW2T);
+            tc::commit(&S.bar_mma);
+        }
+        wait(&S.bar_mma, ph);
+        train_backward_epilogue(S, tl, m1, kDd1);
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        if (__syncthreads_or(failed)) break;
+        // weight and bias gradients over the tile's 128 records (MN-major
+        // operands, 16 records per instruction), accumulated across tiles
+        if (tid == 0) {
+            tc::fence_after_sync();
+            constexpr uint32_t id12 = tc::idesc_f16_f32(kTcRows, 224, true, true);
+            constexpr uint32_t id3 = tc::idesc_f16_f32(kTcRows, 80, true, true);
+#pragma unroll
+            for (int ks = 0; ks < kTcRows / 16; ks++) {
+                const uint32_t acc = first && ks == 0 ? 0u : 1u;
+                tc::mma_f16(T + kAccW12, tc::smem_desc(da + (kDd1 / 8) * 128 + ks * 2 * kDK * 16, kDK * 16, 128),
+                            tc::smem_desc(za + ks * 2 * kZK * 16, kZK * 16, 128), id12, acc);
+                tc::mma_f16(T + kAccW3, tc::smem_desc(da + ks * 2 * kDK * 16, kDK * 16, 128),
+                            tc::smem_desc(za + (kZones / 8) * 128 + ks * 2 * kZK * 16, kZK * 16, 128), id3, acc);
+            }
+            tc::commit(&S.bar_g);
+        }
+        pending = true;
+        first = false;
+    }
+    if (pending) wait(&S.bar_g, phg);
+    tc::fence_before_sync();
+    const bool bad = __syncthreads_or(failed) != 0;
+    tc::fence_after_sync();
+    if (!bad && !first) {
+        // accumulator lane m: rows 0..63 = units of layer 1 (dW1, b1), 64..127
+        // = units of layer 2 (dW2, b2); of the second product rows 0..39 =
+        // the outputs (b3 in column 0, dW3 in columns 16..79)
+        const int m = tid;
+        float v[16];
+        if (warp < 2) {
+            for (int c0 = 0; c0 < kGEnc; c0 += 16) {
+                tc::ld_32x32b_x16(tl + kAccW12 + c0, v);
+#pragma unroll
+                for (int j = 0; j < 16; j++) atomicAdd(grad + kGW1 + m * kGEnc + c0 + j, v[j] * inv_n);
+            }
+        } else {
+            for (int c0 = 0; c0 < kGHid; c0 += 16) {
+                tc::ld_32x32b_x16(tl + kAccW12 + kZh1 + c0, v);
+#pragma unroll
+                for (int j = 0; j < 16; j++) atomicAdd(grad + kGW2 + (m - kGHid) * kGHid + c0 + j, v[j] * inv_n);
+            }
+        }
+        tc::ld_32x32b_x16(tl + kAccW12 + kZones, v);
+        atomicAdd(grad + (warp < 2 ? kGB1 + m : kGB2 + m - kGHid), v[0] * inv_n);
+        for (int c0 = 0; c0 < 80; c0 += 16) {
+            tc::ld_32x32b_x16(tl + kAccW3 + c0, v);
+            if (m < kGOut) {
+                if (c0 == 0) {
+                    atomicAdd(grad + kGB3 + m, v[0] * inv_n);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) atomicAdd(grad + kGW3 + m * kGHid + c0 - 16 + j, v[j] * inv_n);
+                }
+            }
+        }
+    }
+    for (int o = 16; o; o >>= 1) lacc += __shfl_xor_sync(0xffffffffu, lacc, o);
+    if ((tid & 31) == 0) atomicAdd(loss, lacc * inv_n);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (S.fail) {
+        (void)tc::mbar_wait(&S.bar_w, 0, kTcWaitNs);
+        (void)tc::mbar_wait(&S.bar_mma, ph, kTcWaitNs);
+        (void)tc::mbar_wait(&S.bar_g, phg, kTcWaitNs);
+    }
+    if (tid < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(T, kTrainCols);
+    }
 }
 
 // Adam on the fp32 master copy; refreshes the fp16 copy and clears the
@@ -333,10 +481,6 @@ void init_params(uint64_t seed, std::vector<float>& w) {
 
 }  // namespace
 
-size_t guide_act_bytes(int64_t rows) {
-    return (size_t)rows * (kGEnc + 4 * kGHid + kGOutPad) * sizeof(__half);
-}
-
 void guide_init_params(uint64_t seed, std::vector<float>& w) { init_params(seed, w); }
 
 void guide_upload_params(dl_guide* G, const float* host) {
@@ -346,37 +490,24 @@ void guide_upload_params(dl_guide* G, const float* host) {
     DL_CUDA(cudaGetLastError());
 }
 
-// Gradient of the loss over `n` device records into G->grad (added to it);
-// returns nothing, the loss sum lands in scratch[1].
+// Gradient of the loss over `n` device records (every `stride`-th) added to
+// G->grad; the loss sum lands in scratch[1].
 void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cudaStream_t st) {
-    const int64_t ntiles = (n + 15) / 16, npad = ntiles * 16;
-    G->acts.ensure(guide_act_bytes(npad));
-    __half* a = G->acts.as<__half>();
-    TrainActs A;
-    A.x = a;
-    A.h1 = A.x + npad * kGEnc;
-    A.h2 = A.h1 + npad * kGHid;
-    A.d0 = A.h2 + npad * kGHid;
-    A.d2 = A.d0 + npad * kGOutPad;
-    A.d1 = A.d2 + npad * kGHid;
+    static const bool setup = [] {
+        DL_CUDA(cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(GuideTrainSmem)));
+        return true;
+    }();
+    (void)setup;
     float* sc = G->scratch.as<float>();
+    unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
     DL_CUDA(cudaMemsetAsync(sc, 0, 2 * sizeof(float), st));
     const GuideRecord* R = static_cast<const GuideRecord*>(d_recs);
     k_guide_weight_sum<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(R, (int)n, stride, sc);
-    const int blocks = (int)std::min<int64_t>((ntiles + kTrainWarps - 1) / kTrainWarps, 152 * 16);
-    k_guide_fwd_bwd<<<blocks, 32 * kTrainWarps, 0, st>>>(G->w16.as<__half>(), G->w32.as<float>(), R, (int)n, stride,
-                                                         sc,
-                                                         G->grad.as<float>(), A, sc + 1);
-    auto wgrad = [&](const __half* dy, int ldy, const __half* z, int ldz, int M, int N, float* out) {
-        const int tiles = (M / 16) * (N / 8);
-        const int chunks = (int)((npad + kWgradRows - 1) / kWgradRows);
-        const int warps = tiles * chunks;
-        k_guide_wgrad<<<(warps + 3) / 4, 128, 0, st>>>(dy, ldy, z, ldz, M, N, (int)npad, out);
-    };
-    float* g = G->grad.as<float>();
-    wgrad(A.d1, kGHid, A.x, kGEnc, kGHid, kGEnc, g + kGW1);
-    wgrad(A.d2, kGHid, A.h1, kGHid, kGHid, kGHid, g + kGW2);
-    wgrad(A.d0, kGOutPad, A.h2, kGHid, kGOutPad, kGHid, g + kGW3);
+    const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
+    const int blocks = (int)std::min<int64_t>(ntiles, G->ctx->num_sms);
+    k_guide_train_tc<<<blocks, kTcRows, sizeof(GuideTrainSmem), st>>>(G->image.ptr, R, (int)n, stride, sc,
+                                                                       G->grad.as<float>(), sc + 1, err);
     DL_CUDA(cudaGetLastError());
 }
 

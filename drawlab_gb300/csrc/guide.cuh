@@ -4,8 +4,7 @@
 // guided material kernels) and by the training kernels (guide.cu).
 //
 // Network (FP16 weights and activations, FP32 accumulation on the tensor
-// cores: inference with tcgen05.mma in guide_tc.cuh, the training kernels of
-// guide.cu with mma.sync m16n8k16):
+// cores with tcgen05.mma: inference in guide_tc.cuh, training in guide.cu):
 //   input   6 scalars: position scaled to [0, 1]^3 by the scene bounds,
 //           shading normal in [-1, 1]^3
 //   encode  sin / cos (2^(k-3) pi x), k = 0..11, for each scalar: 144 features
@@ -39,16 +38,6 @@ constexpr int kGW3 = kGB2 + kGHid;
 constexpr int kGB3 = kGW3 + kGOutPad * kGHid;
 constexpr int kGParams = kGB3 + kGOutPad;  // 16560
 constexpr float kGLogKappaMin = -3.f, kGLogKappaMax = 8.f;
-
-// Per-warp shared-memory tile of 16 rows (one m16 tile).
-constexpr int kGXs = kGEnc + 8;   // row stride (halves) of the encoding / layer-2 output
-constexpr int kGHs = kGHid + 8;   // row stride (halves) of the layer-1 output
-constexpr int kGOs = kGOutPad + 1;  // row stride (floats) of the network output
-struct GuideTile {
-    __half x[16 * kGXs];   // encoding; later layer-2 output (aliased)
-    __half h[16 * kGHs];   // layer-1 output
-    float o[16 * kGOs];    // network output
-};
 
 struct GuideRecord {   // one training sample, 48 bytes
     float in[6];       // position in [0, 1]^3, normal
@@ -92,85 +81,6 @@ __device__ __forceinline__ void encode_scalar(float x, __half* out) {
     for (int k = 0; k < kGFreq; k++) {
         out[2 * k] = __low2half(h[k]);
         out[2 * k + 1] = __high2half(h[k]);
-    }
-}
-
-__device__ __forceinline__ void encode_input(const float* in6, __half* row) {
-#pragma unroll
-    for (int i = 0; i < kGIn; i++) encode_scalar(in6[i], row + i * 2 * kGFreq);
-}
-
-// ---------------------------------------------------------- mma helpers
-__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, const uint32_t* b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-__device__ __forceinline__ uint32_t pack2(__half lo, __half hi) {
-    return (uint32_t)__half_as_ushort(lo) | ((uint32_t)__half_as_ushort(hi) << 16);
-}
-__device__ __forceinline__ uint32_t ld2(const __half* p) {  // two consecutive halves, 4-byte aligned
-    return *reinterpret_cast<const uint32_t*>(p);
-}
-
-// A fragment of a row-major 16 x 16 block at `a` (row stride lda halves).
-__device__ __forceinline__ void frag_a(uint32_t* r, const __half* a, int lda, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    r[0] = ld2(a + g * lda + 2 * t);
-    r[1] = ld2(a + (g + 8) * lda + 2 * t);
-    r[2] = ld2(a + g * lda + 2 * t + 8);
-    r[3] = ld2(a + (g + 8) * lda + 2 * t + 8);
-}
-// B fragment (16 x 8, B[k][n]) of y = x W^T with W row-major [n][k] at `w`
-// (row stride ldw): B[k][n] = W[n][k], consecutive k are contiguous.
-__device__ __forceinline__ void frag_b_wt(uint32_t* r, const __half* w, int ldw, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    r[0] = ld2(w + g * ldw + 2 * t);
-    r[1] = ld2(w + g * ldw + 2 * t + 8);
-}
-// B fragment of y = x W with W row-major [k][n] (row stride ldw).
-__device__ __forceinline__ void frag_b_w(uint32_t* r, const __half* w, int ldw, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-    r[0] = pack2(w[(2 * t) * ldw + g], w[(2 * t + 1) * ldw + g]);
-    r[1] = pack2(w[(2 * t + 8) * ldw + g], w[(2 * t + 9) * ldw + g]);
-}
-
-// One dense layer on a 16-row tile: out[16][N] = act(in[16][K] W^T + b),
-// W row-major [N][K] (halves, row stride K), b floats.  ReLU output goes to
-// `out16` (halves, row stride ldo); the linear output (no ReLU) to `outf`.
-template <int K, int N, bool kRelu>
-__device__ __forceinline__ void layer16(const __half* in, int ldi, const __half* W, const float* b, __half* out16,
-                                        int ldo, float* outf, int ldf, int lane) {
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < N / 8; nt++) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int ks = 0; ks < K / 16; ks++) {
-            uint32_t a[4], bb[2];
-            frag_a(a, in + ks * 16, ldi, lane);
-            frag_b_wt(bb, W + (nt * 8) * K + ks * 16, K, lane);
-            mma16816(c, a, bb);
-        }
-        const int col = nt * 8 + 2 * t;
-        const float b0 = b[col], b1 = b[col + 1];
-        c[0] += b0;
-        c[1] += b1;
-        c[2] += b0;
-        c[3] += b1;
-        if (kRelu) {
-            out16[g * ldo + col] = __float2half_rn(fmaxf(c[0], 0.f));
-            out16[g * ldo + col + 1] = __float2half_rn(fmaxf(c[1], 0.f));
-            out16[(g + 8) * ldo + col] = __float2half_rn(fmaxf(c[2], 0.f));
-            out16[(g + 8) * ldo + col + 1] = __float2half_rn(fmaxf(c[3], 0.f));
-        } else {
-            outf[g * ldf + col] = c[0];
-            outf[g * ldf + col + 1] = c[1];
-            outf[(g + 8) * ldf + col] = c[2];
-            outf[(g + 8) * ldf + col + 1] = c[3];
-        }
     }
 }
 

@@ -12,8 +12,9 @@
 //
 // The weights reach shared memory in one bulk copy (cp.async.bulk) of the
 // weight image: the fp16 matrices already in the tensor core's canonical
-// K-major layout, followed by the fp32 biases.  The training kernels keep the
-// image current (guide.cu).
+// K-major layout, followed by the fp32 biases (and, for the training
+// kernel, transposed copies of W2 and W3).  The Adam kernel keeps the image
+// current (guide.cu).
 //
 // Every wait is bounded (one second): a wait that runs out sets bit 2 of the
 // error word, the block stops using the network (its paths sample the BSDF
@@ -43,13 +44,23 @@ constexpr int kGImgW3 = kGImgW2 + kGHid * kGHid;
 constexpr int kGImgHalves = kGImgW3 + kGOutPad * kGHid;  // 16384
 constexpr int kGImgB1 = 0, kGImgB2 = kGHid, kGImgB3 = 2 * kGHid;
 constexpr int kGImgBiases = 2 * kGHid + kGOutPad;            // 176
-constexpr int kGImgBytes = kGImgHalves * 2 + kGImgBiases * 4;  // 33472
-static_assert(kGImgBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+constexpr int kGImgBytes = kGImgHalves * 2 + kGImgBiases * 4;  // 33472: what inference loads
+// The training kernel also loads the transposed matrices of layers 2 and 3
+// (the backward pass multiplies by W, not W^T): W2^T [64][64] and W3^T [64][48].
+constexpr int kGImgW2T = kGImgBytes;                                  // byte offsets
+constexpr int kGImgW3T = kGImgW2T + kGHid * kGHid * 2;
+constexpr int kGImgTrainBytes = kGImgW3T + kGHid * kGOutPad * 2;      // 47808
+static_assert(kGImgBytes % 16 == 0 && kGImgTrainBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
 
-// Canonical K-major layout without swizzle of an R x K fp16 matrix: core
-// matrices of 8 rows x 8 halves stored as 128 contiguous bytes; core
-// matrices adjacent along K are 128 bytes apart (the descriptor's leading
-// byte offset), 8-row groups K * 16 bytes apart (its stride byte offset).
+// Canonical layout without swizzle of an R x K fp16 matrix (R rows of K
+// halves): core matrices of 8 rows x 8 halves stored as 128 contiguous
+// bytes; core matrices adjacent along K are 128 bytes apart, 8-row groups
+// K * 16 bytes apart.  Read as a K-major operand (rows = M or N), the
+// descriptor's leading byte offset is 128 and its stride byte offset K * 16.
+// The same bytes read as an MN-major operand (rows = the K dimension of the
+// product, the K halves = M or N) take leading byte offset K * 16 (along the
+// product's K) and stride byte offset 128 (along M or N): the no-swizzle
+// descriptor keeps the leading offset on the product's K axis either way.
 __host__ __device__ constexpr int canon_index(int r, int k, int K) {
     return (r >> 3) * (K * 8) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
 }
@@ -68,9 +79,24 @@ __host__ __device__ constexpr int guide_image_offset(int i) {
                       : kGImgHalves * 2 + 4 * (kGImgB3 + i - kGB3);
 }
 
+// Byte offset of parameter i in the transposed copies, -1 outside W2 and W3.
+__host__ __device__ constexpr int guide_image_offset_t(int i) {
+    return (i >= kGW2 && i < kGB2)
+               ? kGImgW2T + 2 * canon_index((i - kGW2) % kGHid, (i - kGW2) / kGHid, kGHid)
+           : (i >= kGW3 && i < kGB3)
+               ? kGImgW3T + 2 * canon_index((i - kGW3) % kGHid, (i - kGW3) / kGHid, kGOutPad)
+               : -1;
+}
+
 __device__ __forceinline__ void write_image(unsigned char* img, int i, float v) {
-    if (guide_param_is_weight(i)) *reinterpret_cast<__half*>(img + guide_image_offset(i)) = __float2half_rn(v);
-    else *reinterpret_cast<float*>(img + guide_image_offset(i)) = v;
+    if (guide_param_is_weight(i)) {
+        const __half h = __float2half_rn(v);
+        *reinterpret_cast<__half*>(img + guide_image_offset(i)) = h;
+        const int t = guide_image_offset_t(i);
+        if (t >= 0) *reinterpret_cast<__half*>(img + t) = h;
+    } else {
+        *reinterpret_cast<float*>(img + guide_image_offset(i)) = v;
+    }
 }
 
 // floats per output row: the 40 outputs, decoded in place into 48 lobe
@@ -134,8 +160,8 @@ __device__ __forceinline__ void guide_tc_end(GuideTcSmem& S, uint32_t mma_phase)
 }
 
 // The encoding of one input row, written as 16-byte chunks of the canonical
-// layout (the same values as encode_input).
-__device__ __forceinline__ void encode_row_tc(const float* in6, __half* act, int r) {
+// layout of a matrix with rows of K halves (features 0..143 of row r).
+__device__ __forceinline__ void encode_row_tc(const float* in6, __half* act, int r, int K = kGEnc) {
 #pragma unroll
     for (int i = 0; i < kGIn; i++) {
         __half2 h[kGFreq];
@@ -147,7 +173,7 @@ __device__ __forceinline__ void encode_row_tc(const float* in6, __half* act, int
             v.y = *reinterpret_cast<const uint32_t*>(&h[4 * c + 1]);
             v.z = *reinterpret_cast<const uint32_t*>(&h[4 * c + 2]);
             v.w = *reinterpret_cast<const uint32_t*>(&h[4 * c + 3]);
-            *reinterpret_cast<uint4*>(act + canon_index(r, i * 2 * kGFreq + 8 * c, kGEnc)) = v;
+            *reinterpret_cast<uint4*>(act + canon_index(r, i * 2 * kGFreq + 8 * c, K)) = v;
         }
     }
 }

@@ -195,7 +195,7 @@ struct dl_context {
 struct dl_guide {
     dl_context* ctx = nullptr;
     dl_guide_config cfg{};
-    dl::DevBuf w32, w16, grad, m, v, scratch, acts, recs, io_in, io_out;
+    dl::DevBuf w32, w16, grad, m, v, scratch, recs, io_in, io_out;
     dl::DevBuf image;       // the weights as the tensor-core kernels load them (guide_tc.cuh)
     dl::DevBuf pass_recs;   // training records of guided render passes (two halves, alternating)
     int64_t step = 0;

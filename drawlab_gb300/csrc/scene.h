@@ -31,7 +31,7 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
 
 // Learned guiding (guide.cu).
 constexpr int kGuideParams = 16560;
-constexpr int kGuideImageBytes = 33472;   // fp16 weights in the tensor cores' layout + fp32 biases
+constexpr int kGuideImageBytes = 47808;   // fp16 weights in the tensor cores' layout, fp32 biases, W2^T, W3^T
 constexpr int kGuideErrOffset = 64;       // byte offset of the error word in dl_guide::scratch
 void guide_init_params(uint64_t seed, std::vector<float>& w);
 void guide_upload_params(dl_guide* G, const float* host);

@@ -3,10 +3,12 @@
 // and the accumulator in TMEM, completion through an mbarrier, TMEM loads,
 // and bulk global -> shared copies.
 //
-// Shared-memory operands use the canonical K-major layout without swizzle:
-// the matrix is cut into core matrices of 8 rows x 16 bytes (8 halves), each
-// stored as 128 contiguous bytes (row r at byte 16 r).  Core matrix (i, j)
-// (row group i, K group j) sits at  base + i * SBO + j * LBO.
+// Shared-memory operands use the canonical layouts without swizzle: the
+// matrix is cut into core matrices of 8 rows x 16 bytes (8 halves), each
+// stored as 128 contiguous bytes (row r at byte 16 r).  K-major: core matrix
+// (i, j) (M/N group i, K group j) sits at  base + i * SBO + j * LBO.
+// MN-major: the 16-byte rows run along M/N and the 8 rows along K; core
+// matrix (i, j) again at  base + i * SBO + j * LBO.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -20,8 +22,10 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// 64-bit shared-memory matrix descriptor: start address, leading (K)
-// byte offset, stride (M/N) byte offset, descriptor version 1, no swizzle.
+// 64-bit shared-memory matrix descriptor: start address, leading byte offset
+// (between core matrices along the product's K), stride byte offset (along
+// M or N), descriptor version 1, no swizzle.  Without swizzle the two
+// offsets keep these axes for K-major and MN-major operands alike.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = 0;
     d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
@@ -32,11 +36,13 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return d;
 }
 
-// 32-bit instruction descriptor of kind::f16: fp16 A and B (K-major), fp32
-// accumulator, shape M x N.
-__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+// 32-bit instruction descriptor of kind::f16: fp16 A and B, fp32
+// accumulator, shape M x N; A and B K-major unless `a_mn` / `b_mn`.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N, bool a_mn = false, bool b_mn = false) {
     return (1u << 4)                         // accumulator format: f32
            | (0u << 7) | (0u << 10)          // A, B: f16
+           | ((a_mn ? 1u : 0u) << 15)        // A major-ness
+           | ((b_mn ? 1u : 0u) << 16)        // B major-ness
            | ((uint32_t)(N >> 3) << 17)      // N / 8
            | ((uint32_t)(M >> 4) << 24);     // M / 16
 }

@@ -122,14 +122,21 @@ def gradient(params, rec, fp16=True):
     loss, dout = loss_and_dout(o, rec)
     d0 = np.zeros((len(rec), N_OUT_PAD))
     d0[:, :N_OUT] = dout
-    d0h = _h(d0, fp16)
-    g_b3 = d0.sum(0)
+    # activation gradients are rounded to fp16 loss-scaled: times n (so that
+    # they stay out of fp16's subnormal range), saturated at +-65504
+    S = float(len(rec))
+
+    def hs(x):
+        return _h(np.clip(x * S, -65504.0, 65504.0), fp16) / S if fp16 else x
+
+    d0h = hs(d0)
     d2 = (d0h @ w3) * (h2 > 0)
-    g_b2 = d2.sum(0)
-    d2h = _h(d2, fp16)
+    d2h = hs(d2)
     d1 = (d2h @ w2) * (h1 > 0)
-    g_b1 = d1.sum(0)
-    d1h = _h(d1, fp16)
+    d1h = hs(d1)
+    # bias gradients: sums of the rounded activation gradients, as the GPU
+    # forms them (a product with a column of ones)
+    g_b3, g_b2, g_b1 = d0h.sum(0), d2h.sum(0), d1h.sum(0)
     g_w3 = d0h.T @ h2
     g_w2 = d2h.T @ h1
     g_w1 = d1h.T @ x
