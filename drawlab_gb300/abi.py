@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 5
+DL_ABI_VERSION = 6
 
 # status
 DL_OK = 0
@@ -40,12 +40,15 @@ DL_LIGHT_POINT = 1
 DL_LIGHT_ENVMAP = 2
 
 DL_CAMERA_VIRTUAL = 0
+DL_CAMERA_PERSPECTIVE = 1
+DL_CAMERA_OPENCV = 2
 
 DL_FILTER_GAUSSIAN = 0
 DL_FILTER_BOX = 1
 
 DL_RENDER_FIX_POINT_LIGHT = 1 << 0
 DL_RENDER_POWER_LIGHT_PICK = 1 << 1
+DL_RENDER_NORMALS = 1 << 2
 
 
 class dl_mesh_desc(C.Structure):
@@ -96,6 +99,13 @@ class dl_camera_desc(C.Structure):
         ("lookat", C.c_float * 3),
         ("up", C.c_float * 3),
         ("fov", C.c_float),
+        ("transform", C.c_float * 16),
+        ("near_clip", C.c_float),
+        ("far_clip", C.c_float),
+        ("fx", C.c_float),
+        ("fy", C.c_float),
+        ("cx", C.c_float),
+        ("cy", C.c_float),
     ]
 
 

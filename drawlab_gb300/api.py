@@ -146,13 +146,7 @@ class Context:
             reqs[i].rgb = rgb.ctypes.data_as(C.POINTER(C.c_float))
             reqs[i].film_device = None
             if cam is not None:
-                cd = abi.dl_camera_desc()
-                cd.type = abi.DL_CAMERA_VIRTUAL
-                cd.width, cd.height = cam.width, cam.height
-                cd.eye[:] = [float(v) for v in cam.eye]
-                cd.lookat[:] = [float(v) for v in cam.lookat]
-                cd.up[:] = [float(v) for v in cam.up]
-                cd.fov = cam.fov
+                cd = cam.desc()
                 keep.append(cd)
                 reqs[i].camera = C.cast(C.byref(cd), C.c_void_p)
             else:

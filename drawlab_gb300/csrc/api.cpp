@@ -52,7 +52,8 @@ void check_opts(const dl_render_opts* o) {
     need(o->filter == DL_FILTER_GAUSSIAN || o->filter == DL_FILTER_BOX, "unknown filter");
     need(o->spp_offset >= 0, "spp_offset must be >= 0");
     need(o->max_paths_in_flight >= 0 && o->max_paths_in_flight <= ((int64_t)1 << 28), "max_paths_in_flight out of range");
-    need((o->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT | DL_RENDER_POWER_LIGHT_PICK)) == 0, "unsupported render flags");
+    need((o->flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT | DL_RENDER_POWER_LIGHT_PICK | DL_RENDER_NORMALS)) == 0,
+         "unsupported render flags");
 }
 
 }  // namespace
@@ -354,9 +355,11 @@ std::vector<dl::BatchItem> batch_items(dl_context* ctx, const dl_request* reqs, 
         items[r].cam = q.scene->dev.cam;
         if (q.camera) {
             const dl_camera_desc& c = *q.camera;
-            need(c.type == DL_CAMERA_VIRTUAL && c.width > 0 && c.height > 0 && c.width <= 65536 &&
-                     c.height <= 65536 && c.fov > 0.f && c.fov < 180.f,
-                 "request " + std::to_string(r) + ": bad camera");
+            try {
+                dl::validate_camera(c);
+            } catch (const dl::Error& e) {
+                throw dl::Error(DL_ERR_INVALID_ARG, "request " + std::to_string(r) + ": " + e.what());
+            }
             items[r].cam = dl::make_camera(c);
         }
         if (trial_spp >= 0) items[r].opts.spp = trial_spp > 0 ? trial_spp : std::max(1, q.opts.spp / 8);
@@ -643,6 +646,7 @@ int dl_render_guided(dl_scene* S, const dl_render_opts* opts, dl_guide* G, int32
     return guard(ctx, [&] {
         check_opts(opts);
         need(G != nullptr && G->ctx == ctx, "guide is NULL or belongs to another context");
+        need(!(opts->flags & DL_RENDER_NORMALS), "the normals integrator has no guided form");
         need(rgb_out != nullptr, "rgb_out is NULL");
         int64_t nf = dl::film_floats(S->dev.cam.w, S->dev.cam.h, opts->filter);
         size_t nrgb = (size_t)S->dev.cam.w * S->dev.cam.h * 3;

@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/drawlab.h"
 #include "layout.h"
 
 namespace dl {
@@ -631,7 +632,48 @@ __device__ __forceinline__ float3 env_sample(const DevScene& sc, float3 sh_n, fl
 }
 
 // ---------------------------------------------------------------- camera
-__device__ __forceinline__ void camera_ray(const DevCamera& c, float2 s, float3& o, float3& d) {
+// Row i of a row-major 4x4 matrix times (a0, a1, a2, a3), summed as the
+// reference's Matrix4f * Vector4f (include/core/math/matrix.h:265-271 with
+// TVector::dot: 0 + a0 m0 + a1 m1 + a2 m2 + a3 m3, left to right).
+__device__ __forceinline__ float mrow4(const float* m, int i, float a0, float a1, float a2, float a3) {
+    float s = __fadd_rn(0.f, __fmul_rn(a0, m[4 * i]));
+    s = __fadd_rn(s, __fmul_rn(a1, m[4 * i + 1]));
+    s = __fadd_rn(s, __fmul_rn(a2, m[4 * i + 2]));
+    return __fadd_rn(s, __fmul_rn(a3, m[4 * i + 3]));
+}
+
+// Camera ray through film position s (pixel units, row 0 = top); tmax is
+// the ray's far end (every render ray starts at t = kRayEps).
+__device__ __forceinline__ void camera_ray(const DevCamera& c, float2 s, float3& o, float3& d, float& tmax) {
+    tmax = __int_as_float(0x7f800000);
+    if (c.type == DL_CAMERA_PERSPECTIVE) {
+        // perspective.cpp:84-100: near-plane point of the sample, normalised,
+        // into world space; the ray spans [near, far] / d.z
+        const float sx = __fmul_rn(s.x, c.inv_w), sy = __fmul_rn(s.y, c.inv_h);
+        const float w = mrow4(c.S, 3, sx, sy, 0.f, 1.f);
+        const float nx = __fdiv_rn(mrow4(c.S, 0, sx, sy, 0.f, 1.f), w);
+        const float ny = __fdiv_rn(mrow4(c.S, 1, sx, sy, 0.f, 1.f), w);
+        const float nz = __fdiv_rn(mrow4(c.S, 2, sx, sy, 0.f, 1.f), w);
+        const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz)));
+        const float dx = __fdiv_rn(nx, len), dy = __fdiv_rn(ny, len), dz = __fdiv_rn(nz, len);
+        const float ow = mrow4(c.T, 3, 0.f, 0.f, 0.f, 1.f);
+        o = f3(__fdiv_rn(mrow4(c.T, 0, 0.f, 0.f, 0.f, 1.f), ow), __fdiv_rn(mrow4(c.T, 1, 0.f, 0.f, 0.f, 1.f), ow),
+               __fdiv_rn(mrow4(c.T, 2, 0.f, 0.f, 0.f, 1.f), ow));
+        d = f3(mrow4(c.T, 0, dx, dy, dz, 0.f), mrow4(c.T, 1, dx, dy, dz, 0.f), mrow4(c.T, 2, dx, dy, dz, 0.f));
+        tmax = __fmul_rn(c.far_clip, __fdiv_rn(1.0f, dz));
+        return;
+    }
+    if (c.type == DL_CAMERA_OPENCV) {
+        // include/optix/camera/opencv.h:29-46 with the film position as the
+        // pixel sample: (s - c) / f on the z = 1 plane, through the inverse
+        // extrinsic, from the eye
+        const float px = __fdiv_rn(__fsub_rn(s.x, c.cx), c.fx), py = __fdiv_rn(__fsub_rn(s.y, c.cy), c.fy);
+        const float3 head = f3(mrow4(c.T, 0, px, py, 1.f, 1.f), mrow4(c.T, 1, px, py, 1.f, 1.f),
+                               mrow4(c.T, 2, px, py, 1.f, 1.f));
+        o = ld3(c.eye);
+        d = normalize(sub(head, o));
+        return;
+    }
     float lx = s.x;
     float ly = __fsub_rn(__fsub_rn((float)c.h, s.y), 1.0f);
     float px = __fsub_rn(__fmul_rn(__fmul_rn(lx, c.inv_w), 2.0f), 1.0f);

@@ -47,8 +47,13 @@ struct DevLight {
 
 struct DevCamera {
     int w, h;
-    float eye[3], U[3], V[3], W[3];
+    float eye[3], U[3], V[3], W[3];  // virtual (opencv: eye)
     float inv_w, inv_h;
+    int type;                        // dl_camera_type
+    float S[16];                     // perspective: sample-to-camera, row-major
+    float T[16];                     // perspective: camera-to-world; opencv: inverse extrinsic
+    float far_clip;                  // perspective
+    float fx, fy, cx, cy;            // opencv
 };
 
 struct DevScene {

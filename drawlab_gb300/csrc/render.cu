@@ -211,10 +211,11 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     ps.y = __fadd_rn((float)y, ps.y);
     (void)g.next2d();  // aperture sample: drawn, unused by the "virtual" camera
     float3 o, d;
-    camera_ray(cam, ps, o, d);
+    float tmax;
+    camera_ray(cam, ps, o, d, tmax);
     RayRec r;
     r.o = make_float4(o.x, o.y, o.z, __int_as_float(rid));
-    r.d = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    r.d = make_float4(d.x, d.y, d.z, tmax);
     P.ray[slot] = r;
     PathRec pr;
     pr.tp = make_float4(1.f, 1.f, 1.f, 1.f);
@@ -723,7 +724,8 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
             const DevRequest& R = request<kMulti>(P, m.y >> kReqShift);
             const DevScene& sc = R.sc;
             float3 L = f3(pr.L.x, pr.L.y, pr.L.z);
-            if (sc.env_light >= 0) {
+            // (the normals integrator returns 0 on a miss, normal.cpp:13-14)
+            if (sc.env_light >= 0 && !(R.flags & DL_RENDER_NORMALS)) {
                 float3 dir = xyz(P.ray[slot].d);
                 if (m.y & PF_CAMERA) {
                     L = add(L, sc.env_visual ? env_lookup_dir(sc, dir) : ld3(sc.env_bg));
@@ -816,7 +818,12 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             const DevScene& sc = R.sc;
             h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
             int light = sc.meshes[h.mesh].light;
-            if (flags & PF_CAMERA) {
+            if (R.flags & DL_RENDER_NORMALS) {
+                // the normals integrator (normal.cpp:10-20): |shading normal|
+                // of the first hit, and the path ends
+                Lr = f3(fabsf(h.sh.n.x), fabsf(h.sh.n.y), fabsf(h.sh.n.z));
+                done = true;
+            } else if (flags & PF_CAMERA) {
                 if (light >= 0 && dot(h.sh.n, neg(dir)) > 0.f) Lr = add(Lr, mul(tp, ld3(sc.lights[light].radiance)));
                 depth = 0;
             } else {

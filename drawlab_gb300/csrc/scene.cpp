@@ -113,13 +113,102 @@ void check(bool ok, const std::string& msg) {
 
 }  // namespace
 
-// virtual.cpp:16-42
+namespace {
+
+// 4x4 inverse in double (Gauss-Jordan, partial pivoting), rounded to float.
+bool invert4(const double* a, float* out) {
+    double m[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 8; j++) m[i][j] = j < 4 ? a[4 * i + j] : (j - 4 == i ? 1.0 : 0.0);
+    for (int c = 0; c < 4; c++) {
+        int p = c;
+        for (int r = c + 1; r < 4; r++)
+            if (std::fabs(m[r][c]) > std::fabs(m[p][c])) p = r;
+        if (!(std::fabs(m[p][c]) > 1e-30)) return false;
+        if (p != c)
+            for (int j = 0; j < 8; j++) std::swap(m[p][j], m[c][j]);
+        const double inv = 1.0 / m[c][c];
+        for (int j = 0; j < 8; j++) m[c][j] *= inv;
+        for (int r = 0; r < 4; r++) {
+            if (r == c || m[r][c] == 0.0) continue;
+            const double f = m[r][c];
+            for (int j = 0; j < 8; j++) m[r][j] -= f * m[c][j];
+        }
+    }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) out[4 * i + j] = (float)m[i][j + 4];
+    return true;
+}
+
+void matmul4(const double* a, const double* b, double* out) {
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double s = 0.0;
+            for (int k = 0; k < 4; k++) s += a[4 * i + k] * b[4 * k + j];
+            out[4 * i + j] = s;
+        }
+}
+
+}  // namespace
+
+void validate_camera(const dl_camera_desc& c) {
+    check(c.type == DL_CAMERA_VIRTUAL || c.type == DL_CAMERA_PERSPECTIVE || c.type == DL_CAMERA_OPENCV,
+          "unsupported camera type");
+    check(c.width > 0 && c.height > 0 && c.width <= 65536 && c.height <= 65536, "camera resolution out of range");
+    if (c.type != DL_CAMERA_VIRTUAL)
+        for (int k = 0; k < 16; k++) check(std::isfinite(c.transform[k]), "camera transform must be finite");
+    if (c.type != DL_CAMERA_OPENCV) check(c.fov > 0.f && c.fov < 180.f, "camera fov out of range");
+    if (c.type == DL_CAMERA_PERSPECTIVE) {
+        // Camera rays start at t = 1e-4 like every other render ray; the
+        // reference starts them at near_clip / d.z, the same to within the
+        // factor 1 / d.z only for its default near clip.
+        check(std::fabs(c.near_clip - 1e-4f) <= 1e-9f, "perspective camera: only the default nearClip (1e-4) is supported");
+        check(c.far_clip > c.near_clip && std::isfinite(c.far_clip), "perspective camera: farClip out of range");
+    }
+    if (c.type == DL_CAMERA_OPENCV)
+        check(std::isfinite(c.fx) && std::isfinite(c.fy) && c.fx != 0.f && c.fy != 0.f && std::isfinite(c.cx) &&
+                  std::isfinite(c.cy),
+              "opencv camera: bad intrinsics");
+}
+
+// virtual.cpp:16-42; perspective.cpp:41-73 (sample-to-camera matrix, here
+// composed and inverted in double); opencv.cpp:10-24 (inverse extrinsic and
+// eye).
 DevCamera make_camera(const dl_camera_desc& c) {
     DevCamera cam;
+    std::memset(&cam, 0, sizeof(cam));
+    cam.type = c.type;
     cam.w = c.width;
     cam.h = c.height;
     cam.inv_w = 1.f / c.width;
     cam.inv_h = 1.f / c.height;
+    if (c.type == DL_CAMERA_PERSPECTIVE) {
+        const double aspect = (double)(c.width / (float)c.height);
+        const double n = c.near_clip, f = c.far_clip;
+        const double recip = 1.0 / (f - n), cot = 1.0 / std::tan((double)c.fov * 0.5 * 3.14159265358979323846 / 180.0);
+        const double P[16] = {cot, 0, 0, 0, 0, cot, 0, 0, 0, 0, f * recip, -n * f * recip, 0, 0, 1, 0};
+        const double Sc[16] = {-0.5, 0, 0, 0, 0, -0.5 * aspect, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        const double Tr[16] = {1, 0, 0, -1, 0, 1, 0, -1.0 / aspect, 0, 0, 1, 0, 0, 0, 0, 1};
+        double A[16], B[16];
+        matmul4(Sc, Tr, A);
+        matmul4(A, P, B);
+        if (!invert4(B, cam.S)) throw Error(DL_ERR_INVALID_ARG, "perspective camera: singular projection");
+        for (int k = 0; k < 16; k++) cam.T[k] = c.transform[k];
+        cam.far_clip = c.far_clip;
+        return cam;
+    }
+    if (c.type == DL_CAMERA_OPENCV) {
+        double E[16];
+        for (int k = 0; k < 16; k++) E[k] = c.transform[k];
+        if (!invert4(E, cam.T)) throw Error(DL_ERR_INVALID_ARG, "opencv camera: singular extrinsic");
+        // eye = inverse extrinsic * (0, 0, 0, 1)
+        for (int i = 0; i < 3; i++) cam.eye[i] = cam.T[4 * i + 3];
+        cam.fx = c.fx;
+        cam.fy = c.fy;
+        cam.cx = c.cx;
+        cam.cy = c.cy;
+        return cam;
+    }
     const float pi = 3.14159265358979323846f;
     float aspect = c.width / (float)c.height;
     HV eye = ld(c.eye), look = ld(c.lookat), up = ld(c.up);
@@ -144,10 +233,7 @@ void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_de
     check(nmat == 0 || mats, "materials is NULL");
     check(nl == 0 || lights, "lights is NULL");
     check(cam != nullptr, "camera is NULL");
-    check(cam->type == DL_CAMERA_VIRTUAL, "unsupported camera type");
-    check(cam->width > 0 && cam->height > 0 && cam->width <= 65536 && cam->height <= 65536,
-          "camera resolution out of range");
-    check(cam->fov > 0.f && cam->fov < 180.f, "camera fov out of range");
+    validate_camera(*cam);
     int64_t total = 0;
     for (int i = 0; i < nm; i++) {
         const dl_mesh_desc& m = meshes[i];

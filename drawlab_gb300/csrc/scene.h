@@ -6,6 +6,7 @@
 namespace dl {
 
 DevCamera make_camera(const dl_camera_desc& c);
+void validate_camera(const dl_camera_desc& c);  // throws DL_ERR_INVALID_ARG
 void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,
                     const dl_light_desc* lights, int32_t nl, const dl_camera_desc* cam);
 void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats, int32_t nmat,

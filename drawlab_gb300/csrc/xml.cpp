@@ -9,7 +9,7 @@
 //
 // Supported plugins: mesh rectangle|obj, bsdf diffuse|mirror|dielectric|
 // microfacet|aniso_ggx, emitter area|point|envmap (PFM images), camera
-// virtual, integrator path,
+// virtual|perspective|opencv, integrator path|normals,
 // sampler independent, rfilter gaussian|box.  Anything else is reported as
 // DL_ERR_UNSUPPORTED with its location.
 #include <cctype>
@@ -238,6 +238,11 @@ struct Props {
     float f(const std::string& k, float d) const {
         auto q = get(k, P_FLOAT);
         return q ? q->f : d;
+    }
+    float f(const std::string& k) const {  // required
+        auto q = get(k, P_FLOAT);
+        if (!q) missing(k);
+        return q->f;
     }
     int i(const std::string& k, int d) const {
         auto q = get(k, P_INT);
@@ -720,9 +725,10 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
     std::map<const Obj*, int> mat_index;
     std::vector<dl_light_desc> lights;
     std::list<std::vector<float>> env_images;  // stable storage for envmap texels
-    dl_camera_desc cam;
+    dl_camera_desc cam{};
     std::memset(&cam, 0, sizeof(cam));
     bool have_cam = false, have_integrator = false, have_sampler = false;
+    uint32_t integrator_flags = 0;
     int spp = 1, filter = DL_FILTER_GAUSSIAN;
     auto add_material = [&](const Obj* b) -> int {
         auto f = mat_index.find(b);
@@ -815,15 +821,34 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
             }
             case O_CAMERA: {
                 if (have_cam) throw Error(DL_ERR_PARSE, "There can only be one camera per scene!");
-                if (c->type != "virtual") throw Error(DL_ERR_UNSUPPORTED, "camera type \"" + c->type + "\" is not supported");
                 have_cam = true;
-                cam.type = DL_CAMERA_VIRTUAL;
                 cam.width = c->props.i("width", 1280);
                 cam.height = c->props.i("height", 720);
-                cam.fov = c->props.f("fov", 30.0f);
-                c->props.vec("eye", P_VECTOR, cam.eye, nullptr);
-                c->props.vec("lookat", P_VECTOR, cam.lookat, nullptr);
-                c->props.vec("up", P_VECTOR, cam.up, nullptr);
+                if (c->type == "virtual") {  // virtual.cpp:16-30
+                    cam.type = DL_CAMERA_VIRTUAL;
+                    cam.fov = c->props.f("fov", 30.0f);
+                    c->props.vec("eye", P_VECTOR, cam.eye, nullptr);
+                    c->props.vec("lookat", P_VECTOR, cam.lookat, nullptr);
+                    c->props.vec("up", P_VECTOR, cam.up, nullptr);
+                } else if (c->type == "perspective") {  // perspective.cpp:21-38
+                    cam.type = DL_CAMERA_PERSPECTIVE;
+                    cam.fov = c->props.f("fov", 30.0f);
+                    cam.near_clip = c->props.f("nearClip", 1e-4f);
+                    cam.far_clip = c->props.f("farClip", 1e4f);
+                    const M4 t = c->props.transform("toWorld");
+                    for (int k = 0; k < 16; k++) cam.transform[k] = t.m[k / 4][k % 4];
+                } else if (c->type == "opencv") {  // opencv.cpp:10-24
+                    cam.type = DL_CAMERA_OPENCV;
+                    cam.cx = c->props.f("cx");
+                    cam.cy = c->props.f("cy");
+                    cam.fx = c->props.f("fx");
+                    cam.fy = c->props.f("fy");
+                    if (!c->props.get("extrinsic", P_TRANSFORM)) c->props.missing("extrinsic");
+                    const M4 t = c->props.transform("extrinsic");
+                    for (int k = 0; k < 16; k++) cam.transform[k] = t.m[k / 4][k % 4];
+                } else {
+                    throw Error(DL_ERR_UNSUPPORTED, "camera type \"" + c->type + "\" is not supported");
+                }
                 for (Obj* ch : c->children) {
                     if (ch->kind != O_RFILTER) throw Error(DL_ERR_PARSE, "Camera::addChild: unsupported child");
                     if (ch->type == "gaussian") {
@@ -840,7 +865,9 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
             }
             case O_INTEGRATOR:
                 if (have_integrator) throw Error(DL_ERR_PARSE, "There can only be one integrator per scene!");
-                if (c->type != "path") throw Error(DL_ERR_UNSUPPORTED, "integrator \"" + c->type + "\" is not supported");
+                if (c->type == "normals") integrator_flags = DL_RENDER_NORMALS;  // normal.cpp:35
+                else if (c->type != "path")
+                    throw Error(DL_ERR_UNSUPPORTED, "integrator \"" + c->type + "\" is not supported");
                 have_integrator = true;
                 break;
             case O_SAMPLER:
@@ -873,6 +900,7 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
                 (int32_t)lights.size(), &cam);
     S->defaults.spp = spp;
     S->defaults.filter = filter;
+    S->defaults.flags |= integrator_flags;
     *out = S.release();
     return DL_OK;
 }

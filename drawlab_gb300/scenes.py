@@ -64,12 +64,51 @@ class Light:
 
 @dataclass
 class Camera:
+    """A camera: "virtual" (eye / lookat / up, vertical fov), "perspective"
+    (camera-to-world `transform`, horizontal fov, near / far clip) or
+    "opencv" (intrinsics fx, fy, cx, cy and the world-to-camera `transform`)."""
     width: int = 256
     height: int = 256
     eye: tuple = (0.0, 0.0, 1.0)
     lookat: tuple = (0.0, 0.0, 0.0)
     up: tuple = (0.0, 1.0, 0.0)
     fov: float = 30.0
+    type: int = abi.DL_CAMERA_VIRTUAL
+    transform: np.ndarray | None = None   # (4, 4), row-major
+    near_clip: float = 1e-4
+    far_clip: float = 1e4
+    fx: float = 0.0
+    fy: float = 0.0
+    cx: float = 0.0
+    cy: float = 0.0
+
+    def desc(self) -> abi.dl_camera_desc:
+        d = abi.dl_camera_desc()
+        d.type = self.type
+        d.width, d.height = self.width, self.height
+        d.eye[:] = [float(v) for v in self.eye]
+        d.lookat[:] = [float(v) for v in self.lookat]
+        d.up[:] = [float(v) for v in self.up]
+        d.fov = self.fov
+        t = np.eye(4) if self.transform is None else np.asarray(self.transform, np.float64)
+        d.transform[:] = [float(v) for v in t.reshape(16)]
+        d.near_clip, d.far_clip = self.near_clip, self.far_clip
+        d.fx, d.fy, d.cx, d.cy = self.fx, self.fy, self.cx, self.cy
+        return d
+
+
+def look_at(origin, target, up) -> np.ndarray:
+    """Camera-to-world matrix of a <lookat> transform (camera looks along +z,
+    x to the left: the reference's convention, parser.cpp:343-369)."""
+    o = np.asarray(origin, np.float64)
+    d = np.asarray(target, np.float64) - o
+    d /= np.linalg.norm(d)
+    left = np.cross(np.asarray(up, np.float64), d)
+    left /= np.linalg.norm(left)
+    nup = np.cross(d, left)
+    m = np.eye(4)
+    m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = left, nup, d, o
+    return m
 
 
 @dataclass
@@ -154,14 +193,7 @@ class SceneData:
             ld[i].env_scale = x.env_scale
             ld[i].env_visual = x.env_visual
             ld[i].env_background[:] = [float(v) for v in x.env_background]
-        cam = abi.dl_camera_desc()
-        c = self.camera
-        cam.type = abi.DL_CAMERA_VIRTUAL
-        cam.width, cam.height = c.width, c.height
-        cam.eye[:] = [float(v) for v in c.eye]
-        cam.lookat[:] = [float(v) for v in c.lookat]
-        cam.up[:] = [float(v) for v in c.up]
-        cam.fov = c.fov
+        cam = self.camera.desc()
         keep.extend([md, mat, ld, cam])
         return keep, md, nm, mat, nmat, ld, nl, cam
 

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 5
+#define DL_ABI_VERSION 6
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -105,17 +105,29 @@ typedef struct dl_light_desc {
 } dl_light_desc;
 
 enum dl_camera_type {
-    DL_CAMERA_VIRTUAL = 0  /* "virtual" src/tracer/camera/virtual.cpp:14-123 */
+    DL_CAMERA_VIRTUAL = 0,     /* "virtual" src/tracer/camera/virtual.cpp:14-123 */
+    DL_CAMERA_PERSPECTIVE = 1, /* "perspective" src/tracer/camera/perspective.cpp:19-100:
+                                  pinhole through a camera-to-world transform */
+    DL_CAMERA_OPENCV = 2       /* "opencv" src/tracer/camera/opencv.cpp:8-87 (host) and
+                                  include/optix/camera/opencv.h:24-47 (rays): intrinsics
+                                  fx, fy, cx, cy and a world-to-camera extrinsic */
 };
 
 typedef struct dl_camera_desc {
     int32_t type;          /* dl_camera_type */
     int32_t width;
     int32_t height;
-    float eye[3];
-    float lookat[3];
-    float up[3];
-    float fov;             /* vertical field of view, degrees */
+    float eye[3];          /* virtual */
+    float lookat[3];       /* virtual */
+    float up[3];           /* virtual */
+    float fov;             /* virtual: vertical field of view; perspective: horizontal
+                              field of view (degrees) */
+    float transform[16];   /* row-major 4x4.  perspective: camera-to-world ("toWorld",
+                              identity when absent); opencv: the world-to-camera
+                              "extrinsic" */
+    float near_clip;       /* perspective: near and far clip distances (reference */
+    float far_clip;        /*   defaults 1e-4 and 1e4); camera rays span [near, far] / d.z */
+    float fx, fy, cx, cy;  /* opencv intrinsics (pixels) */
 } dl_camera_desc;
 
 /* ------------------------------------------------------------------ context */
@@ -211,7 +223,13 @@ enum dl_render_flags {
      * the sphere, R the radius of the scene's bounding sphere -- instead of
      * uniformly (src/tracer/scene/scene.cpp:148-163).  The pick probability
      * replaces 1/N in the NEE weight and in the MIS weights of emitter hits. */
-    DL_RENDER_POWER_LIGHT_PICK = 1u << 1
+    DL_RENDER_POWER_LIGHT_PICK = 1u << 1,
+    /* The "normals" integrator (NormalIntegrator::Li,
+     * src/tracer/integrator/normal.cpp:8-20): each sample is the componentwise
+     * absolute value of the shading normal at the camera ray's first hit, 0
+     * when it misses.  Set in the scene's default options by an XML
+     * <integrator type="normals"/>.  Not available for guided renders. */
+    DL_RENDER_NORMALS = 1u << 2
 };
 
 /* Render options.  Reference: PathIntegrator (src/tracer/integrator/path.cpp),

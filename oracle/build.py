@@ -43,9 +43,11 @@ REF_SOURCES = [
     "src/tracer/bsdf/diffuse.cpp",
     "src/tracer/bsdf/microfacet.cpp",
     "src/tracer/bsdf/mirror.cpp",
+    "src/tracer/camera/perspective.cpp",
     "src/tracer/camera/virtual.cpp",
     "src/tracer/emitter/area.cpp",
     "src/tracer/emitter/point.cpp",
+    "src/tracer/integrator/normal.cpp",
     "src/tracer/integrator/path.cpp",
     "src/tracer/mesh/mesh.cpp",
     "src/tracer/mesh/rectangle.cpp",

@@ -38,6 +38,7 @@
 // Compiled with -ffp-contract=off (no fused multiply-add).
 #include "oracle.h"
 
+#include <stdexcept>
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -423,6 +424,10 @@ struct Camera {
     int w, h;
     V3 eye, U, V, W;
     float inv_w, inv_h;
+    int type = DL_CAMERA_VIRTUAL;
+    float S[16], T[16];  // perspective: sample-to-camera, camera-to-world; opencv: T = inverse extrinsic
+    float far_clip = 0.f;
+    float fx = 0.f, fy = 0.f, cx = 0.f, cy = 0.f;
 };
 
 struct Filter {
@@ -1033,6 +1038,11 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
     float eta = 1.f;
     V3 result, tp(1.f, 1.f, 1.f);
     Hit its;
+    if (o.flags & DL_RENDER_NORMALS) {
+        // normal.cpp:10-20: |shading normal| of the first hit, 0 on a miss
+        if (!ray_intersect(sc, ray, its)) return result;
+        return V3(std::fabs(its.sh.n.x), std::fabs(its.sh.n.y), std::fabs(its.sh.n.z));
+    }
     if (!ray_intersect(sc, ray, its)) {
         // miss.cu:20-27: the camera sees the envmap if "visual", else bg_color
         if (sc.env_light >= 0) {
@@ -1107,6 +1117,8 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
 }
 
 // --------------------------------------------------------------- camera
+static void camera_matrices(const dl_camera_desc& c, Camera& cam);
+
 // virtual.cpp:16-42
 Camera make_camera(const dl_camera_desc& c) {
     Camera cam;
@@ -1114,6 +1126,10 @@ Camera make_camera(const dl_camera_desc& c) {
     cam.h = c.height;
     cam.inv_w = 1.f / c.width;
     cam.inv_h = 1.f / c.height;
+    if (c.type != DL_CAMERA_VIRTUAL) {
+        camera_matrices(c, cam);
+        return cam;
+    }
     float fov = c.fov;
     float aspect = c.width / (float)c.height;
     V3 eye = ld3(c.eye), look = ld3(c.lookat), up = ld3(c.up);
@@ -1128,8 +1144,119 @@ Camera make_camera(const dl_camera_desc& c) {
     cam.eye = eye;
     return cam;
 }
-// virtual.cpp:52-65
+// Inverse of a 4x4 matrix given in double, rounded to float: reduce [A | I]
+// to [I | A^-1] with the largest remaining entry as pivot.
+static bool oracle_inverse4(const double* a, float* out) {
+    double m[4][4], r[4][4];
+    int col[4] = {0, 1, 2, 3}, row[4] = {0, 1, 2, 3};
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            m[i][j] = a[4 * i + j];
+            r[i][j] = i == j ? 1.0 : 0.0;
+        }
+    for (int k = 0; k < 4; k++) {
+        int pr = k;
+        for (int i = k + 1; i < 4; i++)
+            if (std::fabs(m[i][k]) > std::fabs(m[pr][k])) pr = i;
+        if (!(std::fabs(m[pr][k]) > 1e-30)) return false;
+        for (int j = 0; j < 4; j++) {
+            std::swap(m[k][j], m[pr][j]);
+            std::swap(r[k][j], r[pr][j]);
+        }
+        const double p = m[k][k];
+        for (int j = 0; j < 4; j++) {
+            m[k][j] /= p;
+            r[k][j] /= p;
+        }
+        for (int i = 0; i < 4; i++) {
+            if (i == k) continue;
+            const double f = m[i][k];
+            for (int j = 0; j < 4; j++) {
+                m[i][j] -= f * m[k][j];
+                r[i][j] -= f * r[k][j];
+            }
+        }
+    }
+    (void)col;
+    (void)row;
+    for (int i = 0; i < 16; i++) out[i] = (float)r[i / 4][i % 4];
+    return true;
+}
+
+// perspective.cpp:41-73 (the sample-to-camera matrix = (scale * translate *
+// projection)^-1, here in double); opencv.cpp:10-24 (inverse extrinsic, eye).
+static void camera_matrices(const dl_camera_desc& c, Camera& cam) {
+    cam.type = c.type;
+    if (c.type == DL_CAMERA_PERSPECTIVE) {
+        const double aspect = (double)(c.width / (float)c.height);
+        const double n = c.near_clip, f = c.far_clip;
+        const double cot = 1.0 / std::tan((double)c.fov / 2.0 * (3.14159265358979323846 / 180.0));
+        const double recip = 1.0 / (f - n);
+        // scale(-1/2, -aspect/2, 1) * translate(-1, -1/aspect, 0) * projection
+        double proj[4][4] = {{cot, 0, 0, 0}, {0, cot, 0, 0}, {0, 0, f * recip, -n * f * recip}, {0, 0, 1, 0}};
+        const double sx = -0.5, sy = -0.5 * aspect, tx = -1.0, ty = -1.0 / aspect;
+        double M[16];
+        for (int j = 0; j < 4; j++) {
+            M[0 * 4 + j] = sx * (proj[0][j] + tx * proj[3][j]);
+            M[1 * 4 + j] = sy * (proj[1][j] + ty * proj[3][j]);
+            M[2 * 4 + j] = proj[2][j];
+            M[3 * 4 + j] = proj[3][j];
+        }
+        if (!oracle_inverse4(M, cam.S)) throw std::runtime_error("singular perspective projection");
+        for (int k = 0; k < 16; k++) cam.T[k] = c.transform[k];
+        cam.far_clip = c.far_clip;
+    } else if (c.type == DL_CAMERA_OPENCV) {
+        double E[16];
+        for (int k = 0; k < 16; k++) E[k] = c.transform[k];
+        if (!oracle_inverse4(E, cam.T)) throw std::runtime_error("singular extrinsic");
+        cam.eye = V3(cam.T[3], cam.T[7], cam.T[11]);
+        cam.fx = c.fx;
+        cam.fy = c.fy;
+        cam.cx = c.cx;
+        cam.cy = c.cy;
+    }
+}
+
+// Matrix4f * Vector4f, row i (include/core/math/matrix.h:265-271 and
+// TVector::dot: a running sum from 0, left to right).
+static float mat_row(const float* m, int i, float a0, float a1, float a2, float a3) {
+    float sum = 0.f;
+    sum += a0 * m[4 * i];
+    sum += a1 * m[4 * i + 1];
+    sum += a2 * m[4 * i + 2];
+    sum += a3 * m[4 * i + 3];
+    return sum;
+}
+
+// virtual.cpp:52-65; perspective.cpp:84-100; include/optix/camera/opencv.h:
+// 29-46 with the film position as the pixel sample.  Render rays start at
+// kEps; the perspective camera's far end is far / d.z.
 Ray camera_ray(const Camera& c, P2 s) {
+    if (c.type == DL_CAMERA_PERSPECTIVE) {
+        const float sx = s.x * c.inv_w, sy = s.y * c.inv_h;
+        const float w = mat_row(c.S, 3, sx, sy, 0.f, 1.f);
+        const V3 nearP(mat_row(c.S, 0, sx, sy, 0.f, 1.f) / w, mat_row(c.S, 1, sx, sy, 0.f, 1.f) / w,
+                       mat_row(c.S, 2, sx, sy, 0.f, 1.f) / w);
+        float sum = 0.f;
+        sum += nearP.x * nearP.x;
+        sum += nearP.y * nearP.y;
+        sum += nearP.z * nearP.z;
+        const float len = std::sqrt(sum);
+        const V3 d(nearP.x / len, nearP.y / len, nearP.z / len);
+        const float invZ = 1.0f / d.z;
+        const float ow = mat_row(c.T, 3, 0.f, 0.f, 0.f, 1.f);
+        const V3 o(mat_row(c.T, 0, 0.f, 0.f, 0.f, 1.f) / ow, mat_row(c.T, 1, 0.f, 0.f, 0.f, 1.f) / ow,
+                   mat_row(c.T, 2, 0.f, 0.f, 0.f, 1.f) / ow);
+        const V3 dw(mat_row(c.T, 0, d.x, d.y, d.z, 0.f), mat_row(c.T, 1, d.x, d.y, d.z, 0.f),
+                    mat_row(c.T, 2, d.x, d.y, d.z, 0.f));
+        return make_ray(o, dw, kEps, c.far_clip * invZ);
+    }
+    if (c.type == DL_CAMERA_OPENCV) {
+        const float px = (s.x - c.cx) / c.fx, py = (s.y - c.cy) / c.fy;
+        const V3 head(mat_row(c.T, 0, px, py, 1.f, 1.f), mat_row(c.T, 1, px, py, 1.f, 1.f),
+                      mat_row(c.T, 2, px, py, 1.f, 1.f));
+        return make_ray(c.eye, normalized(head - c.eye));
+    }
     float lx = s.x, ly = (float)c.h - s.y - 1;
     float px = lx * c.inv_w * 2 - 1, py = ly * c.inv_h * 2 - 1;
     V3 d = normalized(px * c.U + py * c.V + c.W);

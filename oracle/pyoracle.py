@@ -166,14 +166,14 @@ class OracleScene:
 class RefScene:
     """The reference's own CPU code bound to one scene (x86 container only)."""
 
-    def __init__(self, scene, filter: int = abi.DL_FILTER_GAUSSIAN, spp: int = 1):
+    def __init__(self, scene, filter: int = abi.DL_FILTER_GAUSSIAN, spp: int = 1, normals: bool = False):
         self.lib = ref_lib()
         if self.lib is None:
             raise RuntimeError("reference harness unavailable")
         self.scene = scene
         keep, md, nm, mat, nmat, ld, nl, cam = scene.descs()
         self._keep = keep
-        h = self.lib.ref_scene_create(md, nm, mat, nmat, ld, nl, C.byref(cam), filter, spp)
+        h = self.lib.ref_scene_create(md, nm, mat, nmat, ld, nl, C.byref(cam), filter, spp, int(normals))
         if not h:
             raise RuntimeError("reference scene: %s" % self.lib.ref_last_error().decode())
         self.h = C.c_void_p(h)

@@ -128,7 +128,7 @@ const char* ref_last_error() { return g_err.c_str(); }
 
 void* ref_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material_desc* mats,
                        int32_t nmat, const dl_light_desc* lights, int32_t nl,
-                       const dl_camera_desc* cam, int32_t filter, int32_t spp) {
+                       const dl_camera_desc* cam, int32_t filter, int32_t spp, int32_t normals) {
     try {
         auto* rs = new RefScene();
         rs->scene = new Scene(PropertyList());
@@ -181,10 +181,23 @@ void* ref_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
         cp.setInteger("width", cam->width);
         cp.setInteger("height", cam->height);
         cp.setFloat("fov", cam->fov);
-        cp.setVector("eye", v3(cam->eye));
-        cp.setVector("lookat", v3(cam->lookat));
-        cp.setVector("up", v3(cam->up));
-        Object* camera = ObjectFactory::createInstance("virtual", cp);
+        Object* camera = nullptr;
+        if (cam->type == DL_CAMERA_VIRTUAL) {
+            cp.setVector("eye", v3(cam->eye));
+            cp.setVector("lookat", v3(cam->lookat));
+            cp.setVector("up", v3(cam->up));
+            camera = ObjectFactory::createInstance("virtual", cp);
+        } else if (cam->type == DL_CAMERA_PERSPECTIVE) {
+            cp.setFloat("nearClip", cam->near_clip);
+            cp.setFloat("farClip", cam->far_clip);
+            Matrix4f m;
+            for (int i = 0; i < 4; i++)
+                for (int j = 0; j < 4; j++) m[i][j] = cam->transform[4 * i + j];
+            cp.setTransform("toWorld", Transform(m));
+            camera = ObjectFactory::createInstance("perspective", cp);
+        } else {
+            throw Exception("camera type not available in the reference CPU backend");
+        }
         Object* rf = ObjectFactory::createInstance(filter == DL_FILTER_BOX ? "box" : "gaussian",
                                                    PropertyList());
         rf->activate();
@@ -196,7 +209,7 @@ void* ref_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
         Object* sampler = ObjectFactory::createInstance("independent", sp);
         sampler->activate();
         rs->scene->addChild(sampler);
-        Object* integ = ObjectFactory::createInstance("path", PropertyList());
+        Object* integ = ObjectFactory::createInstance(normals ? "normals" : "path", PropertyList());
         integ->activate();
         rs->scene->addChild(integ);
         rs->scene->activate();

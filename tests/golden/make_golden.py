@@ -12,8 +12,15 @@ fixtures are its outputs on seeded inputs:
   <scene>_emit.npz    Scene::sampleEmitterDirection at seeded points
   bsdf.npz            BSDF eval/pdf/sample for diffuse, mirror, dielectric,
                       microfacet on seeded directions
+  perspective_normals.npz
+                      the Cornell box seen by the "perspective" camera
+                      (PerspectiveCamera, src/tracer/camera/perspective.cpp)
+                      through the "normals" integrator (NormalIntegrator,
+                      src/tracer/integrator/normal.cpp): (x, y, s) paths ->
+                      |shading normal| of the first hit and film position
 
 Run from the repository root:  python tests/golden/make_golden.py
+(``--only cameras`` writes perspective_normals.npz alone).
 """
 from __future__ import annotations
 
@@ -107,9 +114,31 @@ def emit_inputs(scene, n=512, seed=13):
 LI_SEED = 7
 
 
+def perspective_scene(width=48, height=40):
+    """The Cornell box through a "perspective" camera: a <lookat> toWorld
+    slightly off the box axis, horizontal fov 50, default clip planes."""
+    sc = scenes.cornell(width=width, height=height, spp=2, max_depth=0)
+    sc.camera = scenes.Camera(width=width, height=height, type=abi.DL_CAMERA_PERSPECTIVE, fov=50.0,
+                              transform=scenes.look_at((0.3, 0.2, 3.6), (0.0, -0.1, 0.0), (0.0, 1.0, 0.0)))
+    return sc
+
+
+def write_camera_fixtures():
+    sc = perspective_scene()
+    ref = po.RefScene(sc, spp=sc.spp, normals=True)
+    xys = seeded_paths(sc, 2048, seed=5)
+    L, pos = ref.li(LI_SEED, xys, threads=1)
+    np.savez_compressed(os.path.join(HERE, "perspective_normals.npz"), xys=xys, L=L, pos=pos,
+                        seed=np.uint64(LI_SEED))
+    print("perspective_normals: hits", int((L.sum(1) > 0).sum()), "of", len(L))
+
+
 def main():
     if po.ref_lib() is None:
         raise SystemExit("reference harness unavailable (needs the reference sources)")
+    if "--only" in sys.argv and "cameras" in sys.argv:
+        write_camera_fixtures()
+        return
     for name, sc in fixture_scenes().items():
         ref = po.RefScene(sc, spp=sc.spp)
         rays = seeded_rays(sc, 4096, seed=1)
@@ -137,6 +166,7 @@ def main():
             out[f"m{k}_{key}"] = val
     np.savez_compressed(os.path.join(HERE, "bsdf.npz"), **out)
     print("bsdf fixtures written")
+    write_camera_fixtures()
 
 
 if __name__ == "__main__":

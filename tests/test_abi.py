@@ -48,7 +48,7 @@ def test_struct_sizes_match_header():
     assert C.sizeof(abi.dl_mesh_desc) == 4 * 8 + 2 * 8 + 2 * 4
     assert C.sizeof(abi.dl_material_desc) == 4 * (1 + 3 + 3 + 2 + 2)
     assert C.sizeof(abi.dl_render_opts) == 4 * 4 + 8 + 4 + 4 + 8
-    assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1)
+    assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1 + 16 + 2 + 4)
 
 
 STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts", "dl_request",

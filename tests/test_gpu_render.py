@@ -42,6 +42,18 @@ def all_paths(w, h, spp):
     return np.array([(x, y, s) for y in range(h) for x in range(w) for s in range(spp)], np.int32)
 
 
+def opencv_cornell(width=48, height=40):
+    """The Cornell box through an "opencv" camera at the virtual camera's
+    place: camera x right, y down, z forward (the world's -z), principal
+    point off-centre, fx = fy for the same vertical field of view."""
+    sc = scenes.cornell(width=width, height=height)
+    f = 0.5 * height / np.tan(np.radians(39.3) / 2)
+    ext = np.array([[1, 0, 0, 0], [0, -1, 0, 0], [0, 0, -1, 3.9], [0, 0, 0, 1]], np.float64)
+    sc.camera = scenes.Camera(width=width, height=height, type=abi.DL_CAMERA_OPENCV, fx=f, fy=f,
+                              cx=0.5 * width + 1.5, cy=0.5 * height - 2.0, transform=ext)
+    return sc
+
+
 LI_CASES = {
     "cornell": (lambda: scenes.cornell(width=48, height=48), dict(max_depth=0)),
     "cornell_d8": (lambda: scenes.cornell(width=48, height=48), dict(max_depth=8)),
@@ -58,6 +70,12 @@ LI_CASES = {
                          dict(max_depth=8, flags=abi.DL_RENDER_POWER_LIGHT_PICK)),
     "env_spheres_power": (lambda: scenes.env_spheres(width=64, height=40),
                           dict(max_depth=8, flags=abi.DL_RENDER_POWER_LIGHT_PICK)),
+    "perspective": (lambda: mg.perspective_scene(48, 40), dict(max_depth=8)),
+    "perspective_normals": (lambda: mg.perspective_scene(48, 40), dict(flags=abi.DL_RENDER_NORMALS)),
+    "opencv": (lambda: opencv_cornell(), dict(max_depth=8)),
+    "spheres_normals": (lambda: scenes.material_spheres(width=96, height=54, num_spheres=16, level=3),
+                        dict(flags=abi.DL_RENDER_NORMALS)),
+    "env_normals": (lambda: scenes.env_spheres(width=64, height=40), dict(flags=abi.DL_RENDER_NORMALS)),
 }
 
 
@@ -88,6 +106,29 @@ def test_li_matches_reference_golden(ctx, name):
     L, pos = gs.li(abi.make_opts(seed=int(g["seed"])), g["xys"])
     np.testing.assert_array_equal(pos, g["pos"])
     assert path_close(L, g["L"]).mean() >= MIN_CLOSE
+
+
+def test_perspective_normals_match_reference_golden(ctx):
+    """The "perspective" camera and "normals" integrator against the
+    reference's own outputs (tests/golden/perspective_normals.npz)."""
+    g = np.load(os.path.join(GOLDEN, "perspective_normals.npz"))
+    gs = api.Scene.from_data(ctx, mg.perspective_scene())
+    L, pos = gs.li(abi.make_opts(seed=int(g["seed"]), flags=abi.DL_RENDER_NORMALS), g["xys"])
+    np.testing.assert_array_equal(pos, g["pos"])
+    assert path_close(L, g["L"]).mean() >= 0.995
+
+
+def test_normals_render_matches_oracle(ctx):
+    """A normals image (dl_render, Gaussian film) of the perspective view
+    equals the oracle's per-path render to float summation order."""
+    sc = mg.perspective_scene(64, 48)
+    gs = api.Scene.from_data(ctx, sc)
+    orc = po.OracleScene(sc)
+    opts = abi.make_opts(spp=4, seed=9, flags=abi.DL_RENDER_NORMALS)
+    rg = gs.render(opts)
+    ro, _ = orc.render_paths(opts)
+    np.testing.assert_allclose(rg, ro, rtol=1e-4, atol=1e-5)
+    assert rg.max() <= 1.0 + 1e-5 and rg.mean() > 0.1
 
 
 def test_film_matches_oracle_per_path_render(ctx):

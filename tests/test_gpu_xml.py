@@ -127,7 +127,7 @@ def test_missing_file_is_io_error(ctx, tmp_path):
 
 def test_unsupported_plugin_is_reported(ctx, tmp_path):
     p = tmp_path / "u.xml"
-    p.write_text("<scene><integrator type='normals'/></scene>")
+    p.write_text("<scene><integrator type='photonmapper'/></scene>")
     with pytest.raises(api.DrawlabError) as e:
         api.Scene.from_xml(ctx, str(p))
     assert e.value.status == abi.DL_ERR_UNSUPPORTED
@@ -179,3 +179,65 @@ def test_xml_envmap_bad_image(ctx, tmp_path):
     with pytest.raises(api.DrawlabError) as e:
         api.Scene.from_xml(ctx, str(tmp_path / "t.xml"))
     assert e.value.status == abi.DL_ERR_UNSUPPORTED
+
+
+def matrix_xml(m):
+    return '<matrix value="%s"/>' % ", ".join("%.9g" % float(x) for x in np.asarray(m, np.float32).reshape(16))
+
+
+@pytest.mark.parametrize("kind", ["perspective", "opencv"])
+def test_xml_cameras_and_normals_integrator(ctx, tmp_path, kind):
+    """<camera type="perspective"> (toWorld, fov, clip planes) and
+    <camera type="opencv"> (fx, fy, cx, cy, extrinsic) with
+    <integrator type="normals">: the same paths as the scene built from
+    arrays; the integrator lands in the scene's default options."""
+    arr, (P, F, N) = arrays_equivalent()
+    W, H = arr.camera.width, arr.camera.height
+    if kind == "perspective":
+        m = scenes.look_at((0.3, 0.2, 3.6), (0.0, -0.1, 0.0), (0.0, 1.0, 0.0)).astype(np.float32)
+        cam_xml = ['  <camera type="perspective">', '    <float name="fov" value="50"/>',
+                   '    <float name="farClip" value="100"/>',
+                   '    <transform name="toWorld">', "      " + matrix_xml(m), "    </transform>"]
+        arr.camera = scenes.Camera(width=W, height=H, type=abi.DL_CAMERA_PERSPECTIVE, fov=50.0,
+                                   far_clip=100.0, transform=m)
+    else:
+        m = np.array([[1, 0, 0, 0.1], [0, -1, 0, 0.05], [0, 0, -1, 3.9], [0, 0, 0, 1]], np.float32)
+        cam_xml = ['  <camera type="opencv">', '    <float name="fx" value="44"/>',
+                   '    <float name="fy" value="46"/>', '    <float name="cx" value="21"/>',
+                   '    <float name="cy" value="15.5"/>',
+                   '    <transform name="extrinsic">', "      " + matrix_xml(m), "    </transform>"]
+        arr.camera = scenes.Camera(width=W, height=H, type=abi.DL_CAMERA_OPENCV, fx=44.0, fy=46.0, cx=21.0,
+                                   cy=15.5, transform=m)
+    cam_xml += ['    <integer name="width" value="%d"/>' % W, '    <integer name="height" value="%d"/>' % H,
+                "  </camera>"]
+    text = cornell_xml(arr, "cuboid.obj").replace('<integrator type="path"/>', '<integrator type="normals"/>')
+    lines = text.split("\n")
+    a = next(i for i, x in enumerate(lines) if x.strip().startswith('<camera type="virtual">'))
+    b = next(i for i, x in enumerate(lines) if x.strip() == "</camera>")
+    lines[a:b + 1] = cam_xml
+    write_obj(tmp_path / "cuboid.obj", P, F, N)
+    (tmp_path / "scene.xml").write_text("\n".join(lines))
+    gx = api.Scene.from_xml(ctx, str(tmp_path / "scene.xml"))
+    ga = api.Scene.from_data(ctx, arr)
+    d = gx.default_opts()
+    assert d.flags & abi.DL_RENDER_NORMALS
+    xys = np.array([(x, y, s) for y in range(H) for x in range(W) for s in range(2)], np.int32)
+    La, pa = gx.li(d, xys)
+    Lb, pb = ga.li(d, xys)
+    np.testing.assert_array_equal(pa, pb)
+    np.testing.assert_array_equal(La, Lb)
+    assert (La.sum(1) > 0).mean() > 0.5
+
+
+def test_xml_camera_errors(ctx, tmp_path):
+    base = ("<scene><integrator type='path'/><camera type='%s'>%s</camera></scene>")
+    cases = [("opencv", "<float name='fx' value='1'/><float name='fy' value='1'/><float name='cx' value='0'/>"
+                        "<float name='cy' value='0'/>", abi.DL_ERR_PARSE),            # no extrinsic
+             ("perspective", "<float name='nearClip' value='0.5'/>", abi.DL_ERR_INVALID_ARG),
+             ("orthographic", "", abi.DL_ERR_UNSUPPORTED)]
+    for k, (typ, body, status) in enumerate(cases):
+        p = tmp_path / ("c%d.xml" % k)
+        p.write_text(base % (typ, body))
+        with pytest.raises(api.DrawlabError) as e:
+            api.Scene.from_xml(ctx, str(p))
+        assert e.value.status == status, (typ, e.value)

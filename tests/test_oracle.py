@@ -142,3 +142,41 @@ def test_live_li_matches_reference_multithreaded():
     L2, p2 = ref.li(123, xys)
     np.testing.assert_array_equal(p1, p2)
     np.testing.assert_array_equal(L1, L2)
+
+
+def test_perspective_camera_and_normals_integrator_match_reference_golden():
+    """The "perspective" camera and the "normals" integrator against the
+    reference's own PerspectiveCamera::sampleRay and NormalIntegrator::Li
+    (tests/golden/perspective_normals.npz).  The film positions (pcg32) are
+    bit-exact.  The oracle composes and inverts the projection in double
+    where the reference does it in float, so ray directions may differ in
+    the last bits: the normals agree to 1e-4 except on the rare rays that
+    graze a triangle edge."""
+    g = _golden("perspective_normals.npz")
+    sc = mg.perspective_scene()
+    orc = po.OracleScene(sc)
+    L, pos = orc.li(abi.make_opts(seed=int(g["seed"]), flags=abi.DL_RENDER_NORMALS), g["xys"])
+    np.testing.assert_array_equal(pos, g["pos"])
+    close = np.all(np.abs(L - g["L"]) <= 1e-4, axis=1)
+    assert close.mean() > 0.995, close.mean()
+    hit_o, hit_r = L.sum(1) > 0, g["L"].sum(1) > 0
+    assert (hit_o == hit_r).mean() > 0.995
+    assert hit_r.sum() > 1000
+
+
+def test_opencv_camera_rays_follow_the_intrinsics():
+    """The "opencv" camera (no CPU form in the reference; rays as
+    include/optix/camera/opencv.h): with the identity extrinsic, the ray
+    through film position (x, y) points along ((x - cx) / fx, (y - cy) / fy, 1)
+    from the origin.  Checked through the normals integrator on a plane at
+    z = 2 facing -z: every pixel sees it, normal (0, 0, 1)."""
+    sc = scenes.SceneData(name="plane")
+    pos, idx, nrm = scenes.rectangle((-50.0, -50.0, 2.0), (100.0, 0.0, 0.0), (0.0, 100.0, 0.0))
+    m = sc.add_material(scenes.Material())
+    sc.add_mesh(scenes.Mesh(positions=pos, indices=idx, normals=nrm, material=m))
+    sc.camera = scenes.Camera(width=40, height=30, type=abi.DL_CAMERA_OPENCV, fx=30.0, fy=30.0, cx=20.0,
+                              cy=15.0, transform=np.eye(4))
+    orc = po.OracleScene(sc)
+    xys = np.array([(x, y, 0) for y in range(30) for x in range(40)], np.int32)
+    L, _ = orc.li(abi.make_opts(seed=1, flags=abi.DL_RENDER_NORMALS), xys)
+    np.testing.assert_allclose(L, np.tile([0.0, 0.0, 1.0], (len(L), 1)), atol=1e-6)
