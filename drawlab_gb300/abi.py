@@ -46,6 +46,10 @@ DL_CAMERA_OPENCV = 2
 DL_FILTER_GAUSSIAN = 0
 DL_FILTER_BOX = 1
 
+DL_IMAGE_PNG = 0
+DL_IMAGE_EXR = 1
+DL_IMAGE_PFM = 2
+
 DL_RENDER_FIX_POINT_LIGHT = 1 << 0
 DL_RENDER_POWER_LIGHT_PICK = 1 << 1
 DL_RENDER_NORMALS = 1 << 2

@@ -40,6 +40,7 @@ SIGNATURES = {
     "dl_render": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film_device": (C.c_int, [_vp, _vp, _vp]),
+    "dl_image_write": (C.c_int, [C.c_char_p, _i32, _i32, _vp, _i32]),
     "dl_li": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "dl_stats_get": (C.c_int, [_vp, _vp]),
     "dl_render_traversal_counts": (C.c_int, [_vp, _vp, _vp]),
@@ -59,6 +60,25 @@ SIGNATURES = {
     "dl_guide_train": (C.c_int, [_vp, _i64, _vp, _i32, _vp]),
     "dl_render_guided": (C.c_int, [_vp, _vp, _vp, _i32, _vp]),
 }
+
+
+def write_image(path, rgb, fmt: int | None = None) -> None:
+    """Write a (height, width, 3) float image (row 0 = top) as PNG, OpenEXR
+    or PFM; the format follows the file extension unless `fmt` is given.
+    Needs no GPU."""
+    p = str(path)
+    if fmt is None:
+        ext = p.rsplit(".", 1)[-1].lower()
+        fmt = {"png": abi.DL_IMAGE_PNG, "exr": abi.DL_IMAGE_EXR, "pfm": abi.DL_IMAGE_PFM}.get(ext)
+        if fmt is None:
+            raise ValueError("unknown image extension: %s" % p)
+    a = np.ascontiguousarray(rgb, np.float32)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("expected a (height, width, 3) image")
+    L = lib()
+    rc = L.dl_image_write(p.encode(), a.shape[1], a.shape[0], a.ctypes.data_as(C.c_void_p), fmt)
+    if rc != abi.DL_OK:
+        raise DrawlabError(rc, L.dl_last_error(None).decode())
 
 
 class DrawlabError(RuntimeError):

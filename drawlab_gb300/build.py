@@ -32,7 +32,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
              "-I", str(CUDA_HOME / "include")]
 
 CU_SOURCES = ["trace.cu", "render.cu", "noalloc.cu", "guide.cu"]
-CPP_SOURCES = ["api.cpp", "bvh.cpp", "scene.cpp", "xml.cpp"]
+CPP_SOURCES = ["api.cpp", "bvh.cpp", "image.cpp", "scene.cpp", "xml.cpp"]
 
 
 def _headers():

@@ -64,6 +64,11 @@ int dl_abi_version(void) { return DL_ABI_VERSION; }
 
 const char* dl_last_error(const dl_context* ctx) { return ctx ? ctx->error.c_str() : g_create_error.c_str(); }
 
+int dl_image_write(const char* path, int32_t width, int32_t height, const float* rgb, int32_t format) {
+    g_create_error.clear();
+    return guard(nullptr, [&] { dl::write_image(path, width, height, rgb, format); });
+}
+
 int dl_context_create(int device, dl_context** out) {
     g_create_error.clear();
     if (!out) {

@@ -43,6 +43,9 @@ void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n);
 // Guided progressive render into d_film (render.cu).
 void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_film, bool train);
 
+// Image output (image.cpp); throws dl::Error.
+void write_image(const char* path, int width, int height, const float* rgb, int format);
+
 // XML scene loading (xml.cpp): fills arrays and default render options.
 struct XmlScene;
 int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out);

@@ -266,6 +266,23 @@ int dl_render_film(dl_scene* scene, const dl_render_opts* opts, float* film_out)
  * context stream; the call returns without synchronising. */
 int dl_render_film_device(dl_scene* scene, const dl_render_opts* opts, float* d_film);
 
+/* --------------------------------------------------------------- images */
+
+enum dl_image_format {
+    DL_IMAGE_PNG = 0,  /* Bitmap::savePNG (src/core/bitmap/bitmap.cpp:190-214): sRGB
+                          (Color3f::toSRGB, include/core/bitmap/color.h:76-87), x255,
+                          clamped to [0, 255], truncated to 8 bits */
+    DL_IMAGE_EXR = 1,  /* Bitmap::saveEXR (bitmap.cpp:157-188): float R, G, B; written
+                          uncompressed */
+    DL_IMAGE_PFM = 2   /* linear floats, little endian, rows bottom to top */
+};
+
+/* Write an RGB image (height x width x 3 floats, row 0 = top, as dl_render
+ * returns it) to `path` (the full file name; the reference appends ".png" /
+ * ".exr" itself).  Host only: needs no context or GPU.  Messages of failed
+ * calls: dl_last_error(NULL). */
+int dl_image_write(const char* path, int32_t width, int32_t height, const float* rgb, int32_t format);
+
 /* Radiance of individual camera paths, the reference's
  * Integrator::Li(scene, sampler, ray) (include/tracer/integrator.h:38) for
  * the paths (x, y, s) given as n triples: pixel x, pixel y, sample index s.

@@ -241,3 +241,21 @@ def test_xml_camera_errors(ctx, tmp_path):
         with pytest.raises(api.DrawlabError) as e:
             api.Scene.from_xml(ctx, str(p))
         assert e.value.status == status, (typ, e.value)
+
+
+def test_command_line_renders_xml_to_exr_and_png(ctx, tmp_path):
+    """python -m drawlab_gb300 scene.xml writes scene.exr and scene.png next
+    to the file (the reference's output naming); the EXR holds the render."""
+    import test_image_io as io
+    from drawlab_gb300 import __main__ as cli
+
+    arr, (P, F, N) = arrays_equivalent()
+    write_obj(tmp_path / "cuboid.obj", P, F, N)
+    (tmp_path / "scene.xml").write_text(cornell_xml(arr, str(tmp_path / "cuboid.obj")))
+    assert cli.main([str(tmp_path / "scene.xml"), "--spp", "4", "--seed", "2"]) == 0
+    img = io.read_exr(tmp_path / "scene.exr")
+    gx = api.Scene.from_xml(ctx, str(tmp_path / "scene.xml"))
+    o = gx.default_opts()
+    o.spp, o.seed = 4, 2
+    np.testing.assert_array_equal(img, gx.render(o))
+    assert io.read_png(tmp_path / "scene.png").shape == img.shape
