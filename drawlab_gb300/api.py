@@ -41,6 +41,7 @@ SIGNATURES = {
     "dl_render_film": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film_device": (C.c_int, [_vp, _vp, _vp]),
     "dl_image_write": (C.c_int, [C.c_char_p, _i32, _i32, _vp, _i32]),
+    "dl_image_read": (C.c_int, [C.c_char_p, _vp, _vp, _vp, _i64]),
     "dl_li": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp]),
     "dl_stats_get": (C.c_int, [_vp, _vp]),
     "dl_render_traversal_counts": (C.c_int, [_vp, _vp, _vp]),
@@ -79,6 +80,22 @@ def write_image(path, rgb, fmt: int | None = None) -> None:
     rc = L.dl_image_write(p.encode(), a.shape[1], a.shape[0], a.ctypes.data_as(C.c_void_p), fmt)
     if rc != abi.DL_OK:
         raise DrawlabError(rc, L.dl_last_error(None).decode())
+
+
+def read_image(path) -> np.ndarray:
+    """Read a PNG or PFM image as a (height, width, 3) float32 array (row 0 =
+    top; PNG values are bytes / 255).  Needs no GPU."""
+    L = lib()
+    w, h = C.c_int32(), C.c_int32()
+    p = str(path).encode()
+    rc = L.dl_image_read(p, C.byref(w), C.byref(h), None, 0)
+    if rc != abi.DL_OK:
+        raise DrawlabError(rc, L.dl_last_error(None).decode())
+    out = np.empty((h.value, w.value, 3), np.float32)
+    rc = L.dl_image_read(p, C.byref(w), C.byref(h), out.ctypes.data_as(C.c_void_p), out.size)
+    if rc != abi.DL_OK:
+        raise DrawlabError(rc, L.dl_last_error(None).decode())
+    return out
 
 
 class DrawlabError(RuntimeError):

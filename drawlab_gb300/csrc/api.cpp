@@ -69,6 +69,22 @@ int dl_image_write(const char* path, int32_t width, int32_t height, const float*
     return guard(nullptr, [&] { dl::write_image(path, width, height, rgb, format); });
 }
 
+int dl_image_read(const char* path, int32_t* width, int32_t* height, float* rgb, int64_t capacity) {
+    g_create_error.clear();
+    return guard(nullptr, [&] {
+        need(path != nullptr && width != nullptr && height != nullptr, "path/width/height is NULL");
+        int w = 0, h = 0;
+        bool is_float = false;
+        std::vector<float> img = dl::read_image(path, w, h, is_float);
+        *width = w;
+        *height = h;
+        if (rgb) {
+            need(capacity >= (int64_t)img.size(), "rgb buffer too small");
+            std::memcpy(rgb, img.data(), img.size() * sizeof(float));
+        }
+    });
+}
+
 int dl_context_create(int device, dl_context** out) {
     g_create_error.clear();
     if (!out) {

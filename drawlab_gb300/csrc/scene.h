@@ -43,8 +43,12 @@ void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n);
 // Guided progressive render into d_film (render.cu).
 void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_film, bool train);
 
-// Image output (image.cpp); throws dl::Error.
+// Images (image.cpp); all throw dl::Error.  Readers return RGB floats, row 0
+// = the image's top row; PNG values are bytes / 255 (is_float false), PFM
+// values as stored (is_float true).
 void write_image(const char* path, int width, int height, const float* rgb, int format);
+std::vector<float> load_pfm(const std::string& path, int& w, int& h);
+std::vector<float> read_image(const std::string& path, int& w, int& h, bool& is_float);
 
 // XML scene loading (xml.cpp): fills arrays and default render options.
 struct XmlScene;

@@ -512,41 +512,6 @@ void apply_transform(MeshData& m, const M4& T) {
     }
 }
 
-// Portable float map (PF: RGB, Pf: grey), rows stored bottom to top, scale
-// sign = byte order.  Returns rows top to bottom, RGB.  The reference reads
-// envmaps through its Bitmap class (EXR via OpenEXR, LDR/HDR via stb_image,
-// src/core/bitmap/bitmap.cpp:30-140); this build reads PFM.
-std::vector<float> load_pfm(const std::string& path, int& w, int& h) {
-    std::ifstream in(path, std::ios::binary);
-    if (!in) throw Error(DL_ERR_IO, "cannot open image \"" + path + "\"");
-    std::string magic;
-    double scale = 0;
-    in >> magic >> w >> h >> scale;
-    if (!in || (magic != "PF" && magic != "Pf") || w <= 0 || h <= 0 || (int64_t)w * h > ((int64_t)1 << 26) ||
-        scale == 0)
-        throw Error(DL_ERR_PARSE, "\"" + path + "\": not a PFM image");
-    in.get();  // the single whitespace byte before the raster
-    const int ch = magic == "PF" ? 3 : 1;
-    std::vector<float> raw((size_t)w * h * ch);
-    in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * 4));
-    if (!in) throw Error(DL_ERR_PARSE, "\"" + path + "\": truncated PFM raster");
-    const uint16_t probe = 1;
-    const bool host_le = *reinterpret_cast<const uint8_t*>(&probe) == 1;
-    if ((scale < 0) != host_le) {
-        for (float& v : raw) {
-            uint8_t* b = reinterpret_cast<uint8_t*>(&v);
-            std::swap(b[0], b[3]);
-            std::swap(b[1], b[2]);
-        }
-    }
-    std::vector<float> rgb((size_t)w * h * 3);
-    for (int y = 0; y < h; y++)
-        for (int x = 0; x < w; x++)
-            for (int c = 0; c < 3; c++)
-                rgb[3 * ((size_t)y * w + x) + c] = raw[ch * ((size_t)(h - 1 - y) * w + x) + (ch == 3 ? c : 0)];
-    return rgb;
-}
-
 // Wavefront OBJ: one vertex per distinct (position, texcoord, normal) index
 // triple in order of first use, faces fan-triangulated (the layout
 // tinyobjloader gives src/tracer/mesh/obj.cpp).

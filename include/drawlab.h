@@ -283,6 +283,14 @@ enum dl_image_format {
  * calls: dl_last_error(NULL). */
 int dl_image_write(const char* path, int32_t width, int32_t height, const float* rgb, int32_t format);
 
+/* Read a PNG (8-bit grey / grey + alpha / RGB / RGBA / palette, not
+ * interlaced; values = bytes / 255, alpha dropped) or PFM image as RGB
+ * floats, row 0 = the image's top row.  With rgb NULL only width and height
+ * are returned; then call again with capacity >= width * height * 3.  The
+ * reference reads bitmaps with stb_image / OpenEXR
+ * (src/core/bitmap/bitmap.cpp:33-152); host only. */
+int dl_image_read(const char* path, int32_t* width, int32_t* height, float* rgb, int64_t capacity);
+
 /* Radiance of individual camera paths, the reference's
  * Integrator::Li(scene, sampler, ray) (include/tracer/integrator.h:38) for
  * the paths (x, y, s) given as n triples: pixel x, pixel y, sample index s.

@@ -130,3 +130,85 @@ def test_image_write_errors(tmp_path):
     with pytest.raises(api.DrawlabError) as e:
         api.write_image(tmp_path / "a.png", img, fmt=7)
     assert e.value.status == abi.DL_ERR_INVALID_ARG
+
+
+# ------------------------------------------------------------ reading
+def png_bytes(pixels, ctype, filters, palette=None, level=9):
+    """A PNG made here (Python's zlib: dynamic / fixed Huffman blocks) with
+    the given per-row filter types applied to `pixels` (h, w, channels uint8)."""
+    h, w = pixels.shape[:2]
+    ch = pixels.shape[2]
+    raw = bytearray()
+    prev = np.zeros(w * ch, np.int32)
+    for y in range(h):
+        cur = pixels[y].reshape(-1).astype(np.int32)
+        f = filters[y % len(filters)]
+        out = np.empty_like(cur)
+        for i in range(len(cur)):
+            a = cur[i - ch] if i >= ch else 0
+            b = prev[i]
+            c = prev[i - ch] if i >= ch else 0
+            if f == 0:
+                pred = 0
+            elif f == 1:
+                pred = a
+            elif f == 2:
+                pred = b
+            elif f == 3:
+                pred = (a + b) >> 1
+            else:
+                p = a + b - c
+                pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            out[i] = (cur[i] - pred) & 0xFF
+        raw += bytes([f]) + out.astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(t, body):
+        return struct.pack(">I", len(body)) + t + body + struct.pack(">I", zlib.crc32(t + body) & 0xFFFFFFFF)
+
+    data = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0))
+    if palette is not None:
+        data += chunk(b"PLTE", palette.astype(np.uint8).tobytes())
+    z = zlib.compress(bytes(raw), level)
+    data += chunk(b"IDAT", z[: len(z) // 2]) + chunk(b"IDAT", z[len(z) // 2:])   # split over two chunks
+    return data + chunk(b"IEND", b"")
+
+
+@pytest.mark.parametrize("ctype,ch", [(2, 3), (6, 4), (0, 1), (4, 2)])
+def test_png_reader_decodes_every_filter(tmp_path, ctype, ch):
+    rng = np.random.default_rng(ctype)
+    h, w = 23, 31
+    px = rng.integers(0, 256, (h, w, ch)).astype(np.uint8)
+    px[5:15, 3:20] = 200                     # runs: back-references in the deflate stream
+    for level in (0, 1, 9):                  # stored, fixed and dynamic Huffman blocks
+        p = tmp_path / ("t%d_%d.png" % (ctype, level))
+        p.write_bytes(png_bytes(px, ctype, [0, 1, 2, 3, 4], level=level))
+        img = api.read_image(p)
+        want = px[..., :3] if ch >= 3 else np.repeat(px[..., :1], 3, axis=2)
+        np.testing.assert_array_equal(img, want.astype(np.float32) / np.float32(255))
+
+
+def test_png_reader_palette_and_own_writer(tmp_path):
+    rng = np.random.default_rng(4)
+    pal = rng.integers(0, 256, (16, 3))
+    idx = rng.integers(0, 16, (9, 12, 1)).astype(np.uint8)
+    (tmp_path / "p.png").write_bytes(png_bytes(idx, 3, [4, 2], palette=pal))
+    np.testing.assert_array_equal(api.read_image(tmp_path / "p.png"), pal[idx[..., 0]].astype(np.float32) / 255)
+    img = sample_image()
+    api.write_image(tmp_path / "own.png", img)
+    np.testing.assert_array_equal(api.read_image(tmp_path / "own.png"),
+                                  expected_png_bytes(img).astype(np.float32) / np.float32(255))
+
+
+def test_pfm_reader_round_trip_and_errors(tmp_path):
+    img = sample_image()
+    api.write_image(tmp_path / "a.pfm", img)
+    np.testing.assert_array_equal(api.read_image(tmp_path / "a.pfm"), img)
+    (tmp_path / "bad.png").write_bytes(b"\x89PNG\r\n\x1a\n" + b"\0" * 20)
+    with pytest.raises(api.DrawlabError) as e:
+        api.read_image(tmp_path / "bad.png")
+    assert e.value.status == abi.DL_ERR_PARSE
+    with pytest.raises(api.DrawlabError) as e:
+        api.read_image(tmp_path / "a.jpg")
+    assert e.value.status == abi.DL_ERR_UNSUPPORTED
