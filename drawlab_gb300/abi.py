@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 6
+DL_ABI_VERSION = 7
 
 # status
 DL_OK = 0
@@ -68,6 +68,14 @@ class dl_mesh_desc(C.Structure):
     ]
 
 
+class dl_texture_desc(C.Structure):
+    _fields_ = [
+        ("rgb", C.POINTER(C.c_float)),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+    ]
+
+
 class dl_material_desc(C.Structure):
     _fields_ = [
         ("type", C.c_int32),
@@ -76,6 +84,11 @@ class dl_material_desc(C.Structure):
         ("alpha", C.c_float * 2),
         ("int_ior", C.c_float),
         ("ext_ior", C.c_float),
+        ("albedo_texture", dl_texture_desc),
+        ("specular_texture", dl_texture_desc),
+        ("alpha_texture", dl_texture_desc),
+        ("normal_texture", dl_texture_desc),
+        ("tangent_texture", dl_texture_desc),
     ]
 
 

@@ -286,6 +286,16 @@ __device__ __forceinline__ Frame make_onb(float3 n) {
     f.t = cross(f.b, n);
     return f;
 }
+// Onb(normal, tangent) with a given (non-zero) tangent (onb.h:29-32): the
+// tangent as given, binormal = normalize(n x t).
+__device__ __forceinline__ Frame make_onb_t(float3 n, float3 t) {
+    if (t.x == 0.f && t.y == 0.f && t.z == 0.f) return make_onb(n);
+    Frame f;
+    f.n = n;
+    f.t = t;
+    f.b = normalize(cross(n, t));
+    return f;
+}
 __device__ __forceinline__ float3 to_local(const Frame& f, float3 v) {
     return f3(dot(v, f.t), dot(v, f.b), dot(f.n, v));
 }
@@ -551,9 +561,11 @@ __device__ __forceinline__ float mis_weight(float a, float b) {
 // fp32 weights.
 constexpr float kHalfInvPiF = (float)(0.5 / (double)kPiF);  // (float)(0.5 / M_PIf)
 
-__device__ __forceinline__ float3 env_lookup(const DevScene& sc, float u, float v) {
-    const int W = sc.env_w, H = sc.env_h;
-    if (!isfinite(u) || !isfinite(v)) return f3(0.f, 0.f, 0.f);  // no direction
+// Bilinear, wrap-addressed lookup at normalised coordinates (u, v) of a
+// W x H texel array (the filtering of a CUDA texture with linear filtering
+// and wrap addressing, restated with fp32 weights).
+__device__ __forceinline__ float3 tex_bilinear(const float4* tex, int W, int H, float u, float v) {
+    if (!isfinite(u) || !isfinite(v)) return f3(0.f, 0.f, 0.f);
     u = __fsub_rn(u, floorf(u));
     v = __fsub_rn(v, floorf(v));
     float x = __fsub_rn(__fmul_rn(u, (float)W), 0.5f);
@@ -566,15 +578,33 @@ __device__ __forceinline__ float3 env_lookup(const DevScene& sc, float u, float 
     y0 = y0 < 0 ? y0 + H : y0;
     x1 = x1 >= W ? x1 - W : x1;
     y1 = y1 >= H ? y1 - H : y1;
-    float3 t00 = xyz(__ldg(sc.env_tex + (size_t)y0 * W + x0));
-    float3 t10 = xyz(__ldg(sc.env_tex + (size_t)y0 * W + x1));
-    float3 t01 = xyz(__ldg(sc.env_tex + (size_t)y1 * W + x0));
-    float3 t11 = xyz(__ldg(sc.env_tex + (size_t)y1 * W + x1));
+    float3 t00 = xyz(__ldg(tex + (size_t)y0 * W + x0));
+    float3 t10 = xyz(__ldg(tex + (size_t)y0 * W + x1));
+    float3 t01 = xyz(__ldg(tex + (size_t)y1 * W + x0));
+    float3 t11 = xyz(__ldg(tex + (size_t)y1 * W + x1));
     float bx = __fsub_rn(1.f, ax), by = __fsub_rn(1.f, ay);
-    float3 r = add(add(add(scale(t00, __fmul_rn(bx, by)), scale(t10, __fmul_rn(ax, by))),
-                       scale(t01, __fmul_rn(bx, ay))),
-                   scale(t11, __fmul_rn(ax, ay)));
-    return scale(r, sc.env_scale);
+    return add(add(add(scale(t00, __fmul_rn(bx, by)), scale(t10, __fmul_rn(ax, by))), scale(t01, __fmul_rn(bx, ay))),
+               scale(t11, __fmul_rn(ax, ay)));
+}
+
+__device__ __forceinline__ float3 tex_lookup(const DevScene& sc, int t, float2 uv) {
+    const DevTexture tx = sc.textures[t];
+    return tex_bilinear(tx.texels, tx.w, tx.h, uv.x, uv.y);
+}
+
+// Interpolated texture coordinates of a hit (shader_common.h:38-45:
+// (1 - u - v) t0 + u t1 + v t2; (0, 0) for a mesh without them).
+__device__ __forceinline__ float2 hit_texcoord(const DevScene& sc, int tri, float u, float v) {
+    const int4 vi = __ldg(sc.tri_vidx + tri);
+    if (!sc.meshes[vi.w].has_texcoords) return make_float2(0.f, 0.f);
+    const float2 t0 = __ldg(sc.texcoords + vi.x), t1 = __ldg(sc.texcoords + vi.y), t2 = __ldg(sc.texcoords + vi.z);
+    const float b0 = __fsub_rn(__fsub_rn(1.f, u), v);
+    return make_float2(__fadd_rn(__fadd_rn(__fmul_rn(b0, t0.x), __fmul_rn(u, t1.x)), __fmul_rn(v, t2.x)),
+                       __fadd_rn(__fadd_rn(__fmul_rn(b0, t0.y), __fmul_rn(u, t1.y)), __fmul_rn(v, t2.y)));
+}
+
+__device__ __forceinline__ float3 env_lookup(const DevScene& sc, float u, float v) {
+    return scale(tex_bilinear(sc.env_tex, sc.env_w, sc.env_h, u, v), sc.env_scale);
 }
 
 // Envmap::environment_coords (envmap.h:26-30)

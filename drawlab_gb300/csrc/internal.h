@@ -219,6 +219,7 @@ struct dl_scene {
     dl::DevScene dev{};
     dl::DevBuf nodes, tris, tri_vidx, normals, meshes, materials, lights, emit_tris, emit_cdf;
     dl::DevBuf env_tex, env_accel, light_pick;
+    dl::DevBuf texels, textures, texcoords;   // bitmap textures, their table, per-vertex texcoords
     std::vector<int32_t> tri_order;   // leaf-order triangle -> original id
     dl_scene_info info{};
     dl_render_opts defaults{};

@@ -17,6 +17,9 @@ constexpr float kInvTwoPiF = 0.15915494309189533577f;
 enum MatType { MAT_DIFFUSE = 0, MAT_MIRROR = 1, MAT_DIELECTRIC = 2, MAT_MICROFACET = 3, MAT_ANISO_GGX = 4 };
 enum LightType { LIGHT_AREA = 0, LIGHT_POINT = 1, LIGHT_ENVMAP = 2 };
 
+// texture slots of a material (dl_material_desc's *_texture fields)
+enum TexSlot { TEX_ALBEDO = 0, TEX_SPECULAR = 1, TEX_ALPHA = 2, TEX_NORMAL = 3, TEX_TANGENT = 4, kTexSlots = 5 };
+
 struct DevMaterial {
     int type;
     float albedo[3];
@@ -24,13 +27,20 @@ struct DevMaterial {
     float ax, ay;
     float int_ior, ext_ior;
     float ks;          // microfacet: 1 - max(kd)
+    int tex[kTexSlots];  // texture index per slot, -1 = none
+    int has_tex;         // any slot set
+};
+
+struct DevTexture {
+    const float4* texels;  // rgb + pad, row k at t = (k + 0.5) / h
+    int w, h;
 };
 
 struct DevMesh {
     int material;
     int light;         // emitter index or -1
     int has_normals;
-    int pad;
+    int has_texcoords;
 };
 
 struct DevLight {
@@ -66,6 +76,8 @@ struct DevScene {
     const DevLight* __restrict__ lights;
     const float4* __restrict__ emit_tris;
     const float* __restrict__ emit_cdf;
+    const DevTexture* __restrict__ textures;
+    const float2* __restrict__ texcoords;  // per vertex (global index)
     int num_tris;
     int num_lights;
     DevCamera cam;

@@ -795,6 +795,8 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
         Pcg32 g;
         HitInfo h;
         GuideRec gr;
+        float2 tuv = make_float2(0.f, 0.f);  // texture coordinates (textured materials)
+        float3 s_tan = f3(0.f, 0.f, 0.f);    // aniso_ggx: shading tangent from a tangent map
         float3 tp = f3(0.f, 0.f, 0.f), Lr = tp, dir = tp;
         float eta = 1.f;
         int depth = 0, flags = 0, rid = 0;
@@ -817,6 +819,24 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             const DevRequest& R = request<kMulti>(P, rid);
             const DevScene& sc = R.sc;
             h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
+            if (T == MAT_DIFFUSE || T == MAT_ANISO_GGX) {
+                const DevMaterial& mt = sc.materials[sc.meshes[h.mesh].material];
+                if (mt.has_tex) {
+                    tuv = hit_texcoord(sc, __float_as_int(hit.w), hit.y, hit.z);
+                    // world-space normal / tangent maps (shader_common.h:62-64,
+                    // 104-107): normalize(2 rgb - 1) replaces the shading normal
+                    if (T == MAT_ANISO_GGX && mt.tex[TEX_NORMAL] >= 0) {
+                        const float3 c = tex_lookup(sc, mt.tex[TEX_NORMAL], tuv);
+                        h.sh.n = normalize(f3(__fsub_rn(__fmul_rn(c.x, 2.f), 1.f), __fsub_rn(__fmul_rn(c.y, 2.f), 1.f),
+                                              __fsub_rn(__fmul_rn(c.z, 2.f), 1.f)));
+                    }
+                    if (T == MAT_ANISO_GGX && mt.tex[TEX_TANGENT] >= 0) {
+                        const float3 c = tex_lookup(sc, mt.tex[TEX_TANGENT], tuv);
+                        s_tan = normalize(f3(__fsub_rn(__fmul_rn(c.x, 2.f), 1.f), __fsub_rn(__fmul_rn(c.y, 2.f), 1.f),
+                                             __fsub_rn(__fmul_rn(c.z, 2.f), 1.f)));
+                    }
+                }
+            }
             int light = sc.meshes[h.mesh].light;
             if (R.flags & DL_RENDER_NORMALS) {
                 // the normals integrator (normal.cpp:10-20): |shading normal|
@@ -877,8 +897,29 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
             float prev_pdf = pr.L.w;
             int target = slot;
             if (!done) {
-                const DevMaterial& m = sc.materials[sc.meshes[h.mesh].material];
-                Frame fr = T == MAT_ANISO_GGX ? make_onb(normalize(h.sh.n)) : h.sh;
+                DevMaterial m = sc.materials[sc.meshes[h.mesh].material];
+                if ((T == MAT_DIFFUSE || T == MAT_ANISO_GGX) && m.has_tex) {
+                    // texture lookups replace the constants (diffuse.cu:15-20,
+                    // aniso_ggx.cu:19-35)
+                    if (m.tex[TEX_ALBEDO] >= 0) {
+                        const float3 a = tex_lookup(sc, m.tex[TEX_ALBEDO], tuv);
+                        m.albedo[0] = a.x;
+                        m.albedo[1] = a.y;
+                        m.albedo[2] = a.z;
+                    }
+                    if (T == MAT_ANISO_GGX && m.tex[TEX_SPECULAR] >= 0) {
+                        const float3 a = tex_lookup(sc, m.tex[TEX_SPECULAR], tuv);
+                        m.specular[0] = a.x;
+                        m.specular[1] = a.y;
+                        m.specular[2] = a.z;
+                    }
+                    if (T == MAT_ANISO_GGX && m.tex[TEX_ALPHA] >= 0) {
+                        const float3 a = tex_lookup(sc, m.tex[TEX_ALPHA], tuv);
+                        m.ax = a.x;
+                        m.ay = a.y;
+                    }
+                }
+                Frame fr = T == MAT_ANISO_GGX ? make_onb_t(normalize(h.sh.n), s_tan) : h.sh;
                 float3 wi = to_local(fr, neg(normalize(dir)));
                 if (T == MAT_ANISO_GGX) wi = normalize(wi);
                 const float alpha = use_guide ? P.gnet.fraction : 0.f;

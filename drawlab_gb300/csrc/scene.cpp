@@ -256,6 +256,20 @@ void validate_scene(const dl_mesh_desc* meshes, int32_t nm, const dl_material_de
         check(m.type >= DL_MAT_DIFFUSE && m.type <= DL_MAT_ANISO_GGX, "material " + std::to_string(i) + ": bad type");
         if (m.type == DL_MAT_MICROFACET) check(m.alpha[0] > 0.f, "microfacet alpha must be > 0");
         if (m.type == DL_MAT_ANISO_GGX) check(m.alpha[0] > 0.f && m.alpha[1] > 0.f, "aniso_ggx alpha must be > 0");
+        const std::string who = "material " + std::to_string(i) + ": ";
+        const dl_texture_desc* slots[5] = {&m.albedo_texture, &m.specular_texture, &m.alpha_texture,
+                                           &m.normal_texture, &m.tangent_texture};
+        for (int k = 0; k < 5; k++) {
+            const dl_texture_desc& t = *slots[k];
+            if (!t.rgb) continue;
+            // which textures each BSDF reads (diffuse.cu:15-20, aniso_ggx.cu:19-35)
+            check(m.type == DL_MAT_ANISO_GGX || (m.type == DL_MAT_DIFFUSE && k == 0),
+                  who + "this BSDF takes no such texture");
+            check(t.width > 0 && t.height > 0 && (int64_t)t.width * t.height <= ((int64_t)1 << 26),
+                  who + "texture size out of range");
+            for (int64_t q = 0; q < 3 * (int64_t)t.width * t.height; q++)
+                check(std::isfinite(t.rgb[q]), who + "texture values must be finite");
+        }
     }
     int num_env = 0;
     for (int l = 0; l < nl; l++) {
@@ -293,6 +307,7 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     std::vector<float> tri9((size_t)ntri * 9);
     std::vector<int4> vidx_orig((size_t)ntri);
     std::vector<float4> normals((size_t)std::max<int64_t>(nvert, 1));
+    std::vector<float2> texcoords((size_t)std::max<int64_t>(nvert, 1));
     std::vector<DevMesh> dmesh(std::max(nm, 1));
     int64_t t = 0, vo = 0;
     for (int i = 0; i < nm; i++) {
@@ -314,7 +329,10 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
         dmesh[i].material = m.material;
         dmesh[i].light = m.light;
         dmesh[i].has_normals = m.normals != nullptr;
-        dmesh[i].pad = 0;
+        dmesh[i].has_texcoords = m.texcoords != nullptr;
+        for (int64_t v = 0; v < m.num_vertices; v++)
+            texcoords[vo + v] = m.texcoords ? make_float2(m.texcoords[2 * v], m.texcoords[2 * v + 1])
+                                            : make_float2(0.f, 0.f);
         vo += m.num_vertices;
     }
     BvhBuildOptions bo;
@@ -323,6 +341,9 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     for (size_t k = 0; k < bvh.tri_order.size(); k++) vidx[k] = vidx_orig[bvh.tri_order[k]];
 
     std::vector<DevMaterial> dmat(std::max(nmat, 1));
+    std::vector<float4> texels;
+    std::vector<int64_t> tex_offset;
+    std::vector<DevTexture> dtex;
     for (int i = 0; i < nmat; i++) {
         const dl_material_desc& m = mats[i];
         DevMaterial& d = dmat[i];
@@ -336,6 +357,24 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
         d.int_ior = m.int_ior;
         d.ext_ior = m.ext_ior;
         d.ks = 1 - std::max(std::max(m.albedo[0], m.albedo[1]), m.albedo[2]);
+        const dl_texture_desc* slots[kTexSlots] = {&m.albedo_texture, &m.specular_texture, &m.alpha_texture,
+                                                   &m.normal_texture, &m.tangent_texture};
+        d.has_tex = 0;
+        for (int k = 0; k < kTexSlots; k++) {
+            d.tex[k] = -1;
+            const dl_texture_desc& t = *slots[k];
+            if (!t.rgb) continue;
+            DevTexture dt;
+            dt.texels = nullptr;  // set after the upload
+            dt.w = t.width;
+            dt.h = t.height;
+            tex_offset.push_back((int64_t)texels.size());
+            for (int64_t q = 0; q < (int64_t)t.width * t.height; q++)
+                texels.push_back(make_float4(t.rgb[3 * q], t.rgb[3 * q + 1], t.rgb[3 * q + 2], 0.f));
+            d.tex[k] = (int)dtex.size();
+            dtex.push_back(dt);
+            d.has_tex = 1;
+        }
     }
 
     std::vector<DevLight> dlights(std::max(nl, 1));
@@ -453,6 +492,12 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     S->tris.upload(bvh.tris, st);
     S->tri_vidx.upload(vidx, st);
     S->normals.upload(normals, st);
+    S->texcoords.upload(texcoords, st);
+    if (texels.empty()) texels.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+    S->texels.upload(texels, st);
+    for (size_t k = 0; k < dtex.size(); k++) dtex[k].texels = S->texels.as<float4>() + tex_offset[k];
+    if (dtex.empty()) dtex.push_back(DevTexture{nullptr, 0, 0});
+    S->textures.upload(dtex, st);
     S->meshes.upload(dmesh, st);
     S->materials.upload(dmat, st);
     S->lights.upload(dlights, st);
@@ -472,6 +517,8 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     D.lights = S->lights.as<DevLight>();
     D.emit_tris = S->emit_tris.as<float4>();
     D.emit_cdf = S->emit_cdf.as<float>();
+    D.textures = S->textures.as<DevTexture>();
+    D.texcoords = S->texcoords.as<float2>();
     D.num_tris = (int)ntri;
     D.num_lights = nl;
     D.cam = make_camera(*cam);

@@ -8,7 +8,8 @@
 // them (src/tracer/scene/scene.cpp:36-81).
 //
 // Supported plugins: mesh rectangle|obj, bsdf diffuse|mirror|dielectric|
-// microfacet|aniso_ggx, emitter area|point|envmap (PFM images), camera
+// microfacet|aniso_ggx (with bitmap textures from PNG / PFM), emitter
+// area|point|envmap (PFM images), camera
 // virtual|perspective|opencv, integrator path|normals,
 // sampler independent, rfilter gaussian|box.  Anything else is reported as
 // DL_ERR_UNSUPPORTED with its location.
@@ -274,6 +275,7 @@ enum ObjKind { O_SCENE, O_MESH, O_BSDF, O_EMITTER, O_CAMERA, O_INTEGRATOR, O_SAM
 struct Obj {
     ObjKind kind;
     std::string type;
+    std::string name;  // the "name" attribute (texture slots)
     Props props;
     std::vector<Obj*> children;
     int line = 0;
@@ -370,6 +372,7 @@ struct Interp {
             auto o = std::make_unique<Obj>();
             o->kind = kind;
             o->type = kind == O_SCENE ? "scene" : *n.attr("type");
+            if (const std::string* nm = n.attr("name")) o->name = *nm;
             o->props = props;
             o->children = children;
             o->line = n.line;
@@ -625,14 +628,57 @@ MeshData make_rectangle(const Props& p) {
     return m;
 }
 
-dl_material_desc make_material(const Obj& b) {
+// A <texture type="bitmap"> child: the image (PNG or PFM, resolved against
+// the scene file's directory) in the texel order the reference uploads
+// (src/tracer/texture/bitmap.cpp:60-98): 8-bit images as read (top row at
+// t = 0), float images flipped (bottom row at t = 0).
+dl_texture_desc load_texture(const Obj& t, const std::string& dir, std::list<std::vector<float>>& store) {
+    if (t.type != "bitmap")
+        throw Error(DL_ERR_UNSUPPORTED, "texture type \"" + t.type + "\" is not supported (line " +
+                                            std::to_string(t.line) + ")");
+    std::string fn = t.props.s("filename");
+    if (!fn.empty() && fn[0] != '/') fn = dir + "/" + fn;
+    int w = 0, h = 0;
+    bool is_float = false;
+    std::vector<float> img = read_image(fn, w, h, is_float);
+    if (is_float)
+        for (int y = 0; y < h / 2; y++)
+            std::swap_ranges(img.begin() + (size_t)y * w * 3, img.begin() + (size_t)(y + 1) * w * 3,
+                             img.begin() + (size_t)(h - 1 - y) * w * 3);
+    store.push_back(std::move(img));
+    dl_texture_desc d;
+    d.rgb = store.back().data();
+    d.width = w;
+    d.height = h;
+    return d;
+}
+
+dl_material_desc make_material(const Obj& b, const std::string& dir, std::list<std::vector<float>>& store) {
     dl_material_desc d;
     std::memset(&d, 0, sizeof(d));
     const Props& p = b.props;
     const float half[3] = {0.5f, 0.5f, 0.5f};
-    for (Obj* c : b.children)
-        if (c->kind == O_TEXTURE)
-            throw Error(DL_ERR_UNSUPPORTED, "textures are not supported (line " + std::to_string(c->line) + ")");
+    // texture children by name: diffuse "albedo" (diffuse.cpp:69-73);
+    // aniso_ggx "pd", "ps", "axay", "normal", "tangent" (aniso_ggx.cpp:43-57)
+    const bool aniso = b.type == "aniso_ggx";
+    for (Obj* c : b.children) {
+        if (c->kind != O_TEXTURE) continue;
+        dl_texture_desc* slot = nullptr;
+        if (b.type == "diffuse" && c->name == "albedo") slot = &d.albedo_texture;
+        else if (aniso && c->name == "pd") slot = &d.albedo_texture;
+        else if (aniso && c->name == "ps") slot = &d.specular_texture;
+        else if (aniso && c->name == "axay") slot = &d.alpha_texture;
+        else if (aniso && c->name == "normal") slot = &d.normal_texture;
+        else if (aniso && c->name == "tangent") slot = &d.tangent_texture;
+        else
+            throw Error(DL_ERR_UNSUPPORTED, "texture \"" + c->name + "\" of a " + b.type + " bsdf is not supported (line " +
+                                                std::to_string(c->line) + ")");
+        *slot = load_texture(*c, dir, store);
+    }
+    if (aniso && (d.normal_texture.rgb || d.tangent_texture.rgb) && p.b("is_tangent_space", true))
+        throw Error(DL_ERR_UNSUPPORTED, "tangent-space normal / tangent maps need mesh tangents, which no mesh "
+                                        "provides; set is_tangent_space to false for world-space maps (line " +
+                                            std::to_string(b.line) + ")");
     if (b.type == "diffuse") {
         d.type = DL_MAT_DIFFUSE;
         p.vec("albedo", P_COLOR, d.albedo, half);
@@ -698,7 +744,7 @@ int load_xml_scene(dl_context* ctx, const char* path, dl_scene** out) {
     auto add_material = [&](const Obj* b) -> int {
         auto f = mat_index.find(b);
         if (f != mat_index.end()) return f->second;
-        mats.push_back(make_material(*b));
+        mats.push_back(make_material(*b, it.dir, env_images));
         mat_index[b] = (int)mats.size() - 1;
         return (int)mats.size() - 1;
     };

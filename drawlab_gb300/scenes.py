@@ -48,6 +48,14 @@ class Material:
     alpha: tuple = (0.1, 0.1)
     int_ior: float = 1.5046
     ext_ior: float = 1.000277
+    # bitmap textures, (height, width, 3) float32, row k at t = (k + 0.5) / height
+    albedo_texture: np.ndarray | None = None
+    specular_texture: np.ndarray | None = None
+    alpha_texture: np.ndarray | None = None
+    normal_texture: np.ndarray | None = None
+    tangent_texture: np.ndarray | None = None
+
+TEXTURE_SLOTS = ("albedo_texture", "specular_texture", "alpha_texture", "normal_texture", "tangent_texture")
 
 
 @dataclass
@@ -179,6 +187,12 @@ class SceneData:
             mat[i].alpha[:] = [float(v) for v in x.alpha]
             mat[i].int_ior = x.int_ior
             mat[i].ext_ior = x.ext_ior
+            for slot in TEXTURE_SLOTS:
+                tex = getattr(x, slot)
+                if tex is not None:
+                    t = getattr(mat[i], slot)
+                    t.rgb = fptr(tex)
+                    t.height, t.width = tex.shape[0], tex.shape[1]
         nl = len(self.lights)
         ld = (abi.dl_light_desc * max(nl, 1))()
         for i, x in enumerate(self.lights):
@@ -320,6 +334,53 @@ def cornell(width: int = 256, height: int = 256, spp: int = 16, max_depth: int =
     s.add_area_light(li, (17.0, 12.0, 4.0))
     s.camera = Camera(width=width, height=height, eye=(0.0, 0.0, 3.9), lookat=(0.0, 0.0, 0.0),
                       up=(0.0, 1.0, 0.0), fov=39.3)
+    return s
+
+
+def textured_cornell(width: int = 64, height: int = 64, spp: int = 4, max_depth: int = 8, seed: int = 6) -> SceneData:
+    """The Cornell box with bitmap textures: checkered albedo textures on the
+    floor and back wall (texcoords over the quads, tiled twice: wrap
+    addressing), and in place of the short cuboid an anisotropic GGX sphere
+    with pd / ps / axay textures and world-space normal and tangent maps
+    (spherical texcoords)."""
+    rng = np.random.default_rng(seed)
+    s = cornell(width=width, height=height, spp=spp, max_depth=max_depth)
+    s.name = "textured_cornell"
+    uv_quad = np.array([[0, 0], [2, 0], [0, 2], [2, 2]], np.float32)   # rectangle() vertex order
+
+    def checker(n, a, b):
+        y, x = np.mgrid[0:n, 0:n]
+        m = ((x // 2 + y // 2) % 2)[..., None]
+        return np.where(m, np.asarray(a, np.float32), np.asarray(b, np.float32)).astype(np.float32)
+
+    floor_m = s.add_material(Material(albedo_texture=checker(16, (0.8, 0.75, 0.7), (0.15, 0.2, 0.3))))
+    back_m = s.add_material(Material(albedo_texture=rng.uniform(0.05, 0.9, (9, 13, 3)).astype(np.float32)))
+    s.meshes[0].material, s.meshes[0].texcoords = floor_m, uv_quad
+    s.meshes[2].material, s.meshes[2].texcoords = back_m, uv_quad
+    # the aniso sphere replaces the short cuboid
+    p, f, n = sphere_mesh(3, (0.34, -0.62, 0.32), 0.38)
+    d = (p - np.array([0.34, -0.62, 0.32], np.float32)) / 0.38
+    uv = np.stack([np.arctan2(d[:, 2], d[:, 0]) / (2 * np.pi) + 0.5,
+                   np.arccos(np.clip(d[:, 1], -1, 1)) / np.pi], 1).astype(np.float32)
+    th = 24
+    tw = 32
+    v, u = np.mgrid[0:th, 0:tw]
+    pd = np.stack([0.2 + 0.6 * (u / tw), 0.3 + 0.4 * (v / th), 0.5 + 0.0 * u], -1).astype(np.float32)
+    ps = np.full((th, tw, 3), 0.6, np.float32) * (0.5 + 0.5 * ((u + v) % 2))[..., None].astype(np.float32)
+    axay = np.stack([0.05 + 0.4 * (u / tw), 0.4 - 0.3 * (v / th), 0.0 * u], -1).astype(np.float32)
+    # world-space maps: a perturbed outward normal, a tangent around the y axis
+    phi = (u + 0.5) / tw * 2 * np.pi - np.pi
+    theta = (v + 0.5) / th * np.pi
+    nw = np.stack([np.sin(theta) * np.cos(phi), np.cos(theta), np.sin(theta) * np.sin(phi)], -1)
+    nw = nw + 0.15 * rng.normal(size=nw.shape)
+    nw /= np.linalg.norm(nw, axis=-1, keepdims=True)
+    tw_ = np.stack([-np.sin(phi), np.zeros_like(phi), np.cos(phi)], -1)
+    normal_map = (0.5 * (nw + 1)).astype(np.float32)
+    tangent_map = (0.5 * (tw_ + 1)).astype(np.float32)
+    aniso = s.add_material(Material(type=abi.DL_MAT_ANISO_GGX, albedo=(0.5, 0.5, 0.5), specular=(0.5, 0.5, 0.5),
+                                    alpha=(0.2, 0.2), albedo_texture=pd, specular_texture=ps, alpha_texture=axay,
+                                    normal_texture=normal_map, tangent_texture=tangent_map))
+    s.meshes[6] = Mesh(p, f, n, texcoords=uv, material=aniso)
     return s
 
 

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 6
+#define DL_ABI_VERSION 7
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -67,6 +67,17 @@ enum dl_material_type {
     DL_MAT_ANISO_GGX = 4    /* "aniso_ggx"  src/optix/cuda/material/aniso_ggx.cu */
 };
 
+/* A bitmap texture: `height` rows of `width` RGB floats; row k is sampled
+ * around texture coordinate t = (k + 0.5) / height, column j around
+ * s = (j + 0.5) / width -- the texel order the reference uploads (8-bit
+ * images top row first, float images bottom row first,
+ * src/tracer/texture/bitmap.cpp:60-98).  rgb NULL: no texture. */
+typedef struct dl_texture_desc {
+    const float* rgb;
+    int32_t width;
+    int32_t height;
+} dl_texture_desc;
+
 typedef struct dl_material_desc {
     int32_t type;         /* dl_material_type */
     float albedo[3];      /* diffuse albedo | microfacet kd | aniso_ggx pd */
@@ -74,6 +85,17 @@ typedef struct dl_material_desc {
     float alpha[2];       /* microfacet alpha in [0]; aniso_ggx (ax, ay) */
     float int_ior;        /* dielectric / microfacet interior IOR */
     float ext_ior;        /* dielectric / microfacet exterior IOR */
+    /* Bitmap textures (the reference reads them in its OptiX path only:
+     * src/optix/cuda/material/diffuse.cu:15-20, aniso_ggx.cu:19-35,
+     * src/optix/cuda/shader_common.h:38-143), looked up at the hit's
+     * interpolated texture coordinates (the mesh's texcoords; (0, 0) without
+     * them) with bilinear filtering and wrap addressing.  They replace the
+     * constants above. */
+    dl_texture_desc albedo_texture;    /* diffuse albedo | aniso_ggx pd */
+    dl_texture_desc specular_texture;  /* aniso_ggx ps */
+    dl_texture_desc alpha_texture;     /* aniso_ggx (ax, ay) = (R, G) */
+    dl_texture_desc normal_texture;    /* aniso_ggx world-space shading normal: normalize(2 rgb - 1) */
+    dl_texture_desc tangent_texture;   /* aniso_ggx world-space shading tangent: normalize(2 rgb - 1) */
 } dl_material_desc;
 
 /* Emitter plugins (include/tracer/emitter.h:7-117). */

@@ -253,6 +253,15 @@ inline Frame make_onb(V3 n) {
     f.t = cross(f.b, n);
     return f;
 }
+// Onb(normal, tangent) with a non-zero tangent (onb.h:29-32)
+inline Frame make_onb_t(V3 n, V3 t) {
+    if (t.x == 0.f && t.y == 0.f && t.z == 0.f) return make_onb(n);
+    Frame f;
+    f.n = n;
+    f.t = t;
+    f.b = normalized(cross(n, t));
+    return f;
+}
 inline V3 to_local(const Frame& f, V3 v) { return V3(dot(v, f.t), dot(v, f.b), dot(f.n, v)); }
 inline V3 to_world(const Frame& f, V3 v) { return f.t * v.x + f.b * v.y + f.n * v.z; }
 inline float tan_theta(V3 v) {
@@ -330,6 +339,13 @@ struct Material {
     float ax, ay;
     float int_ior, ext_ior;
     float ks;  // microfacet: 1 - max(kd)
+    int tex[5] = {-1, -1, -1, -1, -1};  // albedo, specular, alpha, normal, tangent texture; -1 = none
+    bool has_tex = false;
+};
+
+struct Texture {
+    int w = 0, h = 0;
+    std::vector<float> rgb;  // row k at t = (k + 0.5) / h
 };
 
 struct Mesh {
@@ -418,6 +434,8 @@ struct Hit {
     Frame sh, geo;
     int mesh = -1;
     int64_t prim = -1;
+    P2 tuv{0, 0};  // texture coordinates ((0, 0) without mesh texcoords)
+    V3 tan;        // aniso_ggx: shading tangent from a tangent map (0: none)
 };
 
 struct Camera {
@@ -440,6 +458,7 @@ struct Filter {
 struct Scene {
     std::vector<Mesh> meshes;
     std::vector<Material> mats;
+    std::vector<Texture> textures;
     std::vector<Light> lights;
     int env_light = -1;
     // power-proportional emitter pick (DL_RENDER_POWER_LIGHT_PICK)
@@ -559,6 +578,26 @@ bool anyhit(const Scene& sc, int node, const Ray& ray) {
     return false;
 }
 
+// Bilinear, wrap-addressed lookup at normalised (u, v) (a CUDA texture with
+// linear filtering and wrap addressing, fp32 weights).
+V3 tex_bilinear(const Texture& T, float u, float v) {
+    const int W = T.w, H = T.h;
+    if (!std::isfinite(u) || !std::isfinite(v)) return V3();
+    u = u - std::floor(u);
+    v = v - std::floor(v);
+    float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy;
+    int x0 = (int)fx, y0 = (int)fy, x1 = x0 + 1, y1 = y0 + 1;
+    if (x0 < 0) x0 += W;
+    if (y0 < 0) y0 += H;
+    if (x1 >= W) x1 -= W;
+    if (y1 >= H) y1 -= H;
+    auto tx = [&](int yy, int xx) { return ld3(&T.rgb[3 * ((size_t)yy * W + xx)]); };
+    float bx = 1.f - ax, by = 1.f - ay;
+    return tx(y0, x0) * (bx * by) + tx(y0, x1) * (ax * by) + tx(y1, x0) * (bx * ay) + tx(y1, x1) * (ax * ay);
+}
+
 // octree.cpp:153-212
 bool ray_intersect(const Scene& sc, const Ray& ray_in, Hit& its) {
     Ray ray = ray_in;
@@ -592,7 +631,34 @@ bool ray_intersect(const Scene& sc, const Ray& ray_in, Hit& its) {
     } else {
         its.sh = its.geo;
     }
+    const Material& mat = sc.mats[m.material];
+    if (mat.has_tex) {
+        // texture coordinates as the OptiX shader (shader_common.h:38-45);
+        // world-space normal / tangent maps of aniso_ggx (62-64, 104-107)
+        its.tuv = m.UV.empty() ? P2{0.f, 0.f} : its.uv;
+        auto mapped = [&](int t) {
+            V3 c = tex_bilinear(sc.textures[t], its.tuv.x, its.tuv.y);
+            return normalized(V3(c.x * 2.f - 1.f, c.y * 2.f - 1.f, c.z * 2.f - 1.f));
+        };
+        if (mat.type == DL_MAT_ANISO_GGX && mat.tex[3] >= 0) its.sh.n = mapped(mat.tex[3]);
+        if (mat.type == DL_MAT_ANISO_GGX && mat.tex[4] >= 0) its.tan = mapped(mat.tex[4]);
+    }
     return true;
+}
+
+// The material at a hit with its textures looked up (diffuse.cu:15-20,
+// aniso_ggx.cu:19-35).
+Material material_at(const Scene& sc, const Hit& its) {
+    Material m = sc.mats[sc.meshes[its.mesh].material];
+    if (!m.has_tex) return m;
+    if (m.tex[0] >= 0) m.albedo = tex_bilinear(sc.textures[m.tex[0]], its.tuv.x, its.tuv.y);
+    if (m.type == DL_MAT_ANISO_GGX && m.tex[1] >= 0) m.specular = tex_bilinear(sc.textures[m.tex[1]], its.tuv.x, its.tuv.y);
+    if (m.type == DL_MAT_ANISO_GGX && m.tex[2] >= 0) {
+        V3 a = tex_bilinear(sc.textures[m.tex[2]], its.tuv.x, its.tuv.y);
+        m.ax = a.x;
+        m.ay = a.y;
+    }
+    return m;
 }
 
 inline bool occluded(const Scene& sc, const Ray& r) { return anyhit(sc, sc.root, r); }
@@ -1022,7 +1088,7 @@ inline V3 emitter_eval(const Light& L, const Hit& its, V3 wi) {
 // for aniso_ggx).
 inline Frame shading_frame(const Scene& sc, const Hit& its) {
     const Material& m = sc.mats[sc.meshes[its.mesh].material];
-    if (m.type == DL_MAT_ANISO_GGX) return make_onb(normalized(its.sh.n));
+    if (m.type == DL_MAT_ANISO_GGX) return make_onb_t(normalized(its.sh.n), its.tan);
     return its.sh;
 }
 
@@ -1055,7 +1121,7 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
     if (light >= 0) result = result + mul(tp, emitter_eval(sc.lights[light], its, -ray.d));
     for (int depth = 0;; ++depth) {
         if (o.max_depth > 0 && depth >= o.max_depth) break;
-        const Material& bsdf = sc.mats[sc.meshes[its.mesh].material];
+        const Material bsdf = material_at(sc, its);
         Frame fr = shading_frame(sc, its);
         DirSample ds;
         V3 ev;
@@ -1435,6 +1501,19 @@ void* orc_scene_create(const dl_mesh_desc* meshes, int32_t nm, const dl_material
         m.int_ior = mats[i].int_ior;
         m.ext_ior = mats[i].ext_ior;
         m.ks = 1 - maxc(m.albedo);
+        const dl_texture_desc* slots[5] = {&mats[i].albedo_texture, &mats[i].specular_texture,
+                                           &mats[i].alpha_texture, &mats[i].normal_texture,
+                                           &mats[i].tangent_texture};
+        for (int k = 0; k < 5; k++) {
+            if (!slots[k]->rgb) continue;
+            Texture t;
+            t.w = slots[k]->width;
+            t.h = slots[k]->height;
+            t.rgb.assign(slots[k]->rgb, slots[k]->rgb + 3 * (size_t)t.w * t.h);
+            m.tex[k] = (int)sc->textures.size();
+            sc->textures.push_back(std::move(t));
+            m.has_tex = true;
+        }
         sc->mats.push_back(m);
     }
     int64_t off = 0;

@@ -46,12 +46,12 @@ def test_abi_version(lib):
 def test_struct_sizes_match_header():
     # sizes of the descriptor structs as laid out by a C compiler (x86-64/aarch64 LP64)
     assert C.sizeof(abi.dl_mesh_desc) == 4 * 8 + 2 * 8 + 2 * 4
-    assert C.sizeof(abi.dl_material_desc) == 4 * (1 + 3 + 3 + 2 + 2)
+    assert C.sizeof(abi.dl_material_desc) == 4 * (1 + 3 + 3 + 2 + 2) + 4 + 5 * 16
     assert C.sizeof(abi.dl_render_opts) == 4 * 4 + 8 + 4 + 4 + 8
     assert C.sizeof(abi.dl_camera_desc) == 4 * (3 + 9 + 1 + 16 + 2 + 4)
 
 
-STRUCTS = ["dl_mesh_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts", "dl_request",
+STRUCTS = ["dl_mesh_desc", "dl_texture_desc", "dl_material_desc", "dl_light_desc", "dl_camera_desc", "dl_render_opts", "dl_request",
            "dl_tune_params", "dl_guide_config",
            "dl_scene_info", "dl_stats", "dl_traversal_counts"]
 

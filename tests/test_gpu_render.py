@@ -76,6 +76,7 @@ LI_CASES = {
     "spheres_normals": (lambda: scenes.material_spheres(width=96, height=54, num_spheres=16, level=3),
                         dict(flags=abi.DL_RENDER_NORMALS)),
     "env_normals": (lambda: scenes.env_spheres(width=64, height=40), dict(flags=abi.DL_RENDER_NORMALS)),
+    "textured": (lambda: scenes.textured_cornell(48, 48), dict(max_depth=8)),
 }
 
 

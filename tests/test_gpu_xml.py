@@ -259,3 +259,68 @@ def test_command_line_renders_xml_to_exr_and_png(ctx, tmp_path):
     o.spp, o.seed = 4, 2
     np.testing.assert_array_equal(img, gx.render(o))
     assert io.read_png(tmp_path / "scene.png").shape == img.shape
+
+
+@pytest.mark.parametrize("fmt", ["png", "pfm"])
+def test_xml_bitmap_texture_matches_arrays(ctx, tmp_path, fmt):
+    """<texture type="bitmap" name="albedo"> on the floor's diffuse BSDF:
+    the same paths as the arrays scene whose floor carries the texture in the
+    texel order the reference uploads -- PNG rows as read (top row at t = 0),
+    float images flipped (bottom row at t = 0) -- and the rectangle's
+    texcoords (1, 0), (1, 1), (0, 0), (0, 1)."""
+    import test_image_io as io
+    arr, (P, F, N) = arrays_equivalent()
+    rng = np.random.default_rng(8)
+    if fmt == "png":
+        px = rng.integers(0, 256, (6, 9, 3)).astype(np.uint8)
+        (tmp_path / "tex.png").write_bytes(io.png_bytes(px, 2, [0, 1, 4]))
+        tex = px.astype(np.float32) / np.float32(255)
+    else:
+        img = rng.uniform(0.05, 0.9, (6, 9, 3)).astype(np.float32)
+        api.write_image(tmp_path / "tex.pfm", img)
+        tex = np.ascontiguousarray(img[::-1])
+    floor = arr.meshes[0]
+    floor.texcoords = np.array([[1, 0], [1, 1], [0, 0], [0, 1]], np.float32)
+    floor.material = arr.add_material(scenes.Material(albedo_texture=tex))
+    text = cornell_xml(arr, "cuboid.obj")
+    # the floor is the first rectangle: give its BSDF the texture
+    first = text.index('<bsdf type="diffuse"><color name="albedo" value="0.725, 0.725, 0.725"/></bsdf>',
+                       text.index('<mesh type="rectangle">'))
+    text = (text[:first] + '<bsdf type="diffuse"><texture type="bitmap" name="albedo">'
+            '<string name="filename" value="tex.%s"/></texture></bsdf>' % fmt
+            + text[first + len('<bsdf type="diffuse"><color name="albedo" value="0.725, 0.725, 0.725"/></bsdf>'):])
+    write_obj(tmp_path / "cuboid.obj", P, F, N)
+    (tmp_path / "scene.xml").write_text(text)
+    gx = api.Scene.from_xml(ctx, str(tmp_path / "scene.xml"))
+    ga = api.Scene.from_data(ctx, arr)
+    W, H = arr.camera.width, arr.camera.height
+    xys = np.array([(x, y, s) for y in range(H) for x in range(W) for s in range(2)], np.int32)
+    opts = abi.make_opts(seed=3, max_depth=6)
+    La, _ = gx.li(opts, xys)
+    Lb, _ = ga.li(opts, xys)
+    np.testing.assert_array_equal(La, Lb)
+    # and the texture is visible: differs from the untextured scene
+    plain, _ = api.Scene.from_data(ctx, arrays_equivalent()[0]).li(opts, xys)
+    assert np.abs(La - plain).max() > 0.05
+
+
+def test_xml_texture_errors(ctx, tmp_path):
+    (tmp_path / "t.pfm").write_bytes(b"PF\n1 1\n-1.0\n" + np.zeros(3, "<f4").tobytes())
+    cases = [
+        ("<bsdf type='mirror'><texture type='bitmap' name='albedo'><string name='filename' value='t.pfm'/>"
+         "</texture></bsdf>", abi.DL_ERR_UNSUPPORTED),
+        ("<bsdf type='aniso_ggx'><texture type='bitmap' name='normal'><string name='filename' value='t.pfm'/>"
+         "</texture></bsdf>", abi.DL_ERR_UNSUPPORTED),            # tangent space by default
+        ("<bsdf type='diffuse'><texture type='checkerboard' name='albedo'/></bsdf>", abi.DL_ERR_UNSUPPORTED),
+        ("<bsdf type='diffuse'><texture type='bitmap' name='albedo'><string name='filename' value='none.png'/>"
+         "</texture></bsdf>", abi.DL_ERR_IO),
+    ]
+    for k, (bsdf, status) in enumerate(cases):
+        p = tmp_path / ("b%d.xml" % k)
+        p.write_text("<scene><integrator type='path'/><camera type='virtual'><vector name='eye' value='0,0,3'/>"
+                     "<vector name='lookat' value='0,0,0'/><vector name='up' value='0,1,0'/></camera>"
+                     "<mesh type='rectangle'><vector name='pos' value='-1,-1,0'/><vector name='v0' value='2,0,0'/>"
+                     "<vector name='v1' value='0,2,0'/>%s</mesh></scene>" % bsdf)
+        with pytest.raises(api.DrawlabError) as e:
+            api.Scene.from_xml(ctx, str(p))
+        assert e.value.status == status, (k, e.value)

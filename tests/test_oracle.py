@@ -180,3 +180,23 @@ def test_opencv_camera_rays_follow_the_intrinsics():
     xys = np.array([(x, y, 0) for y in range(30) for x in range(40)], np.int32)
     L, _ = orc.li(abi.make_opts(seed=1, flags=abi.DL_RENDER_NORMALS), xys)
     np.testing.assert_allclose(L, np.tile([0.0, 0.0, 1.0], (len(L), 1)), atol=1e-6)
+
+
+def test_constant_texture_matches_constant_albedo():
+    """A texture whose texels all equal a material's constant gives the same
+    radiance as the constant (to the rounding of the bilinear weights), and
+    the textured scene renders (a sanity check of the oracle's texture
+    restatement; the GPU is checked against it path by path)."""
+    sc = scenes.cornell(width=24, height=24)
+    xys = mg.seeded_paths(sc, 1500, seed=2)
+    opts = abi.make_opts(seed=4, max_depth=6)
+    L0, _ = po.OracleScene(sc).li(opts, xys)
+    for m in sc.materials:
+        m.albedo_texture = np.tile(np.asarray(m.albedo, np.float32), (5, 7, 1))
+    for mesh in sc.meshes:
+        mesh.texcoords = np.random.default_rng(1).uniform(-2, 3, (mesh.positions.shape[0], 2)).astype(np.float32)
+    L1, _ = po.OracleScene(sc).li(opts, xys)
+    close = np.all(np.abs(L1 - L0) <= 1e-4 * (1 + np.abs(L0)), axis=1)
+    assert close.mean() > 0.99
+    Lt, _ = po.OracleScene(scenes.textured_cornell(24, 24)).li(opts, xys)
+    assert np.isfinite(Lt).all() and Lt.mean() > 0
