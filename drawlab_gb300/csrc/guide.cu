@@ -32,25 +32,26 @@ namespace dl {
 static_assert(kGImgTrainBytes == kGuideImageBytes, "image size");
 
 // Raw network outputs (40 per row) of n input rows, 128 rows per tile on
-// the tensor cores.
-__global__ void __launch_bounds__(kTcRows) k_guide_infer(const void* image, const float* in, float* out, int n,
-                                                          unsigned* err) {
+// the tensor cores; each of a block's two warpgroups walks its own tiles.
+__global__ void __launch_bounds__(kTcThreads) k_guide_infer(const void* image, const float* in, float* out, int n,
+                                                             unsigned* err) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     GuideTcSmem& S = *reinterpret_cast<GuideTcSmem*>(dyn_smem);
     const int ntiles = (n + kTcRows - 1) / kTcRows;
-    if ((int)blockIdx.x >= ntiles) return;
+    if ((int)blockIdx.x * kTcGroups >= ntiles) return;
+    const int g = tc_group(), row = tc_row();
     uint32_t phase = 0;
     bool ok = guide_tc_begin(S, image, err);
-    for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-        const int r = tile * kTcRows + threadIdx.x;
+    for (int tile = blockIdx.x * kTcGroups + g; ok && tile < ntiles; tile += gridDim.x * kTcGroups) {
+        const int r = tile * kTcRows + row;
         float x[kGIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (r < n)
             for (int i = 0; i < kGIn; i++) x[i] = in[(size_t)kGIn * r + i];
-        __syncthreads();  // the previous tile's outputs have been read
-        encode_row_tc(x, S.act, threadIdx.x);
-        ok = guide_tc_forward(S, phase, err);
+        wg_sync(g);  // the previous tile's outputs have been read
+        encode_row_tc(x, S.act[g], row);
+        ok = guide_tc_forward(S, g, phase, err);
         if (ok && r < n) {
-            const float* o = tc_out_row(S, threadIdx.x);
+            const float* o = tc_out_row(S, g, row);
             for (int j = 0; j < kGOut; j++) out[(size_t)r * kGOut + j] = o[j];
         }
     }
@@ -550,7 +551,7 @@ static int infer_blocks_per_sm() {
     cudaFuncAttributes fa;
     DL_CUDA(cudaFuncGetAttributes(&fa, k_guide_infer));
     const int regs_per_warp = ((fa.numRegs + 7) / 8) * 8 * 32;
-    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcRows / 32));
+    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcThreads / 32));
     const size_t smem = sizeof(GuideTcSmem) + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
     return std::max(1, std::min(by_regs, (int)(prop.sharedMemPerMultiprocessor / smem)));
 }
@@ -561,8 +562,8 @@ void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n) {
     unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
     DL_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
     const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
-    const int blocks = (int)std::min<int64_t>(ntiles, (int64_t)G->ctx->num_sms * per_sm);
-    k_guide_infer<<<blocks, kTcRows, sizeof(GuideTcSmem), st>>>(G->image.ptr, d_in, d_out, (int)n, err);
+    const int blocks = (int)std::min<int64_t>((ntiles + kTcGroups - 1) / kTcGroups, (int64_t)G->ctx->num_sms * per_sm);
+    k_guide_infer<<<blocks, kTcThreads, sizeof(GuideTcSmem), st>>>(G->image.ptr, d_in, d_out, (int)n, err);
     DL_CUDA(cudaGetLastError());
 }
 

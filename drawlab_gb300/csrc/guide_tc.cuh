@@ -1,14 +1,17 @@
 // The guiding network (guide.cuh) on the fifth-generation tensor cores.
 //
-// A 128-thread block evaluates 128 shading points at a time, one row per
-// thread.  Each thread writes its row's input encoding into shared memory;
-// one thread issues each layer as tcgen05.mma instructions (M = 128 rows,
-// N = 64 or 48 outputs, K = 16 per instruction) with both operands in shared
-// memory and the fp32 accumulator in tensor memory (64 columns per block);
-// completion arrives on an mbarrier.  Each warp then reads its 32 rows back
-// with tcgen05.ld, adds the bias, applies ReLU, and writes the fp16
-// activations as the next layer's operand.  The outputs land, fp32, in a
-// per-row slot of shared memory.
+// A block holds two warpgroups (256 threads) that share one copy of the
+// weights; each warpgroup evaluates its own 128 shading points at a time,
+// one row per thread, independently of the other (two tiles in flight per
+// block, synchronised by per-warpgroup named barriers).  Each thread writes
+// its row's input encoding into its warpgroup's operand tile; the
+// warpgroup's first thread issues each layer as tcgen05.mma instructions
+// (M = 128 rows, N = 64 or 48 outputs, K = 16 per instruction) with both
+// operands in shared memory and the fp32 accumulator in the warpgroup's 64
+// tensor-memory columns; completion arrives on the warpgroup's mbarrier.
+// Each warp then reads its 32 rows back with tcgen05.ld, adds the bias,
+// applies ReLU, and writes the fp16 activations as the next layer's
+// operand.  The outputs land, fp32, in a per-row slot of shared memory.
 //
 // The weights reach shared memory in one bulk copy (cp.async.bulk) of the
 // weight image: the fp16 matrices already in the tensor core's canonical
@@ -31,8 +34,11 @@
 
 namespace dl {
 
-constexpr int kTcRows = 128;  // rows per tile = threads per block
-constexpr int kTcCols = 64;   // tensor-memory columns per block (fp32 accumulators, reused by every layer)
+constexpr int kTcRows = 128;                     // rows per tile = threads per warpgroup
+constexpr int kTcGroups = 2;                     // warpgroups (tiles in flight) per block
+constexpr int kTcThreads = kTcRows * kTcGroups;  // threads per block
+constexpr int kTcCols = 64 * kTcGroups;          // tensor-memory columns per block (64 per warpgroup,
+                                                 // fp32 accumulators reused by every layer)
 constexpr uint64_t kTcWaitNs = 1000000000ull;
 constexpr unsigned kErrTensorWait = 2u;  // error-word bit: a tensor-core wait ran out
 
@@ -106,19 +112,38 @@ constexpr int kTcOutStride = kGStoredLobes + 1;
 struct GuideTcSmem {
     __half w[kGImgHalves];    // the image: weights ...
     float bias[kGImgBiases];  // ... and biases, contiguous
-    // encodings; then the hidden activations (K = 64 layout); then the fp32
-    // outputs (kTcOutStride floats per row), decoded in place into lobes
-    alignas(16) __half act[kTcRows * kGEnc];
-    uint64_t bar_w, bar_mma;
+    // per warpgroup: encodings; then the hidden activations (K = 64 layout);
+    // then the fp32 outputs (kTcOutStride floats per row), decoded in place
+    alignas(16) __half act[kTcGroups][kTcRows * kGEnc];
+    uint64_t bar_w, bar_mma[kTcGroups];
     uint32_t tmem;
     int fail;
 };
 static_assert(offsetof(GuideTcSmem, bias) == kGImgHalves * 2, "image layout");
-static_assert(offsetof(GuideTcSmem, act) % 16 == 0, "operand alignment");
-static_assert(kTcRows * kTcOutStride * 4 <= (int)sizeof(GuideTcSmem::act), "outputs fit the operand tile");
+static_assert(offsetof(GuideTcSmem, act) % 16 == 0 && (kTcRows * kGEnc * 2) % 16 == 0, "operand alignment");
+static_assert(kTcRows * kTcOutStride * 4 <= kTcRows * kGEnc * 2, "outputs fit the operand tile");
 
-__device__ __forceinline__ float* tc_out_row(GuideTcSmem& S, int r) {
-    return reinterpret_cast<float*>(S.act) + r * kTcOutStride;
+__device__ __forceinline__ int tc_group() { return (int)threadIdx.x >> 7; }  // the thread's warpgroup
+__device__ __forceinline__ int tc_row() { return (int)threadIdx.x & (kTcRows - 1); }  // its row in the tile
+
+// Named barrier 1 + g over warpgroup g's 128 threads (0 is __syncthreads).
+__device__ __forceinline__ void wg_sync(int g) {
+    asm volatile("bar.sync %0, 128;\n" :: "r"(1 + g) : "memory");
+}
+// The same barrier, returning whether `pred` holds in any of its threads.
+__device__ __forceinline__ bool wg_or(int g, bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r) : "r"((uint32_t)pred), "r"(1 + g) : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ float* tc_out_row(GuideTcSmem& S, int g, int r) {
+    return reinterpret_cast<float*>(S.act[g]) + r * kTcOutStride;
 }
 
 __device__ __forceinline__ void tc_record_failure(GuideTcSmem& S, unsigned* err) {
@@ -131,7 +156,7 @@ __device__ __forceinline__ void tc_record_failure(GuideTcSmem& S, unsigned* err)
 __device__ __forceinline__ bool guide_tc_begin(GuideTcSmem& S, const void* image, unsigned* err) {
     if (threadIdx.x == 0) {
         tc::mbar_init(&S.bar_w, 1);
-        tc::mbar_init(&S.bar_mma, 1);
+        for (int g = 0; g < kTcGroups; g++) tc::mbar_init(&S.bar_mma[g], 1);
         S.fail = 0;
     }
     if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, kTcCols);
@@ -145,14 +170,16 @@ __device__ __forceinline__ bool guide_tc_begin(GuideTcSmem& S, const void* image
 }
 
 // Block end (all threads): after a failed wait, wait (bounded) for the
-// outstanding weight copy and layer, then free the tensor memory.
+// outstanding weight copy and the thread's warpgroup's outstanding layer
+// (`mma_phase`: that warpgroup's next parity), then free the tensor memory.
 __device__ __forceinline__ void guide_tc_end(GuideTcSmem& S, uint32_t mma_phase) {
     tc::fence_before_sync();
     __syncthreads();
     if (S.fail) {
         (void)tc::mbar_wait(&S.bar_w, 0, kTcWaitNs);
-        (void)tc::mbar_wait(&S.bar_mma, mma_phase, kTcWaitNs);
+        (void)tc::mbar_wait(&S.bar_mma[tc_group()], mma_phase, kTcWaitNs);
     }
+    __syncthreads();
     if (threadIdx.x < 32) {
         tc::fence_after_sync();
         tc::tmem_dealloc(S.tmem, kTcCols);
@@ -178,24 +205,31 @@ __device__ __forceinline__ void encode_row_tc(const float* in6, __half* act, int
     }
 }
 
-// One layer: D (tensor memory) = act (128 x K) W^T, W [N][K] in the image.
+// One layer of warpgroup g: D (its tensor-memory columns) = act (128 x K)
+// W^T, W [N][K] in the image.
 template <int K, int N>
-__device__ __forceinline__ void tc_issue_layer(GuideTcSmem& S, int w_off) {
+__device__ __forceinline__ void tc_issue_layer(GuideTcSmem& S, int g, int w_off) {
     constexpr uint32_t idesc = tc::idesc_f16_f32(kTcRows, N);
-    const uint32_t a = tc::smem_addr(S.act), b = tc::smem_addr(S.w + w_off);
+    const uint32_t a = tc::smem_addr(S.act[g]), b = tc::smem_addr(S.w + w_off);
     tc::fence_after_sync();
 #pragma unroll
     for (int ks = 0; ks < K / 16; ks++)
-        tc::mma_f16(S.tmem, tc::smem_desc(a + ks * 256, 128, K * 16), tc::smem_desc(b + ks * 256, 128, K * 16), idesc,
-                    ks > 0 ? 1u : 0u);
-    tc::commit(&S.bar_mma);
+        tc::mma_f16(S.tmem + 64u * g, tc::smem_desc(a + ks * 256, 128, K * 16), tc::smem_desc(b + ks * 256, 128, K * 16),
+                    idesc, ks > 0 ? 1u : 0u);
+    tc::commit(&S.bar_mma[g]);
+}
+
+// The warp's 32 accumulator lanes in its warpgroup's columns.
+__device__ __forceinline__ uint32_t tc_warp_tmem(const GuideTcSmem& S, int g) {
+    return S.tmem + 64u * g + ((uint32_t)(tc_row() & ~31) << 16);
 }
 
 // Bias + ReLU of the warp's 32 rows (64 columns of tensor memory), written
 // as the next layer's operand (K = 64 layout).
-__device__ __forceinline__ void tc_hidden_epilogue(GuideTcSmem& S, const float* bias) {
-    const int r = threadIdx.x;
-    const uint32_t t = S.tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
+__device__ __forceinline__ void tc_hidden_epilogue(GuideTcSmem& S, int g, const float* bias) {
+    const int r = tc_row();
+    const uint32_t t = tc_warp_tmem(S, g);
+    __half* act = S.act[g];
 #pragma unroll
     for (int c0 = 0; c0 < kGHid; c0 += 16) {
         float v[16];
@@ -207,21 +241,23 @@ __device__ __forceinline__ void tc_hidden_epilogue(GuideTcSmem& S, const float* 
                                           fmaxf(v[2 * j + 1] + bias[c0 + 2 * j + 1], 0.f));
             p[j] = *reinterpret_cast<const uint32_t*>(&h);
         }
-        *reinterpret_cast<uint4*>(S.act + canon_index(r, c0, kGHid)) = make_uint4(p[0], p[1], p[2], p[3]);
-        *reinterpret_cast<uint4*>(S.act + canon_index(r, c0 + 8, kGHid)) = make_uint4(p[4], p[5], p[6], p[7]);
+        *reinterpret_cast<uint4*>(act + canon_index(r, c0, kGHid)) = make_uint4(p[0], p[1], p[2], p[3]);
+        *reinterpret_cast<uint4*>(act + canon_index(r, c0 + 8, kGHid)) = make_uint4(p[4], p[5], p[6], p[7]);
     }
     tc::fence_smem_to_async();
 }
 
-// Runs the network on the 128 rows whose encodings the threads wrote to
-// S.act.  All threads of the block call it together.  On return (true) each
-// thread's 40 outputs are at tc_out_row(S, threadIdx.x).  `phase` is the
-// parity of the next completion of S.bar_mma, kept by every thread.
-// Returns false (the same in every thread) after a wait ran out.
-__device__ __forceinline__ bool guide_tc_forward(GuideTcSmem& S, uint32_t& phase, unsigned* err) {
+// Runs the network on the 128 rows whose encodings the threads of
+// warpgroup g wrote to S.act[g].  All threads of the warpgroup call it
+// together.  On return (true) each thread's 40 outputs are at
+// tc_out_row(S, g, tc_row()).  `phase` is the parity of the next completion
+// of S.bar_mma[g], kept by every thread of the warpgroup.  Returns false
+// (the same in every thread of the warpgroup) after a wait ran out.
+__device__ __forceinline__ bool guide_tc_forward(GuideTcSmem& S, int g, uint32_t& phase, unsigned* err) {
     bool failed = false;
+    const bool issuer = tc_row() == 0;
     auto wait = [&]() {
-        if (!tc::mbar_wait(&S.bar_mma, phase, kTcWaitNs)) {
+        if (!tc::mbar_wait(&S.bar_mma[g], phase, kTcWaitNs)) {
             failed = true;
             tc_record_failure(S, err);
         } else {
@@ -231,24 +267,24 @@ __device__ __forceinline__ bool guide_tc_forward(GuideTcSmem& S, uint32_t& phase
     };
     tc::fence_smem_to_async();
     tc::fence_before_sync();
-    __syncthreads();
-    if (threadIdx.x == 0) tc_issue_layer<kGEnc, kGHid>(S, kGImgW1);
+    wg_sync(g);
+    if (issuer) tc_issue_layer<kGEnc, kGHid>(S, g, kGImgW1);
     wait();
-    tc_hidden_epilogue(S, S.bias + kGImgB1);
+    tc_hidden_epilogue(S, g, S.bias + kGImgB1);
     tc::fence_before_sync();
-    if (__syncthreads_or(failed)) return false;
-    if (threadIdx.x == 0) tc_issue_layer<kGHid, kGHid>(S, kGImgW2);
+    if (wg_or(g, failed)) return false;
+    if (issuer) tc_issue_layer<kGHid, kGHid>(S, g, kGImgW2);
     wait();
-    tc_hidden_epilogue(S, S.bias + kGImgB2);
+    tc_hidden_epilogue(S, g, S.bias + kGImgB2);
     tc::fence_before_sync();
-    if (__syncthreads_or(failed)) return false;
-    if (threadIdx.x == 0) tc_issue_layer<kGHid, kGOutPad>(S, kGImgW3);
+    if (wg_or(g, failed)) return false;
+    if (issuer) tc_issue_layer<kGHid, kGOutPad>(S, g, kGImgW3);
     wait();
     tc::fence_before_sync();
-    if (__syncthreads_or(failed)) return false;
+    if (wg_or(g, failed)) return false;
     tc::fence_after_sync();
-    float* out = tc_out_row(S, threadIdx.x);
-    const uint32_t t = S.tmem + ((uint32_t)(threadIdx.x & ~31) << 16);
+    float* out = tc_out_row(S, g, tc_row());
+    const uint32_t t = tc_warp_tmem(S, g);
 #pragma unroll
     for (int c0 = 0; c0 < kGOutPad; c0 += 16) {
         float v[16];

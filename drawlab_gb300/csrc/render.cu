@@ -758,9 +758,10 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 // to the stored sample when traced.  Mirror and dielectric still draw the NEE
 // sample (their eval and pdf are zero: no contribution, no shadow ray).
 //
-// kGuided (diffuse, Beckmann, GGX in a guided render): 128-thread blocks take
-// 128 queued hits at a time and evaluate the guiding network for them on the
-// tensor cores (guide_tc.cuh: tcgen05.mma, accumulators in tensor memory);
+// kGuided (diffuse, Beckmann, GGX in a guided render): blocks of two
+// warpgroups; each warpgroup takes 128 queued hits at a time and evaluates
+// the guiding network for them on the tensor cores (guide_tc.cuh:
+// tcgen05.mma, accumulators in tensor memory);
 // each path samples its next direction by one-sample MIS between the learned
 // vMF mixture (probability `fraction`) and the BSDF, weighting by
 // f cos / (fraction q + (1 - fraction) p_bsdf); NEE's MIS weight uses the
@@ -768,22 +769,23 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 constexpr size_t kGuidedSmem = sizeof(GuideTcSmem);
 
 template <int T, bool kMulti, bool kGuided>
-__global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
+__global__ void __launch_bounds__(kGuided ? kTcThreads : 128) k_material(RenderParams P, int p) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int q = p ^ 1;
     const int lane = lane_id();
     const int n = P.cnt->mat[p][T].n;
-    // guided: the block walks whole 128-row tiles (every thread takes part in
-    // the network's block-wide steps); otherwise each warp walks 32 rows
+    // guided: each warpgroup walks whole 128-row tiles (every thread takes
+    // part in the network's warpgroup-wide steps); otherwise each warp walks
+    // 32 rows
     constexpr int kSpan = kGuided ? kTcRows : 32;
     uint32_t mma_phase = 0;
     bool net_ok = false;
     if (kGuided) {
-        if ((int)blockIdx.x * kTcRows >= n) return;
+        if ((int)blockIdx.x * kTcThreads >= n) return;
         net_ok = guide_tc_begin(*reinterpret_cast<GuideTcSmem*>(dyn_smem), P.gnet.image, &P.cnt->err);
     }
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~(kSpan - 1); i0 < n; i0 += gridDim.x * blockDim.x) {
-        int i = i0 + (kGuided ? (int)threadIdx.x : lane);
+        int i = i0 + (kGuided ? tc_row() : lane);
         bool active = i < n;
         int slot = active ? P.mat_q[T][i] : 0;
         bool cont = false, emit = false, done = false;
@@ -877,12 +879,13 @@ __global__ void __launch_bounds__(128) k_material(RenderParams P, int p) {
         float* lob = nullptr;
         if (kGuided) {
             GuideTcSmem& S = *reinterpret_cast<GuideTcSmem*>(dyn_smem);
-            lob = tc_out_row(S, threadIdx.x);
+            const int grp = tc_group();
+            lob = tc_out_row(S, grp, tc_row());
             if (use_guide) guide_input(request<kMulti>(P, rid).sc, h.p, normalize(h.sh.n), in6);
             // (also the barrier after which the previous tile's lobes are dead)
-            if (__syncthreads_or(use_guide) && net_ok) {
-                encode_row_tc(in6, S.act, threadIdx.x);
-                net_ok = guide_tc_forward(S, mma_phase, &P.cnt->err);
+            if (wg_or(grp, use_guide) && net_ok) {
+                encode_row_tc(in6, S.act[grp], tc_row());
+                net_ok = guide_tc_forward(S, grp, mma_phase, &P.cnt->err);
             }
             if (!net_ok) use_guide = false;  // a wait ran out: sample the BSDF alone
             if (use_guide) decode_lobes_inplace(lob);
@@ -1219,7 +1222,7 @@ template <int T, bool kMulti>
 static void launch_material(const RenderParams& P, int p, cudaStream_t st, int wb, int th) {
     constexpr bool kCanGuide = !kMulti && T != MAT_MIRROR && T != MAT_DIELECTRIC;
     if (kCanGuide && P.guided)
-        k_material<T, false, true><<<P.gnet.blocks, kTcRows, kGuidedSmem, st>>>(P, p);
+        k_material<T, false, true><<<P.gnet.blocks, kTcThreads, kGuidedSmem, st>>>(P, p);
     else
         k_material<T, kMulti, false><<<wb, th, 0, st>>>(P, p);
 }
@@ -1557,7 +1560,7 @@ static int guided_resident_blocks() {
     cudaFuncAttributes fa;
     DL_CUDA(cudaFuncGetAttributes(&fa, fn));
     const int regs_per_warp = ((fa.numRegs + 7) / 8) * 8 * 32;
-    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcRows / 32));
+    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcThreads / 32));
     const size_t smem = kGuidedSmem + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
     const int by_smem = (int)(prop.sharedMemPerMultiprocessor / smem);
     return std::max(1, std::min(by_regs, by_smem));
