@@ -50,9 +50,17 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer(const void* image, c
         wg_sync(g);  // the previous tile's outputs have been read
         encode_row_tc(x, S.act[g], row);
         ok = guide_tc_forward(S, g, phase, err);
-        if (ok && r < n) {
-            const float* o = tc_out_row(S, g, row);
-            for (int j = 0; j < kGOut; j++) out[(size_t)r * kGOut + j] = o[j];
+        if (ok) {
+            // the tile's rows are contiguous in `out`: copy them out as
+            // consecutive 16-byte chunks (coalesced stores), 10 per row
+            wg_sync(g);
+            const int rows = min(kTcRows, n - tile * kTcRows);
+            float4* dst = reinterpret_cast<float4*>(out + (size_t)tile * kTcRows * kGOut);
+            const float* src = tc_out_row(S, g, 0);
+            for (int c = row; c < rows * (kGOut / 4); c += kTcRows) {
+                const float* q = src + (c / (kGOut / 4)) * kTcOutStride + 4 * (c % (kGOut / 4));
+                dst[c] = make_float4(q[0], q[1], q[2], q[3]);
+            }
         }
     }
     guide_tc_end(S, phase);
