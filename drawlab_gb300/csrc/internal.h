@@ -131,7 +131,7 @@ struct RenderCounters {
 // Wavefront path-state buffers, sized for the pool and reused across renders.
 struct RenderBuffers {
     int64_t capacity = 0;
-    DevBuf ray, path, meta, hit, pos;   // 32-byte path records per slot (pos: Li mode)
+    DevBuf rec, pos;   // 128-byte path record per slot (pos: Li mode)
     DevBuf ext_q[2], mat_q[kNumMaterialTypes + 1];
     DevBuf sh_o, sh_d, sh_c;
     DevBuf counters, invalid;

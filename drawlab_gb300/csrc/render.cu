@@ -63,6 +63,17 @@ struct __align__(32) HitRec {
 };
 static_assert(sizeof(RayRec) == 32 && sizeof(PathRec) == 32 && sizeof(MetaRec) == 32 && sizeof(HitRec) == 32,
               "path records are one 32-byte sector each");
+// A slot's four records share one 128-byte line: the ray and its hit in one
+// half, the path state in the other.  Slots are visited in queue order, i.e.
+// at random; a random 32-byte read costs a whole DRAM burst, so records read
+// together are kept inside one.
+struct __align__(128) SlotRec {
+    RayRec ray;
+    HitRec hit;
+    PathRec path;
+    MetaRec meta;
+};
+static_assert(sizeof(SlotRec) == 128, "one 128-byte line per slot");
 constexpr size_t kSlotBytes = 4 * 32 + 8 + 3 * 16 + 4 * (2 + kNumMaterialTypes + 1);  // records, pos, shadow, queues
 
 constexpr int kMissQueue = kNumMaterialTypes;  // queue index of rays that hit nothing
@@ -96,10 +107,7 @@ struct RenderParams {
     DevRequest r0;                 // the request of a single render
     const DevRequest* reqs;        // batch: request table (pid_first ascending)
     int num_reqs;
-    RayRec* ray;
-    PathRec* path;
-    MetaRec* meta;
-    HitRec* hit;
+    SlotRec* rec;    // per slot: ray, hit, path state
     float2* pos;     // film position of the camera sample (Li mode only)
     int* ext_q[2];
     int* mat_q[kNumMaterialTypes + 1];  // per material type, then the miss queue
@@ -199,10 +207,18 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     } else {
         unsigned long long local = pid - R.pid_first;
         unsigned long long npix = (unsigned long long)cam.w * cam.h;
-        unsigned long long pix = local % npix;
-        s = (int)(local / npix) + (kMulti ? R.spp_offset : P.cnt->pass_spp_offset);
-        x = (int)(pix % cam.w);
-        y = (int)(pix / cam.w);
+        if ((local | npix) < 0x100000000ull) {  // 32-bit division where it fits
+            const unsigned l32 = (unsigned)local, n32 = (unsigned)npix, pix = l32 % n32;
+            s = (int)(l32 / n32);
+            x = (int)(pix % (unsigned)cam.w);
+            y = (int)(pix / (unsigned)cam.w);
+        } else {
+            unsigned long long pix = local % npix;
+            s = (int)(local / npix);
+            x = (int)(pix % cam.w);
+            y = (int)(pix / cam.w);
+        }
+        s += kMulti ? R.spp_offset : P.cnt->pass_spp_offset;
     }
     Pcg32 g;
     seed_path(g, R.seed_mix, cam.w, cam.h, x, y, s);
@@ -216,15 +232,15 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
     RayRec r;
     r.o = make_float4(o.x, o.y, o.z, __int_as_float(rid));
     r.d = make_float4(d.x, d.y, d.z, tmax);
-    P.ray[slot] = r;
+    P.rec[slot].ray = r;
     PathRec pr;
     pr.tp = make_float4(1.f, 1.f, 1.f, 1.f);
     pr.L = make_float4(0.f, 0.f, 0.f, 0.f);
-    P.path[slot] = pr;
+    P.rec[slot].path = pr;
     MetaRec mr;
     mr.m = make_int4(0, PF_CAMERA | (rid << kReqShift), (int)(pid & 0xffffffffu), (int)(pid >> 32));
     mr.rng = store_rng(g);
-    P.meta[slot] = mr;
+    P.rec[slot].meta = mr;
     if (P.mode == 1) P.pos[slot] = ps;
     if (P.guided) {
         GuideRec gr;
@@ -537,7 +553,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         rd = P.sh_d[idx];
                     } else {
                         slot = P.ext_q[p][idx];
-                        RayRec r = P.ray[slot];
+                        RayRec r = P.rec[slot].ray;
                         ro = r.o;
                         rd = r.d;
                     }
@@ -627,10 +643,10 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         float4 c = P.sh_c[idx];
                         int target = __float_as_int(c.w);
                         if (target >= 0) {
-                            PathRec pr = P.path[target];
+                            PathRec pr = P.rec[target].path;
                             pr.L = make_float4(__fadd_rn(pr.L.x, c.x), __fadd_rn(pr.L.y, c.y),
                                                __fadd_rn(pr.L.z, c.z), pr.L.w);
-                            P.path[target] = pr;
+                            P.rec[target].path = pr;
                             // NEE at the newest guided vertex feeds the record before it
                             if (P.guided) credit(P, P.grec[target], xyz(c), false);
                         } else {
@@ -649,7 +665,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         hr.h = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                         dest = kMissQueue;
                     }
-                    P.hit[slot] = hr;
+                    P.rec[slot].hit = hr;
                 }
                 has = false;
             }
@@ -719,14 +735,14 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
         bool active = i < n;
         int slot = active ? P.mat_q[kMissQueue][i] : 0;
         if (active) {
-            PathRec pr = P.path[slot];
-            int4 m = P.meta[slot].m;
+            PathRec pr = P.rec[slot].path;
+            int4 m = P.rec[slot].meta.m;
             const DevRequest& R = request<kMulti>(P, m.y >> kReqShift);
             const DevScene& sc = R.sc;
             float3 L = f3(pr.L.x, pr.L.y, pr.L.z);
             // (the normals integrator returns 0 on a miss, normal.cpp:13-14)
             if (sc.env_light >= 0 && !(R.flags & DL_RENDER_NORMALS)) {
-                float3 dir = xyz(P.ray[slot].d);
+                float3 dir = xyz(P.rec[slot].ray.d);
                 if (m.y & PF_CAMERA) {
                     L = add(L, sc.env_visual ? env_lookup_dir(sc, dir) : ld3(sc.env_bg));
                 } else {
@@ -804,10 +820,10 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : 128) k_material(RenderP
         int depth = 0, flags = 0, rid = 0;
         unsigned long long pid = 0;
         if (active) {
-            float4 hit = P.hit[slot].h;
-            ray = P.ray[slot];
-            pr = P.path[slot];
-            mr = P.meta[slot];
+            float4 hit = P.rec[slot].hit.h;
+            ray = P.rec[slot].ray;
+            pr = P.rec[slot].path;
+            mr = P.rec[slot].meta;
             if (P.guided) gr = P.grec[slot];
             g = load_rng(mr.rng);
             pid = path_index(mr.m);
@@ -994,7 +1010,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : 128) k_material(RenderP
                     RayRec nr;
                     nr.o = make_float4(h.p.x, h.p.y, h.p.z, __int_as_float(rid));
                     nr.d = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
-                    P.ray[slot] = nr;
+                    P.rec[slot].ray = nr;
                     cont = true;
                     rotate = use_guide && P.grecords != nullptr;
                     record = rotate && (uint32_t)(splitmix64(pid * 64ull + (unsigned long long)depth) >> 40) <
@@ -1013,11 +1029,11 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : 128) k_material(RenderP
                 PathRec npr;
                 npr.tp = make_float4(tp.x, tp.y, tp.z, eta);
                 npr.L = make_float4(Lr.x, Lr.y, Lr.z, prev_pdf);
-                P.path[slot] = npr;
+                P.rec[slot].path = npr;
                 MetaRec nmr;
                 nmr.m = make_int4(depth, flags, mr.m.z, mr.m.w);
                 nmr.rng = store_rng(g);
-                P.meta[slot] = nmr;
+                P.rec[slot].meta = nmr;
             }
         }
         // ---- phase 4 (guided): training record of the vertex (a hashed
@@ -1195,7 +1211,7 @@ __global__ void k_resolve(const float4* film, int cols, int border, int w, int h
 void RenderBuffers::ensure(int64_t cap) {
     if (cap <= capacity) return;
     size_t c = (size_t)cap;
-    for (DevBuf* b : {&ray, &path, &meta, &hit}) b->ensure(32 * c);
+    rec.ensure(128 * c);
     pos.ensure(8 * c);
     for (DevBuf* b : {&sh_o, &sh_d, &sh_c}) b->ensure(16 * c);
     for (DevBuf* b : {&ext_q[0], &ext_q[1]}) b->ensure(4 * c);
@@ -1207,7 +1223,7 @@ void RenderBuffers::ensure(int64_t cap) {
 }
 
 size_t RenderBuffers::device_bytes() const {
-    size_t s = ray.bytes + path.bytes + meta.bytes + hit.bytes + pos.bytes + ext_q[0].bytes + ext_q[1].bytes +
+    size_t s = rec.bytes + pos.bytes + ext_q[0].bytes + ext_q[1].bytes +
                sh_o.bytes + sh_d.bytes + sh_c.bytes + counters.bytes + film.bytes + rgb.bytes + samples.bytes;
     for (int k = 0; k <= kNumMaterialTypes; k++) s += mat_q[k].bytes;
     return s;
@@ -1243,7 +1259,7 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
     if (ev) { cudaEventRecord(ev[1], st); cudaEventRecord(ev[2], st); }
     if (count) k_traverse<true, true, kMulti><<<tb, th, 0, st>>>(P, p);
     else k_traverse<false, true, kMulti><<<tb, th, 0, st>>>(P, p);
-    if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[6], st); }
+    if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[4], st); }
     if (!ev && fj) {
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
@@ -1257,23 +1273,20 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
             cudaEventRecord(fj->join_ev[i], fj->aux[i]);
             cudaStreamWaitEvent(st, fj->join_ev[i], 0);
         }
-        return;
+    } else {
+        launch_material<MAT_DIFFUSE, kMulti>(P, p, st, wb, th);
+        launch_material<MAT_MIRROR, kMulti>(P, p, st, wb, th);
+        launch_material<MAT_DIELECTRIC, kMulti>(P, p, st, wb, th);
+        launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, th);
+        launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, th);
+        if (ev) { cudaEventRecord(ev[5], st); cudaEventRecord(ev[6], st); }
+        k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
     }
-    k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
-    if (ev) { cudaEventRecord(ev[7], st); cudaEventRecord(ev[4], st); }
-    launch_material<MAT_DIFFUSE, kMulti>(P, p, st, wb, th);
-    launch_material<MAT_MIRROR, kMulti>(P, p, st, wb, th);
-    launch_material<MAT_DIELECTRIC, kMulti>(P, p, st, wb, th);
-    launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, th);
-    launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, th);
-    if (ev) cudaEventRecord(ev[5], st);
+    if (ev) cudaEventRecord(ev[7], st);
 }
 
 static void bind_pool(RenderParams& P, const RenderBuffers& B) {
-    P.ray = B.ray.as<RayRec>();
-    P.path = B.path.as<PathRec>();
-    P.meta = B.meta.as<MetaRec>();
-    P.hit = B.hit.as<HitRec>();
+    P.rec = B.rec.as<SlotRec>();
     P.pos = B.pos.as<float2>();
     P.ext_q[0] = B.ext_q[0].as<int>();
     P.ext_q[1] = B.ext_q[1].as<int>();
@@ -1791,10 +1804,7 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     char* b = static_cast<char*>(pool);
     P.cnt = reinterpret_cast<RenderCounters*>(b);
     b += kCounterBytes;
-    P.ray = reinterpret_cast<RayRec*>(b); b += 32 * c;
-    P.path = reinterpret_cast<PathRec*>(b); b += 32 * c;
-    P.meta = reinterpret_cast<MetaRec*>(b); b += 32 * c;
-    P.hit = reinterpret_cast<HitRec*>(b); b += 32 * c;
+    P.rec = reinterpret_cast<SlotRec*>(b); b += 128 * c;
     float4** f4[] = {&P.sh_o, &P.sh_d, &P.sh_c};
     for (float4** f : f4) {
         *f = reinterpret_cast<float4*>(b);
