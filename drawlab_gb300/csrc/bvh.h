@@ -50,7 +50,8 @@ struct BvhBuildOptions {
     int max_leaf_size = 4;         // SAH leaves hold at most this many triangles
     int bins = 32;
     float traversal_cost = 1.0f;
-    float intersect_cost = 1.0f;
+    float intersect_cost = 0.5f;   // a triangle test costs half a node visit (both child
+                                   // boxes) in the traversal kernels: measured best of 0.25-2
     int threads = 0;               // 0 = hardware concurrency
 };
 
