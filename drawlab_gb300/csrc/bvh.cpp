@@ -231,7 +231,7 @@ BvhResult build_bvh(const float* tris, int64_t n, const BvhBuildOptions& opt) {
             std::memcpy(t.v1, tris + 9 * id + 3, 12);
             std::memcpy(t.v2, tris + 9 * id + 6, 12);
             t.prim = id;
-            t.pad1 = t.pad2 = 0;
+            t.mat_type = t.pad2 = 0;
             res.tris.push_back(t);
             res.tri_order.push_back(id);
         }

@@ -29,13 +29,13 @@ struct alignas(16) GpuNode {
 };
 static_assert(sizeof(GpuNode) == 64, "node layout");
 
-// 48-byte triangle: v0.xyz + original triangle id (int bits), v1.xyz + 0,
-// v2.xyz + 0.
+// 48-byte triangle: v0.xyz + original triangle id (int bits), v1.xyz +
+// material type of its mesh (set by the scene), v2.xyz + 0.
 struct alignas(16) GpuTri {
     float v0[3];
     int32_t prim;
     float v1[3];
-    int32_t pad1;
+    int32_t mat_type;
     float v2[3];
     int32_t pad2;
 };

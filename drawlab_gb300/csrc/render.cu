@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     }
     uint32_t err = 0, nn = 0, nt = 0;
     bool has = false, exhausted = false;
-    int idx = 0, slot = 0, node = kDone, sp = 0, hit_tri = -1;
+    int idx = 0, slot = 0, node = kDone, sp = 0, hit_tri = -1, hit_mat = 0;
     float3 o = f3(0.f, 0.f, 0.f), d = o;
     float tmin = 0.f, tmax = 0.f, ht = 0.f, hu = 0.f, hv = 0.f;
     RayBox rb;
@@ -627,6 +627,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         hu = u;
                         hv = v;
                         hit_tri = first + k;
+                        hit_mat = __float_as_int(p1.w);  // material type of the triangle's mesh
                     }
                 }
                 if (kAny && any) {
@@ -658,9 +659,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                     hr.pad = make_float4(0.f, 0.f, 0.f, 0.f);
                     if (hit_tri >= 0) {
                         hr.h = make_float4(ht, hu, hv, __int_as_float(hit_tri));
-                        const DevScene& sc = request<kMulti>(P, rid).sc;
-                        int mesh = __ldg(sc.tri_vidx + hit_tri).w;
-                        dest = sc.materials[sc.meshes[mesh].material].type;
+                        dest = hit_mat;
                     } else {
                         hr.h = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                         dest = kMissQueue;

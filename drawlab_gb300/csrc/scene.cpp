@@ -488,6 +488,10 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     }
     S->light_pick.upload(pick, st);
 
+    // the closest-hit kernel routes a hit to its material's queue from the
+    // triangle record it has just tested (second vertex's w)
+    for (size_t k = 0; k < bvh.tris.size(); k++)
+        bvh.tris[k].mat_type = dmat[dmesh[vidx[k].w].material].type;
     S->nodes.upload(bvh.nodes, st);
     S->tris.upload(bvh.tris, st);
     S->tri_vidx.upload(vidx, st);
