@@ -487,6 +487,7 @@ constexpr int kDone = kEmptyChild;  // traversal state: ray finished
 constexpr unsigned kFetchChunk = 32;
 constexpr int kTraverseWarps = 4;  // 128 threads
 constexpr int kStage = 64;         // staged entries per warp and destination (flushed at 32)
+constexpr int kSmemStack = 8;      // top traversal-stack entries per thread kept in shared memory
 
 template <bool kCount, bool kAny, bool kMulti>
 __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
@@ -521,7 +522,21 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     RayBox rb;
     rb.idir = o;
     rb.ood = o;
-    int stack[kStackSize];
+    // traversal stack: the first kSmemStack entries in shared memory, laid out
+    // [depth][thread] so that lanes at different depths hit different banks;
+    // deeper entries in local memory
+    __shared__ int s_stack[kSmemStack][kTraverseWarps * 32];
+    int stack[kStackSize - kSmemStack];
+    int* const my_stack = &s_stack[0][threadIdx.x];
+    auto push = [&](int v) {
+        if (sp < kSmemStack) my_stack[sp * kTraverseWarps * 32] = v;
+        else stack[sp - kSmemStack] = v;
+        sp++;
+    };
+    auto pop = [&]() -> int {
+        --sp;
+        return sp < kSmemStack ? my_stack[sp * kTraverseWarps * 32] : stack[sp - kSmemStack];
+    };
     int rid = 0;  // the ray's request
     const float4* nodes = P.r0.sc.nodes;
     const float4* tris = P.r0.sc.tris;
@@ -596,14 +611,14 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 if (h0 && h1) {
                     int near = ch.x, far = ch.y;
                     if (t1 < t0) { near = ch.y; far = ch.x; }
-                    if (sp < kStackSize) stack[sp++] = far; else err |= 1u;
+                    if (sp < kStackSize) push(far); else err |= 1u;
                     node = near;
                 } else if (h0) {
                     node = ch.x;
                 } else if (h1) {
                     node = ch.y;
                 } else {
-                    node = sp > 0 ? stack[--sp] : kDone;
+                    node = sp > 0 ? pop() : kDone;
                 }
             }
             finished = node == kDone;
@@ -634,7 +649,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                     finished = true;
                     hit_tri = 0;
                 } else {
-                    node = sp > 0 ? stack[--sp] : kDone;
+                    node = sp > 0 ? pop() : kDone;
                     finished = node == kDone;
                 }
             }
