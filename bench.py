@@ -450,7 +450,7 @@ def run_batch(args):
                        "max_depth": 8, "l2_flush": "inputs larger than L2 (BVHs 2.6 GB, samples 4 GB)"},
             "gpu_launches": launches,
             "autotune": {"paths_in_flight": tune.paths_in_flight, "traverse_ctas_per_sm": tune.traverse_ctas_per_sm,
-                         "shade_ctas_per_sm": tune.shade_ctas_per_sm,
+                         "shade_ctas_per_sm": tune.shade_ctas_per_sm, "shade_threads": tune.shade_threads,
                          "iterations_per_graph": tune.iterations_per_graph, "trials": trials, "seconds": t_tune},
             "e2e": {"value": samples * args.steps / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": sum(c.width * c.height * 12 for _, _, c in reqs),

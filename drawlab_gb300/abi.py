@@ -202,7 +202,7 @@ class dl_tune_params(C.Structure):
         ("traverse_ctas_per_sm", C.c_int32),
         ("shade_ctas_per_sm", C.c_int32),
         ("iterations_per_graph", C.c_int32),
-        ("reserved", C.c_int32),
+        ("shade_threads", C.c_int32),
     ]
 
 

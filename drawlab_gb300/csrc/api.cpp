@@ -429,6 +429,7 @@ int dl_context_get_tune(const dl_context* ctx, dl_tune_params* out) {
     out->traverse_ctas_per_sm = ctx->tune.trav_ctas_per_sm;
     out->shade_ctas_per_sm = ctx->tune.shade_ctas_per_sm;
     out->iterations_per_graph = ctx->tune.iters_per_graph;
+    out->shade_threads = ctx->tune.shade_threads;
     return DL_OK;
 }
 
@@ -441,10 +442,13 @@ int dl_context_set_tune(dl_context* ctx, const dl_tune_params* t) {
         need(t->shade_ctas_per_sm >= 1 && t->shade_ctas_per_sm <= 64, "shade_ctas_per_sm out of range");
         need(t->iterations_per_graph >= 2 && t->iterations_per_graph <= 8 && t->iterations_per_graph % 2 == 0,
              "iterations_per_graph must be 2, 4, 6 or 8");
+        need(t->shade_threads == 0 || t->shade_threads == 64 || t->shade_threads == 128 || t->shade_threads == 256,
+             "shade_threads must be 64, 128 or 256 (0: 128)");
         ctx->tune.paths_in_flight = t->paths_in_flight;
         ctx->tune.trav_ctas_per_sm = t->traverse_ctas_per_sm;
         ctx->tune.shade_ctas_per_sm = t->shade_ctas_per_sm;
         ctx->tune.iters_per_graph = t->iterations_per_graph;
+        ctx->tune.shade_threads = t->shade_threads == 0 ? 128 : t->shade_threads;
     });
 }
 
@@ -485,6 +489,13 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
                    {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23});
             search([](dl::TuneParams& t, int64_t v) { t.trav_ctas_per_sm = (int)v; }, {4, 6, 8});
             search([](dl::TuneParams& t, int64_t v) { t.shade_ctas_per_sm = (int)v; }, {8, 16, 32});
+            // block size of the shading kernels at the same threads per SM
+            search(
+                [&](dl::TuneParams& t, int64_t v) {
+                    t.shade_ctas_per_sm = std::max(1, std::min(64, best.shade_ctas_per_sm * best.shade_threads / (int)v));
+                    t.shade_threads = (int)v;
+                },
+                {64, 256});
             search([](dl::TuneParams& t, int64_t v) { t.iters_per_graph = (int)v; }, {2, 4, 8});
         } catch (...) {
             ctx->tune = best;
@@ -500,6 +511,7 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
             out->traverse_ctas_per_sm = best.trav_ctas_per_sm;
             out->shade_ctas_per_sm = best.shade_ctas_per_sm;
             out->iterations_per_graph = best.iters_per_graph;
+            out->shade_threads = best.shade_threads;
         }
     });
 }

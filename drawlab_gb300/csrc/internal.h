@@ -91,6 +91,7 @@ struct TuneParams {
     int64_t paths_in_flight = (int64_t)1 << 22;
     int trav_ctas_per_sm = 8;
     int shade_ctas_per_sm = 16;
+    int shade_threads = 128;   // threads per CTA of the miss and material kernels
     int iters_per_graph = 4;
 };
 

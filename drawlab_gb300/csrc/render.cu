@@ -740,7 +740,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
 // a diffuse bounce).  Store the sample, then start new camera paths in the
 // freed slots.
 template <bool kMulti>
-__global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
+__global__ void __launch_bounds__(256) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
     const int n = P.cnt->mat[p][kMissQueue].n;
@@ -799,7 +799,7 @@ __global__ void __launch_bounds__(128) k_miss(RenderParams P, int p) {
 constexpr size_t kGuidedSmem = sizeof(GuideTcSmem);
 
 template <int T, bool kMulti, bool kGuided>
-__global__ void __launch_bounds__(kGuided ? kTcThreads : 128) k_material(RenderParams P, int p) {
+__global__ void __launch_bounds__(256) k_material(RenderParams P, int p) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int q = p ^ 1;
     const int lane = lane_id();
@@ -1266,7 +1266,7 @@ static void launch_material(const RenderParams& P, int p, cudaStream_t st, int w
 template <bool kMulti>
 static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, const TuneParams& tp,
                              bool count, cudaEvent_t* ev, const dl_context* fj) {
-    const int tb = sms * tp.trav_ctas_per_sm, wb = sms * tp.shade_ctas_per_sm, th = 128;
+    const int tb = sms * tp.trav_ctas_per_sm, wb = sms * tp.shade_ctas_per_sm, th = 128, sth = tp.shade_threads;
     if (ev) cudaEventRecord(ev[0], st);
     if (count) k_traverse<true, false, kMulti><<<tb, th, 0, st>>>(P, p);
     else k_traverse<false, false, kMulti><<<tb, th, 0, st>>>(P, p);
@@ -1277,24 +1277,24 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
     if (!ev && fj) {
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
-        k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
-        launch_material<MAT_DIFFUSE, kMulti>(P, p, fj->aux[0], wb, th);
-        launch_material<MAT_MIRROR, kMulti>(P, p, fj->aux[1], wb, th);
-        launch_material<MAT_DIELECTRIC, kMulti>(P, p, fj->aux[2], wb, th);
-        launch_material<MAT_MICROFACET, kMulti>(P, p, fj->aux[3], wb, th);
-        launch_material<MAT_ANISO_GGX, kMulti>(P, p, fj->aux[4], wb, th);
+        k_miss<kMulti><<<wb, sth, 0, st>>>(P, p);
+        launch_material<MAT_DIFFUSE, kMulti>(P, p, fj->aux[0], wb, sth);
+        launch_material<MAT_MIRROR, kMulti>(P, p, fj->aux[1], wb, sth);
+        launch_material<MAT_DIELECTRIC, kMulti>(P, p, fj->aux[2], wb, sth);
+        launch_material<MAT_MICROFACET, kMulti>(P, p, fj->aux[3], wb, sth);
+        launch_material<MAT_ANISO_GGX, kMulti>(P, p, fj->aux[4], wb, sth);
         for (int i = 0; i < dl_context::kAux; i++) {
             cudaEventRecord(fj->join_ev[i], fj->aux[i]);
             cudaStreamWaitEvent(st, fj->join_ev[i], 0);
         }
     } else {
-        launch_material<MAT_DIFFUSE, kMulti>(P, p, st, wb, th);
-        launch_material<MAT_MIRROR, kMulti>(P, p, st, wb, th);
-        launch_material<MAT_DIELECTRIC, kMulti>(P, p, st, wb, th);
-        launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, th);
-        launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, th);
+        launch_material<MAT_DIFFUSE, kMulti>(P, p, st, wb, sth);
+        launch_material<MAT_MIRROR, kMulti>(P, p, st, wb, sth);
+        launch_material<MAT_DIELECTRIC, kMulti>(P, p, st, wb, sth);
+        launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, sth);
+        launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, sth);
         if (ev) { cudaEventRecord(ev[5], st); cudaEventRecord(ev[6], st); }
-        k_miss<kMulti><<<wb, th, 0, st>>>(P, p);
+        k_miss<kMulti><<<wb, sth, 0, st>>>(P, p);
     }
     if (ev) cudaEventRecord(ev[7], st);
 }

@@ -362,14 +362,15 @@ typedef struct dl_request {
 int dl_render_batch(dl_context* ctx, const dl_request* reqs, int32_t n);
 
 /* Launch shape of the wavefront renderer: path slots in flight (the pool),
- * resident CTAs per SM of the traversal kernels and of the shading kernels,
+ * CTAs per SM of the traversal kernels and of the shading kernels, threads
+ * per CTA of the shading kernels (the miss and the material kernels),
  * wavefront iterations per captured graph launch (between queue checks). */
 typedef struct dl_tune_params {
     int64_t paths_in_flight;        /* 32 .. 2^28; opts.max_paths_in_flight overrides */
     int32_t traverse_ctas_per_sm;   /* 1 .. 16 */
     int32_t shade_ctas_per_sm;      /* 1 .. 64 */
     int32_t iterations_per_graph;   /* 2, 4, 6 or 8 */
-    int32_t reserved;
+    int32_t shade_threads;          /* 64, 128 or 256; 0 = 128 */
 } dl_tune_params;
 int dl_context_get_tune(const dl_context* ctx, dl_tune_params* out);
 int dl_context_set_tune(dl_context* ctx, const dl_tune_params* tune);
@@ -377,7 +378,8 @@ int dl_context_set_tune(dl_context* ctx, const dl_tune_params* tune);
 /* Autotuner: renders the requests at `trial_spp` samples per pixel each (0:
  * an eighth of each request's spp, at least 1) under candidate launch shapes
  * -- a coordinate search over the pool size, then the traversal and shading
- * grid sizes, then the graph length -- times each on the GPU, and keeps the
+ * grid sizes, the shading block size, then the graph length -- times each
+ * on the GPU, and keeps the
  * fastest on the context.  `out` (may be NULL) receives it; `trials` (may be
  * NULL) the number of shapes timed.  Outputs of the requests are not written. */
 int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t trial_spp, dl_tune_params* out,

@@ -47,12 +47,16 @@ def test_batch_in_several_passes(ctx):
 def test_autotune_keeps_a_valid_shape(ctx):
     items = small_batch(ctx)
     t, trials = ctx.autotune(items, trial_spp=2)
-    assert trials == 15
+    assert trials == 17
     assert t.paths_in_flight in (1 << 20, 1 << 21, 1 << 22, 1 << 23)
-    assert t.traverse_ctas_per_sm in (4, 6, 8) and t.shade_ctas_per_sm in (8, 16, 32)
+    assert t.traverse_ctas_per_sm in (4, 6, 8)
+    # shading block size is searched at the same threads per SM
+    assert t.shade_threads in (64, 128, 256)
+    assert t.shade_ctas_per_sm * t.shade_threads in (8 * 128, 16 * 128, 32 * 128)
     assert t.iterations_per_graph in (2, 4, 8)
     g = ctx.get_tune()
-    assert (g.paths_in_flight, g.iterations_per_graph) == (t.paths_in_flight, t.iterations_per_graph)
+    assert (g.paths_in_flight, g.iterations_per_graph, g.shade_threads) == (
+        t.paths_in_flight, t.iterations_per_graph, t.shade_threads)
     # images do not depend on the launch shape
     for (s, o), img in zip(items, ctx.render_batch(items)):
         np.testing.assert_array_equal(img, s.render(o))
@@ -60,6 +64,17 @@ def test_autotune_keeps_a_valid_shape(ctx):
                              iterations_per_graph=3)
     with pytest.raises(api.DrawlabError):
         ctx.set_tune(bad)
+    bad = abi.dl_tune_params(paths_in_flight=64, traverse_ctas_per_sm=8, shade_ctas_per_sm=16,
+                             iterations_per_graph=4, shade_threads=96)
+    with pytest.raises(api.DrawlabError):
+        ctx.set_tune(bad)
+    # every shading block size renders the same image
+    s, o = items[0]
+    ref = ctx.render_batch([(s, o)])[0]
+    for th in (64, 256):
+        ctx.set_tune(abi.dl_tune_params(paths_in_flight=1 << 20, traverse_ctas_per_sm=8, shade_ctas_per_sm=16,
+                                        iterations_per_graph=4, shade_threads=th))
+        np.testing.assert_array_equal(ctx.render_batch([(s, o)])[0], ref)
     ctx.set_tune(abi.dl_tune_params(paths_in_flight=1 << 22, traverse_ctas_per_sm=8, shade_ctas_per_sm=16,
                                     iterations_per_graph=4))
 
