@@ -110,6 +110,7 @@ int dl_context_create(int device, dl_context** out) {
             DL_CUDA(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming));
         }
         DL_CUDA(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+        dl::render_setup_device();
     });
     if (rc != DL_OK) {
         delete ctx;

@@ -1089,15 +1089,22 @@ __global__ void __launch_bounds__(256) k_material(RenderParams P, int p) {
 
 // Film accumulation as a gather (the reference splats each sample with
 // ImageBlock::put, src/core/bitmap/block.cpp:81-113).  One block owns a
-// 16x16 tile of film pixels; it stages the samples of the 20x20 image pixels
-// around it (radiance from the sample buffer, film position recomputed from
-// the path's pcg32 stream: its first 2D draw) in shared memory together with
-// their 5 x and 5 y filter weights (the reference's table lookup), then every
-// thread sums the weighted samples of its 5x5 neighbourhood in a fixed order:
-// no atomics, bit-reproducible films.  Samples the film rejects (NaN, Inf or
-// negative: ImageBlock::put block.cpp:82-88) get zero weight and are counted.
-constexpr int kFilmTile = 16, kFilmApron = 2, kFilmRegion = kFilmTile + 2 * kFilmApron, kFilmStage = 2;
+// 32x32 tile of film pixels; per sample index it stages the samples of the
+// 36x36 image pixels around it (radiance from the sample buffer, film
+// position recomputed from the path's pcg32 stream: its first 2D draw) in
+// shared memory together with their 5 x and 5 y filter weights (the
+// reference's table lookup).  Each thread then owns four film pixels of one
+// column and sums the weighted samples of their 5x5 neighbourhoods; a staged
+// sample's radiance and x weight are read once for all four.  Every pixel
+// sums in a fixed order (sample index, then row, then column): no atomics,
+// bit-reproducible films.  Samples the film rejects (NaN, Inf or negative:
+// ImageBlock::put block.cpp:82-88) get zero weight and are counted.
+constexpr int kFilmTile = 32, kFilmApron = 2, kFilmRegion = kFilmTile + 2 * kFilmApron, kFilmRows = 4;
 constexpr int kFilmCells = kFilmRegion * kFilmRegion;
+constexpr int kFilmTaps = 2 * kFilmApron + 1;  // 5 film pixels per axis around a sample
+constexpr int kFilmThreads = kFilmTile * kFilmTile / kFilmRows;
+// staged per cell: r, g, b, 5 x weights, 5 y weights
+constexpr size_t kFilmSmem = (size_t)(3 + 2 * kFilmTaps) * kFilmCells * sizeof(float);
 
 struct FilmParams {
     float4* film;
@@ -1112,32 +1119,35 @@ struct FilmParams {
     int accumulate;       // add to the film instead of overwriting it
 };
 
-__global__ void __launch_bounds__(256) k_film_gather(FilmParams F) {
-    constexpr int kTaps = 2 * kFilmApron + 1;  // 5 film pixels per axis around a sample
-    constexpr int kN = kFilmStage * kFilmCells;
-    __shared__ float s_r[kN], s_g[kN], s_b[kN];
-    __shared__ float s_wx[kTaps][kN], s_wy[kTaps][kN];
+__global__ void __launch_bounds__(kFilmThreads) k_film_gather(FilmParams F) {
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
+    float* const s_r = reinterpret_cast<float*>(dyn_smem);
+    float* const s_g = s_r + kFilmCells;
+    float* const s_b = s_g + kFilmCells;
+    float* const s_wx = s_b + kFilmCells;               // [kFilmTaps][kFilmCells]
+    float* const s_wy = s_wx + kFilmTaps * kFilmCells;  // [kFilmTaps][kFilmCells]
     __shared__ float s_table[33];
     __shared__ unsigned int s_invalid;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int tx = threadIdx.x % kFilmTile, ty = threadIdx.x / kFilmTile;  // column, group of 4 rows
     const int X0 = blockIdx.x * kFilmTile, Y0 = blockIdx.y * kFilmTile;
-    const int X = X0 + tx, Y = Y0 + ty;
+    const int X = X0 + tx, Yb = Y0 + kFilmRows * ty;
     const int IX0 = X0 - F.border - kFilmApron, IY0 = Y0 - F.border - kFilmApron;
     const size_t npix = (size_t)F.w * F.h;
     if (threadIdx.x < 33) s_table[threadIdx.x] = F.table[threadIdx.x];
     if (threadIdx.x == 0) s_invalid = 0;
     __syncthreads();
-    float ar = 0.f, ag = 0.f, ab = 0.f, aw = 0.f;
-    for (int k0 = 0; k0 < F.nspp; k0 += kFilmStage) {
-        for (int e = threadIdx.x; e < kN; e += blockDim.x) {
-            int kk = e / kFilmCells, r = e - kk * kFilmCells;
-            int rx = r % kFilmRegion, ry = r / kFilmRegion;
-            int sx = IX0 + rx, sy = IY0 + ry;
+    float ar[kFilmRows], ag[kFilmRows], ab[kFilmRows], aw[kFilmRows];
+#pragma unroll
+    for (int j = 0; j < kFilmRows; j++) ar[j] = ag[j] = ab[j] = aw[j] = 0.f;
+    for (int k = 0; k < F.nspp; k++) {
+        for (int e = threadIdx.x; e < kFilmCells; e += kFilmThreads) {
+            const int rx = e % kFilmRegion, ry = e / kFilmRegion;
+            const int sx = IX0 + rx, sy = IY0 + ry;
             float L0 = 0.f, L1 = 0.f, L2 = 0.f;
             bool ok = false;
             float px = 0.f, py = 0.f;
-            if (k0 + kk < F.nspp && sx >= 0 && sx < F.w && sy >= 0 && sy < F.h) {
-                float4 L = F.samples[(size_t)(k0 + kk) * npix + (size_t)sy * F.w + sx];
+            if (sx >= 0 && sx < F.w && sy >= 0 && sy < F.h) {
+                float4 L = F.samples[(size_t)k * npix + (size_t)sy * F.w + sx];
                 ok = L.w != 0.f && L.x >= 0.f && L.y >= 0.f && L.z >= 0.f && isfinite(L.x) && isfinite(L.y) &&
                      isfinite(L.z);
                 // each sample is counted by the tile that owns its pixel
@@ -1146,7 +1156,7 @@ __global__ void __launch_bounds__(256) k_film_gather(FilmParams F) {
                     atomicAdd(&s_invalid, 1u);
                 if (ok) {
                     Pcg32 g;
-                    seed_path(g, F.seed_mix, F.w, F.h, sx, sy, F.s_first + k0 + kk);
+                    seed_path(g, F.seed_mix, F.w, F.h, sx, sy, F.s_first + k);
                     float2 ps = g.next2d();
                     float fx = __fadd_rn((float)sx, ps.x), fy = __fadd_rn((float)sy, ps.y);
                     px = __fsub_rn(__fsub_rn(fx, 0.5f), (float)(-F.border));
@@ -1161,47 +1171,61 @@ __global__ void __launch_bounds__(256) k_film_gather(FilmParams F) {
             s_b[e] = L2;
             // weights of this sample for film columns X0 + rx - d and rows Y0 + ry - d
 #pragma unroll
-            for (int d = 0; d < kTaps; d++) {
+            for (int d = 0; d < kFilmTaps; d++) {
                 int cx = X0 + rx - d, cy = Y0 + ry - d;
                 float wx = 0.f, wy = 0.f;
                 if (ok && cx >= 0 && cx < F.cols)
                     wx = s_table[min((int)__fmul_rn(fabsf(__fsub_rn((float)cx, px)), F.lookup), 32)];
                 if (ok && cy >= 0 && cy < F.rows)
                     wy = s_table[min((int)__fmul_rn(fabsf(__fsub_rn((float)cy, py)), F.lookup), 32)];
-                s_wx[d][e] = wx;
-                s_wy[d][e] = wy;
+                s_wx[d * kFilmCells + e] = wx;
+                s_wy[d * kFilmCells + e] = wy;
             }
         }
         __syncthreads();
-        if (X < F.cols && Y < F.rows) {
-            for (int kk = 0; kk < kFilmStage; kk++) {
-                const int base = kk * kFilmCells;
+        // region rows kFilmRows*ty + r reach this thread's pixel j when
+        // dy = r - j is a filter tap; per pixel the order is dy, then dx
 #pragma unroll
-                for (int dy = 0; dy < kTaps; dy++) {
+        for (int r = 0; r < kFilmRows + kFilmTaps - 1; r++) {
 #pragma unroll
-                    for (int dx = 0; dx < kTaps; dx++) {
-                        int c = base + (ty + dy) * kFilmRegion + (tx + dx);
-                        float wx = s_wx[dx][c], wy = s_wy[dy][c];
-                        ar = __fadd_rn(ar, __fmul_rn(__fmul_rn(s_r[c], wx), wy));
-                        ag = __fadd_rn(ag, __fmul_rn(__fmul_rn(s_g[c], wx), wy));
-                        ab = __fadd_rn(ab, __fmul_rn(__fmul_rn(s_b[c], wx), wy));
-                        aw = __fadd_rn(aw, __fmul_rn(wx, wy));
-                    }
+            for (int dx = 0; dx < kFilmTaps; dx++) {
+                const int c = (kFilmRows * ty + r) * kFilmRegion + tx + dx;
+                const float R = s_r[c], G = s_g[c], B = s_b[c], wx = s_wx[dx * kFilmCells + c];
+#pragma unroll
+                for (int j = 0; j < kFilmRows; j++) {
+                    const int dy = r - j;
+                    if (dy < 0 || dy >= kFilmTaps) continue;
+                    const float wy = s_wy[dy * kFilmCells + c];
+                    ar[j] = __fadd_rn(ar[j], __fmul_rn(__fmul_rn(R, wx), wy));
+                    ag[j] = __fadd_rn(ag[j], __fmul_rn(__fmul_rn(G, wx), wy));
+                    ab[j] = __fadd_rn(ab[j], __fmul_rn(__fmul_rn(B, wx), wy));
+                    aw[j] = __fadd_rn(aw[j], __fmul_rn(wx, wy));
                 }
             }
         }
         __syncthreads();
     }
     if (threadIdx.x == 0 && s_invalid) atomicAdd(F.invalid, (unsigned long long)s_invalid);
-    if (X < F.cols && Y < F.rows) {
+    if (X >= F.cols) return;
+#pragma unroll
+    for (int j = 0; j < kFilmRows; j++) {
+        const int Y = Yb + j;
+        if (Y >= F.rows) break;
         float4* o = F.film + (size_t)Y * F.cols + X;
         if (F.accumulate) {
             float4 c = *o;
-            *o = make_float4(__fadd_rn(c.x, ar), __fadd_rn(c.y, ag), __fadd_rn(c.z, ab), __fadd_rn(c.w, aw));
+            *o = make_float4(__fadd_rn(c.x, ar[j]), __fadd_rn(c.y, ag[j]), __fadd_rn(c.z, ab[j]),
+                             __fadd_rn(c.w, aw[j]));
         } else {
-            *o = make_float4(ar, ag, ab, aw);
+            *o = make_float4(ar[j], ag[j], ab[j], aw[j]);
         }
     }
+}
+
+// Per device, once per context: kernels whose shared memory exceeds the
+// default 48 KB limit.
+void render_setup_device() {
+    DL_CUDA(cudaFuncSetAttribute(k_film_gather, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFilmSmem));
 }
 
 // film -> rgb (ImageBlock::toBitmap, block.cpp:58-66)
@@ -1550,7 +1574,7 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
             F.nspp = ns;
             F.s_first = o.spp_offset + s0;
             F.accumulate = s0 > 0;
-            k_film_gather<<<fgrid, 256, 0, st>>>(F);
+            k_film_gather<<<fgrid, kFilmThreads, kFilmSmem, st>>>(F);
             launches += 1;
             DL_CUDA(cudaGetLastError());
         }
@@ -1666,7 +1690,7 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
         F.nspp = ns;
         F.s_first = o.spp_offset + done;
         F.accumulate = done > 0;
-        k_film_gather<<<fgrid, 256, 0, st>>>(F);
+        k_film_gather<<<fgrid, kFilmThreads, kFilmSmem, st>>>(F);
         launches += 1;
         DL_CUDA(cudaGetLastError());
         done += ns;
@@ -1783,7 +1807,7 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
             F.s_first = hreq[a].spp_offset;
             F.accumulate = done[r] > 0;
             dim3 fgrid((F.cols + kFilmTile - 1) / kFilmTile, (F.rows + kFilmTile - 1) / kFilmTile);
-            k_film_gather<<<fgrid, 256, 0, st>>>(F);
+            k_film_gather<<<fgrid, kFilmThreads, kFilmSmem, st>>>(F);
             launches += 1;
             DL_CUDA(cudaGetLastError());
             done[r] += ns[a];

@@ -19,6 +19,8 @@ int64_t film_floats(int w, int h, int filter);
 void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys, float* d_L,
                 float* d_pos, bool count_traversal, RenderCounters* out_counters);
 void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb);
+// One-time kernel attributes of the current device (called by context creation).
+void render_setup_device();
 
 // One request of a batch: scene, options, device film (film_floats sized).
 struct BatchItem {
