@@ -739,8 +739,8 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
 // background colour; later rays weight it by MIS against the BSDF pdf after
 // a diffuse bounce).  Store the sample, then start new camera paths in the
 // freed slots.
-template <bool kMulti>
-__global__ void __launch_bounds__(256) k_miss(RenderParams P, int p) {
+template <bool kMulti, int kThreads>
+__global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
     const int n = P.cnt->mat[p][kMissQueue].n;
@@ -798,8 +798,8 @@ __global__ void __launch_bounds__(256) k_miss(RenderParams P, int p) {
 // same combined pdf.  The vertex becomes a training record.
 constexpr size_t kGuidedSmem = sizeof(GuideTcSmem);
 
-template <int T, bool kMulti, bool kGuided>
-__global__ void __launch_bounds__(256) k_material(RenderParams P, int p) {
+template <int T, bool kMulti, bool kGuided, int kThreads>
+__global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(RenderParams P, int p) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int q = p ^ 1;
     const int lane = lane_id();
@@ -1276,9 +1276,19 @@ template <int T, bool kMulti>
 static void launch_material(const RenderParams& P, int p, cudaStream_t st, int wb, int th) {
     constexpr bool kCanGuide = !kMulti && T != MAT_MIRROR && T != MAT_DIELECTRIC;
     if (kCanGuide && P.guided)
-        k_material<T, false, true><<<P.gnet.blocks, kTcThreads, kGuidedSmem, st>>>(P, p);
+        k_material<T, false, true, kTcThreads><<<P.gnet.blocks, kTcThreads, kGuidedSmem, st>>>(P, p);
+    else if (th > 128)  // compiled for 256-thread blocks
+        k_material<T, kMulti, false, 256><<<wb, th, 0, st>>>(P, p);
     else
-        k_material<T, kMulti, false><<<wb, th, 0, st>>>(P, p);
+        k_material<T, kMulti, false, 128><<<wb, th, 0, st>>>(P, p);
+}
+
+template <bool kMulti>
+static void launch_miss(const RenderParams& P, int p, cudaStream_t st, int wb, int th) {
+    if (th > 128)
+        k_miss<kMulti, 256><<<wb, th, 0, st>>>(P, p);
+    else
+        k_miss<kMulti, 128><<<wb, th, 0, st>>>(P, p);
 }
 
 // Launches one wavefront iteration (8 kernels) with the context's launch
@@ -1301,7 +1311,7 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
     if (!ev && fj) {
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
-        k_miss<kMulti><<<wb, sth, 0, st>>>(P, p);
+        launch_miss<kMulti>(P, p, st, wb, sth);
         launch_material<MAT_DIFFUSE, kMulti>(P, p, fj->aux[0], wb, sth);
         launch_material<MAT_MIRROR, kMulti>(P, p, fj->aux[1], wb, sth);
         launch_material<MAT_DIELECTRIC, kMulti>(P, p, fj->aux[2], wb, sth);
@@ -1318,7 +1328,7 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
         launch_material<MAT_MICROFACET, kMulti>(P, p, st, wb, sth);
         launch_material<MAT_ANISO_GGX, kMulti>(P, p, st, wb, sth);
         if (ev) { cudaEventRecord(ev[5], st); cudaEventRecord(ev[6], st); }
-        k_miss<kMulti><<<wb, sth, 0, st>>>(P, p);
+        launch_miss<kMulti>(P, p, st, wb, sth);
     }
     if (ev) cudaEventRecord(ev[7], st);
 }
@@ -1601,7 +1611,7 @@ void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_
 // limit (before any graph capture).
 template <int T>
 static int guided_resident_blocks() {
-    auto* fn = k_material<T, false, true>;
+    auto* fn = k_material<T, false, true, kTcThreads>;
     DL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGuidedSmem));
     DL_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int dev = 0;
