@@ -50,7 +50,7 @@ NODE_BYTES, TRI_BYTES, RAY_IN, HIT_OUT = 64, 48, 32, 16
 # from one ncu capture of the full-size launch list (dram__bytes_read.sum +
 # dram__bytes_write.sum over the 374 extension launches of that capture /
 # 374); a profile measurement, not a live one.
-TRAVERSE_DRAM_BYTES_PER_LAUNCH = (180.54e9 + 39.95e9) / 374
+TRAVERSE_DRAM_BYTES_PER_LAUNCH = (172.2e9 + 38.3e9) / 374
 
 
 def peaks():
