@@ -808,6 +808,10 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
     // part in the network's warpgroup-wide steps); otherwise each warp walks
     // 32 rows
     constexpr int kSpan = kGuided ? kTcRows : 32;
+    // training-record bookkeeping: guided kernels, and mirror / dielectric
+    // hits of a guided render (the other types then run their guided kernel)
+    constexpr bool kMayGuide = kGuided || (!kMulti && (T == MAT_MIRROR || T == MAT_DIELECTRIC));
+    const bool guided = kMayGuide && P.guided;
     uint32_t mma_phase = 0;
     bool net_ok = false;
     if (kGuided) {
@@ -838,7 +842,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
             ray = P.rec[slot].ray;
             pr = P.rec[slot].path;
             mr = P.rec[slot].meta;
-            if (P.guided) gr = P.grec[slot];
+            if (guided) gr = P.grec[slot];
             g = load_rng(mr.rng);
             pid = path_index(mr.m);
             tp = f3(pr.tp.x, pr.tp.y, pr.tp.z);
@@ -891,7 +895,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
                     float w = (flags & PF_PREV_DIFFUSE) ? mis_weight(pr.L.w, ep) : 1.f;
                     float3 c = mul(scale(tp, w), le);
                     Lr = add(Lr, c);
-                    if (P.guided) credit(P, gr, c, true);
+                    if (guided) credit(P, gr, c, true);
                 }
                 if (depth > R.rr_depth) {
                     float pq = fminf(maxc(scale(scale(tp, eta), eta)), 0.99f);
