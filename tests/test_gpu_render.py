@@ -132,6 +132,23 @@ def test_normals_render_matches_oracle(ctx):
     assert rg.max() <= 1.0 + 1e-5 and rg.mean() > 0.1
 
 
+@pytest.mark.parametrize("w,h,filt", [(37, 23, abi.DL_FILTER_GAUSSIAN), (33, 5, abi.DL_FILTER_BOX),
+                                      (1, 1, abi.DL_FILTER_GAUSSIAN), (70, 35, abi.DL_FILTER_BOX)])
+def test_film_edges_match_oracle(ctx, w, h, filt):
+    # film sizes that leave partial 32x32 tiles and partial 4-row groups
+    sc = scenes.cornell(width=w, height=h)
+    gs = api.Scene.from_data(ctx, sc)
+    orc = po.OracleScene(sc, filter=filt)
+    opts = abi.make_opts(spp=3, max_depth=4, seed=11, filter=filt)
+    fg = gs.render_film(opts)
+    _, fo, _ = orc.render_paths(opts, film=True)
+    assert fg.shape == fo.shape
+    np.testing.assert_allclose(fg[..., 3], fo[..., 3], rtol=2e-5, atol=1e-6)
+    # radiance: per-path float differences between the two renderers only
+    rel = np.abs(fg[..., :3] - fo[..., :3]) / (np.abs(fo[..., :3]) + 1e-2)
+    assert np.mean(rel < 1e-3) > 0.9
+
+
 def test_film_matches_oracle_per_path_render(ctx):
     sc = scenes.cornell(width=64, height=64)
     gs = api.Scene.from_data(ctx, sc)
