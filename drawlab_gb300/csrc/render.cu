@@ -508,9 +508,9 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
             P.cnt->shadow[q] = 0;
             P.cnt->stat_ext += (unsigned long long)n;
         } else {
-            // next iteration's material queues and extend cursor start empty
+            // next iteration's material queues start empty (the extension
+            // traversal, which may run concurrently, appends to mat[p])
             for (int k = 0; k <= kNumMaterialTypes; k++) P.cnt->mat[q][k].n = 0;
-            P.cnt->work_ext = 0;
             P.cnt->stat_shadow += (unsigned long long)n;
         }
     }
@@ -742,7 +742,10 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
 template <bool kMulti, int kThreads>
 __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
     const int q = p ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.cnt->work_sh = 0;  // next iteration's shadow cursor
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // next iteration's traversal cursors (both traversals are done)
+        P.cnt->work_ext = 0;
+        P.cnt->work_sh = 0;
+    }
     const int n = P.cnt->mat[p][kMissQueue].n;
     for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
         int i = i0 + lane_id();
@@ -1298,20 +1301,37 @@ static void launch_miss(const RenderParams& P, int p, cudaStream_t st, int wb, i
 // Launches one wavefront iteration (8 kernels) with the context's launch
 // shape.  `ev`, when given, holds 8 events bracketing extend, shadow, the
 // material kernels, miss (kernels then run one after another).  Otherwise,
-// with `fj` given, the miss kernel and the five material kernels (disjoint
-// slots and queues) run concurrently on the context's side streams, joined
-// before the next iteration.
+// with `fj` given, independent kernels run concurrently on the context's
+// side streams: the extension traversal (this iteration's rays: reads their
+// ray records, writes hit records) beside the shadow traversal (the previous
+// iteration's NEE rays: adds to path records), then the miss kernel beside
+// the five material kernels (disjoint slots and queues), joined before the
+// next iteration.
 template <bool kMulti>
 static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int sms, const TuneParams& tp,
                              bool count, cudaEvent_t* ev, const dl_context* fj) {
     const int tb = sms * tp.trav_ctas_per_sm, wb = sms * tp.shade_ctas_per_sm, th = 128, sth = tp.shade_threads;
-    if (ev) cudaEventRecord(ev[0], st);
-    if (count) k_traverse<true, false, kMulti><<<tb, th, 0, st>>>(P, p);
-    else k_traverse<false, false, kMulti><<<tb, th, 0, st>>>(P, p);
-    if (ev) { cudaEventRecord(ev[1], st); cudaEventRecord(ev[2], st); }
-    if (count) k_traverse<true, true, kMulti><<<tb, th, 0, st>>>(P, p);
-    else k_traverse<false, true, kMulti><<<tb, th, 0, st>>>(P, p);
-    if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[4], st); }
+    if (!ev && fj) {
+        cudaEventRecord(fj->fork_ev, st);
+        cudaStreamWaitEvent(fj->aux[0], fj->fork_ev, 0);
+        if (count) {
+            k_traverse<true, false, kMulti><<<tb, th, 0, st>>>(P, p);
+            k_traverse<true, true, kMulti><<<tb, th, 0, fj->aux[0]>>>(P, p);
+        } else {
+            k_traverse<false, false, kMulti><<<tb, th, 0, st>>>(P, p);
+            k_traverse<false, true, kMulti><<<tb, th, 0, fj->aux[0]>>>(P, p);
+        }
+        cudaEventRecord(fj->join_ev[0], fj->aux[0]);
+        cudaStreamWaitEvent(st, fj->join_ev[0], 0);
+    } else {
+        if (ev) cudaEventRecord(ev[0], st);
+        if (count) k_traverse<true, false, kMulti><<<tb, th, 0, st>>>(P, p);
+        else k_traverse<false, false, kMulti><<<tb, th, 0, st>>>(P, p);
+        if (ev) { cudaEventRecord(ev[1], st); cudaEventRecord(ev[2], st); }
+        if (count) k_traverse<true, true, kMulti><<<tb, th, 0, st>>>(P, p);
+        else k_traverse<false, true, kMulti><<<tb, th, 0, st>>>(P, p);
+        if (ev) { cudaEventRecord(ev[3], st); cudaEventRecord(ev[4], st); }
+    }
     if (!ev && fj) {
         cudaEventRecord(fj->fork_ev, st);
         for (int i = 0; i < dl_context::kAux; i++) cudaStreamWaitEvent(fj->aux[i], fj->fork_ev, 0);
