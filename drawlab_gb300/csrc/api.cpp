@@ -562,7 +562,12 @@ int dl_guide_create(dl_context* ctx, const dl_guide_config* cfg, dl_guide** out)
         G->w16.ensure(dl::kGuideParams * 2);
         G->image.ensure(dl::kGuideImageBytes);
         G->scratch.ensure(256);
-        DL_CUDA(cudaStreamCreateWithFlags(&G->train_stream, cudaStreamNonBlocking));
+        // training overlaps the next render pass; at the highest priority its
+        // few short kernels are scheduled ahead of the pass's blocks, so the
+        // pass samples with the updated network early on
+        int lo_prio = 0, hi_prio = 0;
+        DL_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+        DL_CUDA(cudaStreamCreateWithPriority(&G->train_stream, cudaStreamNonBlocking, hi_prio));
         for (int k = 0; k < 2; k++) {
             DL_CUDA(cudaEventCreateWithFlags(&G->pass_done[k], cudaEventDisableTiming));
             DL_CUDA(cudaEventCreateWithFlags(&G->train_done[k], cudaEventDisableTiming));

@@ -49,6 +49,17 @@ def test_guided_room_mean_matches_plain(ctx):
     assert abs(got - ref) / ref < 0.08, (got, ref)
 
 
+def test_guided_render_is_reproducible(ctx):
+    # a frozen network: every path's value depends only on its seed, so two
+    # renders are bit-identical whatever order the concurrent kernels take
+    gs = api.Scene.from_data(ctx, room(64, 36))
+    g = api.Guide(ctx, seed=4)
+    opts = abi.make_opts(spp=32, max_depth=12, seed=3)
+    a = gs.render_guided(opts, g, train=False)
+    b = gs.render_guided(opts, g, train=False)
+    np.testing.assert_array_equal(a, b)
+
+
 def test_training_changes_the_network(ctx):
     gs = api.Scene.from_data(ctx, room(32, 18))
     g = api.Guide(ctx, seed=7)
