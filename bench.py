@@ -361,7 +361,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (procedural scene, seed 2; no scene files ship with the reference)",
             "config": dict(WORKLOAD, spp=spp, l2_flush="256 MB buffer written between timed steps",
-                           paths_in_flight=min(1 << 22, W * H * spp), parallelism="replicas" if ws > 1 else "single"),
+                           paths_in_flight=min(ctx.get_tune().paths_in_flight, W * H * spp),
+                           parallelism="replicas" if ws > 1 else "single"),
             "mrays_per_s": mrays,
             "rays": {"camera": cam_rays, "extension": ext_rays, "shadow": sh_rays},
             "wall_s": wall,

@@ -487,7 +487,8 @@ int dl_autotune(dl_context* ctx, const dl_request* reqs, int32_t n, int32_t tria
                 }
             };
             search([](dl::TuneParams& t, int64_t v) { t.paths_in_flight = v; },
-                   {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23});
+                   {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23, (int64_t)1 << 24,
+                    (int64_t)1 << 25});
             search([](dl::TuneParams& t, int64_t v) { t.trav_ctas_per_sm = (int)v; }, {4, 6, 8});
             search([](dl::TuneParams& t, int64_t v) { t.shade_ctas_per_sm = (int)v; }, {8, 16, 32});
             // block size of the shading kernels at the same threads per SM

@@ -88,11 +88,13 @@ constexpr int kNumMaterialTypes = 5;
 // otherwise): path slots in flight, resident CTAs per SM of the traversal
 // kernels and of the shading kernels, iterations per captured graph (even).
 struct TuneParams {
-    int64_t paths_in_flight = (int64_t)1 << 22;
+    // 32M slots (6.9 GB of path state; a render uses at most one slot per
+    // path): fewer, fuller wavefront iterations per frame
+    int64_t paths_in_flight = (int64_t)1 << 25;
     int trav_ctas_per_sm = 8;
     int shade_ctas_per_sm = 16;
     int shade_threads = 128;   // threads per CTA of the miss and material kernels
-    int iters_per_graph = 4;
+    int iters_per_graph = 8;
 };
 
 // A queue length that kernels bump with atomics, alone in its 128-byte line:
