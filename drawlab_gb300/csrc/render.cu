@@ -458,15 +458,19 @@ __device__ __forceinline__ float3 sample_emitter(const DevRequest& R, float3 its
 }
 
 // ---------------------------------------------------------------- kernels
+// First camera paths of a pass: slot i starts path i (no claiming needed),
+// and the extension queue lists the started slots in order.
 template <bool kMulti>
 __global__ void k_init(RenderParams P, int capacity) {
-    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < capacity;
-         i0 += gridDim.x * blockDim.x) {
-        int slot = i0 + lane_id();
-        bool active = slot < capacity;
-        bool ok = regenerate<kMulti>(P, slot, active);
-        int e = warp_push(&P.cnt->ext[0], ok);
-        if (ok) P.ext_q[0][e] = slot;
+    const unsigned long long total = P.cnt->pass_total;
+    const int n = (int)min((unsigned long long)capacity, total);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.cnt->next_path = (unsigned long long)n;
+        P.cnt->ext[0] = n;
+    }
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += gridDim.x * blockDim.x) {
+        start_path<kMulti>(P, slot, (unsigned long long)slot);
+        P.ext_q[0][slot] = slot;
     }
 }
 
@@ -747,7 +751,27 @@ __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
         P.cnt->work_sh = 0;
     }
     const int n = P.cnt->mat[p][kMissQueue].n;
-    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; i0 < n; i0 += gridDim.x * blockDim.x) {
+    // Every queued miss starts a new path in its slot.  A warp's entries over
+    // the whole launch are known (i0 = w0 + j * stride, all lanes but the
+    // last round's tail), so it claims their path indices, and queue
+    // positions for the ones the pass still has, with one atomic each; the
+    // started paths are a prefix of the warp's entries.
+    const int stride = gridDim.x * blockDim.x;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31;
+    int count = 0;
+    for (int i0 = w0; i0 < n; i0 += stride) count += min(32, n - i0);
+    const unsigned long long total = P.cnt->pass_total;
+    unsigned long long pid0 = 0;
+    int e0 = 0;
+    if (lane_id() == 0 && count > 0) {
+        pid0 = atomicAdd(&P.cnt->next_path, (unsigned long long)count);
+        const int starts = pid0 < total ? (int)min((unsigned long long)count, total - pid0) : 0;
+        if (starts > 0) e0 = atomicAdd(&P.cnt->ext[q], starts);
+    }
+    pid0 = __shfl_sync(0xffffffffu, pid0, 0);
+    e0 = __shfl_sync(0xffffffffu, e0, 0);
+    int done_before = 0;  // the warp's entries in earlier rounds
+    for (int i0 = w0; i0 < n; i0 += stride) {
         int i = i0 + lane_id();
         bool active = i < n;
         int slot = active ? P.mat_q[kMissQueue][i] : 0;
@@ -777,9 +801,13 @@ __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
             }
             store_sample(P, path_index(m), L, slot);
         }
-        bool ok = regenerate<kMulti>(P, slot, active);
-        int e = warp_push(&P.cnt->ext[q], ok);
-        if (ok) P.ext_q[q][e] = slot;
+        const int r = done_before + lane_id();
+        const unsigned long long pid = pid0 + (unsigned long long)r;
+        if (active && pid < total) {
+            start_path<kMulti>(P, slot, pid);
+            P.ext_q[q][e0 + r] = slot;
+        }
+        done_before += min(32, n - i0);
     }
 }
 
