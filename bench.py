@@ -48,9 +48,9 @@ METRIC = "samples/s (material-sphere scene 1920x1080, 64 spp, depth 16)"
 NODE_BYTES, TRI_BYTES, RAY_IN, HIT_OUT = 64, 48, 32, 16
 # DRAM bytes (read + write) per closest-hit traversal launch of this workload,
 # from one ncu capture of the full-size launch list (dram__bytes_read.sum +
-# dram__bytes_write.sum over the 374 extension launches of that capture /
-# 374); a profile measurement, not a live one.
-TRAVERSE_DRAM_BYTES_PER_LAUNCH = (172.2e9 + 38.3e9) / 374
+# dram__bytes_write.sum over the 120 extension launches of that capture /
+# 120); a profile measurement, not a live one.
+TRAVERSE_DRAM_BYTES_PER_LAUNCH = (170.30e9 + 42.23e9) / 120
 
 
 def peaks():
