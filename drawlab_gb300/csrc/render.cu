@@ -488,7 +488,7 @@ constexpr int kDone = kEmptyChild;  // traversal state: ray finished
 //                 and one coalesced 128-byte store per 32 entries.
 //   kAny = true:  any hit of shadow rays S (queue positions); unoccluded ones
 //                 add their contribution to the path or the ended path's sample
-constexpr unsigned kFetchChunk = 32;
+constexpr unsigned kFetchChunk = 64;
 constexpr int kTraverseWarps = 4;  // 128 threads
 constexpr int kStage = 64;         // staged entries per warp and destination (flushed at 32)
 constexpr int kSmemStack = 8;      // top traversal-stack entries per thread kept in shared memory
