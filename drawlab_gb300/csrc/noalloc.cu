@@ -1,12 +1,12 @@
 // dl_li_static: per-path radiance with no allocation at call time.
 //
 // Who needs it: callers that must not allocate device memory while they
-// render -- a frame loop recorded into a CUDA graph (cudaMalloc cannot be
-// captured), an engine that hands all device memory to its own pool at
-// start-up and forbids allocation afterwards, or a host thread that may not
-// block on the driver's allocator.  dl_li grows its path pool on demand;
-// this entry point instead runs the same wavefront kernels out of one
-// fixed, file-scope device array.
+// render -- an engine that hands all device memory to its own pool at
+// start-up and forbids allocation afterwards, a real-time loop with a fixed
+// memory budget, or a host thread that may not block on the driver's
+// allocator.  dl_li grows its path pool on demand; this entry point instead
+// runs the same wavefront kernels out of one fixed, file-scope device array.
+// It is a synchronous call: it returns after the paths have finished.
 //
 // Limits and sharing:
 //  * the array holds kStaticPathSlots = 16384 path slots (240 bytes each,
@@ -18,10 +18,13 @@
 //  * every call uses the same array and leaves its contents behind; the
 //    counters that must start at zero are cleared at the start of each call;
 //  * two calls whose work overlaps on the GPU (different streams or
-//    contexts on one device) race on the array and corrupt each other.
+//    contexts on one device) race on the array and corrupt each other, so
+//    calls from all contexts on one device must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <exception>
 #include <mutex>
+#include <string>
 
 #include "internal.h"
 #include "scene.h"
@@ -29,8 +32,8 @@
 namespace dl {
 
 size_t fixed_pool_bytes(int64_t slots);
-cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
-                            const int* d_xys, float* d_L, float* d_pos);
+void render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
+                     const int* d_xys, float* d_L, float* d_pos);
 
 constexpr int64_t kStaticPathSlots = 16384;
 constexpr size_t kStaticPoolBytes = 240 * (size_t)kStaticPathSlots + 256;
@@ -88,12 +91,20 @@ extern "C" int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t
     cudaError_t e = cudaSetDevice(ctx->device);
     void* pool = nullptr;
     if (e == cudaSuccess) e = dl::pool_address(ctx->device, &pool);
+    if (e != cudaSuccess) {
+        ctx->error = std::string("dl_li_static: static pool address: ") + cudaGetErrorString(e);
+        return DL_ERR_CUDA;
+    }
     int64_t slots = opts->max_paths_in_flight > 0 ? opts->max_paths_in_flight : dl::kStaticPathSlots;
     slots = (slots / 32) * 32;
     if (slots < 32) slots = 32;
-    if (e == cudaSuccess) e = dl::render_li_fixed(scene, *opts, pool, slots, n, d_xys, d_L, d_pos);
-    if (e != cudaSuccess) {
-        ctx->error = cudaGetErrorString(e);
+    try {
+        dl::render_li_fixed(scene, *opts, pool, slots, n, d_xys, d_L, d_pos);
+    } catch (const dl::Error& err) {
+        ctx->error = err.what();
+        return err.status;
+    } catch (const std::exception& err) {
+        ctx->error = err.what();
         return DL_ERR_CUDA;
     }
     return DL_OK;

@@ -1888,12 +1888,14 @@ void render_batch(dl_context* ctx, const BatchItem* items, int n, bool count_tra
 // Li of explicit paths with every piece of path state in caller-provided
 // device memory (`pool`, laid out below) and no allocation of any kind: no
 // cudaMalloc, no pinned staging (the counters are read back into a stack
-// copy), no exceptions, no graph.  Used by the allocation-free entry point.
+// copy), no graph.  Used by the allocation-free entry point.
 constexpr size_t kCounterBytes = (sizeof(RenderCounters) + 255) / 256 * 256;
 size_t fixed_pool_bytes(int64_t slots) { return kSlotBytes * (size_t)slots + kCounterBytes; }
 
-cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
-                            const int* d_xys, float* d_L, float* d_pos) {
+// Failures throw dl::Error with the status and message that run_wavefront
+// gives for the same condition.
+void render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t slots, int64_t li_n,
+                     const int* d_xys, float* d_L, float* d_pos) {
     dl_context* ctx = S->ctx;
     cudaStream_t st = ctx->stream;
     RenderParams P;
@@ -1922,16 +1924,14 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
     P.li_pos = d_pos;
     int64_t cap = std::min<int64_t>(slots, ((li_n + 31) / 32) * 32);
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
-    cudaError_t e = cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st);
-    if (e != cudaSuccess) return e;
+    DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
     // pass values from the stack (a pageable copy: staged before it returns)
     PassValues pv;
     pv.total = (unsigned long long)li_n;
     pv.spp_offset = 0;
     pv.keep = 1u << 24;
     pv.recs = nullptr;
-    e = cudaMemcpyAsync(&P.cnt->pass_total, &pv, sizeof(pv), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return e;
+    DL_CUDA(cudaMemcpyAsync(&P.cnt->pass_total, &pv, sizeof(pv), cudaMemcpyHostToDevice, st));
     k_init<false><<<sms * 16, 128, 0, st>>>(P, (int)cap);
     RenderCounters hc;
     int64_t iters = 0;
@@ -1940,14 +1940,14 @@ cudaError_t render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, in
         for (int k = 0; k < tp.iters_per_graph; k++)
             launch_iteration<false>(P, k & 1, st, sms, tp, false, nullptr, nullptr);
         iters += tp.iters_per_graph;
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
-        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-        if (hc.err) return cudaErrorUnknown;
+        DL_CUDA(cudaGetLastError());
+        DL_CUDA(cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st));
+        DL_CUDA(cudaStreamSynchronize(st));
+        if (hc.err & kErrTensorWait) throw Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in a guided kernel");
+        if (hc.err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         if (hc.ext[0] == 0 && hc.shadow[0] == 0 && hc.next_path >= (unsigned long long)li_n) break;
-        if (iters > 1000000) return cudaErrorLaunchTimeout;
+        if (iters > 1000000) throw Error(DL_ERR_TIMEOUT, "render did not converge");
     }
-    return cudaSuccess;
 }
 
 void resolve_film(dl_scene* S, const float* d_film, int filter, float* d_rgb) {

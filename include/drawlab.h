@@ -324,16 +324,19 @@ int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
           const int32_t* xys, float* L_out, float* pos_out);
 
 /* Allocation-free form of dl_li, with no counterpart in the reference.  For
- * callers that may not allocate device memory while rendering (a frame loop
- * recorded into a CUDA graph, an engine that owns all device memory after
- * start-up): the path state lives in one fixed array of 16384 path slots
- * (3.75 MiB) compiled into the library, present on every GPU that loads it.
+ * callers that may not allocate device memory while rendering (an engine
+ * that owns all device memory after start-up, a loop with a fixed memory
+ * budget, a thread that may not block on the allocator): the path state
+ * lives in one fixed array of 16384 path slots (3.75 MiB) compiled into the
+ * library, present on every GPU that loads it until the process exits.
  * d_xys (n x 3 int32), d_L (n x 3 float) and d_pos (n x 2 float) are device
  * pointers supplied by the caller.  opts->max_paths_in_flight must be 0
  * (whole pool) or at most 16384, else DL_ERR_INVALID_ARG.  The first call on
  * a device resolves the array's address, so make it before any stream
- * capture.  All calls share the array: calls whose work overlaps on the GPU
- * race.  Runs on the context stream and returns after the paths finish. */
+ * capture.  All calls, from every context on the device, share the array:
+ * calls whose work overlaps on the GPU race, so the caller serialises them.
+ * A synchronous call on the context stream: it returns after the paths
+ * finish, with the status codes and messages of dl_li for the same faults. */
 int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t n,
                  const int32_t* d_xys, float* d_L, float* d_pos);
 
