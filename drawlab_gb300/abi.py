@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-DL_ABI_VERSION = 7
+DL_ABI_VERSION = 8
 
 # status
 DL_OK = 0

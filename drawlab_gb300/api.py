@@ -37,6 +37,10 @@ SIGNATURES = {
     "dl_trace_any": (C.c_int, [_vp, _vp, _i64, _vp]),
     "dl_trace_closest_device": (C.c_int, [_vp, _vp, _i64, _vp]),
     "dl_trace_any_device": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "dl_trace_closest_wavefront": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "dl_trace_any_wavefront": (C.c_int, [_vp, _vp, _i64, _vp]),
+    "dl_bsdf_query": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dl_scene_env_query": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "dl_render": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film_device": (C.c_int, [_vp, _vp, _vp]),
@@ -167,6 +171,27 @@ class Context:
         self.check(self.lib.dl_stats_get(self.h, C.byref(s)))
         return s
 
+    def bsdf_query(self, mat, wi, wo, smp):
+        """BSDF eval / pdf of (wi, wo) and sample(wi) from smp (n x 3) of one
+        material (a scenes.Material), computed on the GPU; the same keys as
+        the oracle's bsdf_query."""
+        wi, wo, smp = (np.ascontiguousarray(a, np.float32) for a in (wi, wo, smp))
+        n = wi.shape[0]
+        out = dict(eval=np.empty((n, 3), np.float32), pdf=np.empty(n, np.float32),
+                   wo=np.empty((n, 3), np.float32), weight=np.empty((n, 3), np.float32),
+                   eta=np.empty(n, np.float32), measure=np.empty(n, np.int32))
+        md = abi.dl_material_desc()
+        md.type = mat.type
+        md.albedo[:] = [float(v) for v in mat.albedo]
+        md.specular[:] = [float(v) for v in mat.specular]
+        md.alpha[:] = [float(v) for v in mat.alpha]
+        md.int_ior = mat.int_ior
+        md.ext_ior = mat.ext_ior
+        self.check(self.lib.dl_bsdf_query(self.h, C.byref(md), n, _ptr(wi), _ptr(wo), _ptr(smp),
+                                          _ptr(out["eval"]), _ptr(out["pdf"]), _ptr(out["wo"]),
+                                          _ptr(out["weight"]), _ptr(out["eta"]), _ptr(out["measure"])))
+        return out
+
     @staticmethod
     def _requests(items):
         """items: (Scene, opts) or (Scene, opts, Camera override)."""
@@ -266,20 +291,37 @@ class Scene:
         self.ctx.check(self.ctx.lib.dl_scene_default_opts(self.h, C.byref(o)))
         return o
 
-    def trace_closest(self, rays: np.ndarray):
+    def trace_closest(self, rays: np.ndarray, wavefront: bool = False):
+        """Closest hits (prim, t, u, v).  wavefront=True traces them with the
+        renderer's own traversal kernel (every tmin must be 1e-4)."""
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
         prim = np.empty(n, np.int32)
         t, u, v = (np.empty(n, np.float32) for _ in range(3))
-        self.ctx.check(self.ctx.lib.dl_trace_closest(self.h, _ptr(rays), n, _ptr(prim), _ptr(t), _ptr(u), _ptr(v)))
+        fn = self.ctx.lib.dl_trace_closest_wavefront if wavefront else self.ctx.lib.dl_trace_closest
+        self.ctx.check(fn(self.h, _ptr(rays), n, _ptr(prim), _ptr(t), _ptr(u), _ptr(v)))
         return prim, t, u, v
 
-    def trace_any(self, rays: np.ndarray):
+    def trace_any(self, rays: np.ndarray, wavefront: bool = False):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
         occ = np.empty(n, np.uint8)
-        self.ctx.check(self.ctx.lib.dl_trace_any(self.h, _ptr(rays), n, _ptr(occ)))
+        fn = self.ctx.lib.dl_trace_any_wavefront if wavefront else self.ctx.lib.dl_trace_any
+        self.ctx.check(fn(self.h, _ptr(rays), n, _ptr(occ)))
         return occ
+
+    def env_query(self, xi, nrm, dirs):
+        """The envmap's sampleDirection(xi, normal) -> (dir, pdf, value) and
+        pdfDirection / eval of dirs, computed on the GPU."""
+        xi, nrm, dirs = (np.ascontiguousarray(a, np.float32) for a in (xi, nrm, dirs))
+        n = xi.shape[0]
+        out = dict(s_dir=np.empty((n, 3), np.float32), s_pdf=np.empty(n, np.float32),
+                   s_value=np.empty((n, 3), np.float32), pdf=np.empty(n, np.float32),
+                   value=np.empty((n, 3), np.float32))
+        self.ctx.check(self.ctx.lib.dl_scene_env_query(
+            self.h, n, _ptr(xi), _ptr(nrm), _ptr(dirs), _ptr(out["s_dir"]), _ptr(out["s_pdf"]),
+            _ptr(out["s_value"]), _ptr(out["pdf"]), _ptr(out["value"])))
+        return out
 
     def render(self, opts: abi.dl_render_opts) -> np.ndarray:
         rgb = np.empty((self.height, self.width, 3), np.float32)

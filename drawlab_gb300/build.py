@@ -31,7 +31,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
              "-I", str(CUDA_HOME / "include")]
 
-CU_SOURCES = ["trace.cu", "render.cu", "noalloc.cu", "guide.cu"]
+CU_SOURCES = ["trace.cu", "render.cu", "noalloc.cu", "guide.cu", "query.cu"]
 CPP_SOURCES = ["api.cpp", "bvh.cpp", "image.cpp", "scene.cpp", "xml.cpp"]
 
 

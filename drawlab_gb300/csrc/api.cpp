@@ -262,6 +262,87 @@ int dl_trace_any(dl_scene* S, const float* rays, int64_t n, uint8_t* occluded) {
     });
 }
 
+namespace {
+// Rays through the renderer's own traversal kernels (render.cu): every ray
+// must start at the renderer's constant t = kRayEps.
+void trace_wavefront_host(dl_scene* S, bool any, const float* rays, int64_t n, float* hits_or_null,
+                          uint8_t* occ_or_null) {
+    dl_context* ctx = S->ctx;
+    need(n >= 0 && n < ((int64_t)1 << 31), "bad ray count");
+    for (int64_t i = 0; i < n; i++)
+        need(rays[8 * i + 3] == dl::kRayEps, "wavefront traversal: every ray's tmin must be 1e-4");
+    if (n == 0) return;
+    cudaStream_t st = ctx->stream;
+    dl::TraceBuffers& B = ctx->trace;
+    B.rays.ensure((size_t)n * 32);
+    B.hits.ensure((size_t)n * 16);
+    B.wavefront.ensure(dl::wavefront_rays_bytes(n));
+    DL_CUDA(cudaEventRecord(ctx->ev0, st));
+    DL_CUDA(cudaMemcpyAsync(B.rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, st));
+    dl::trace_wavefront_launch(S, any, B.rays.as<float>(), n, B.hits.as<float>(), B.hits.as<uint8_t>(),
+                               B.wavefront.ptr);
+    if (any) {
+        DL_CUDA(cudaMemcpyAsync(occ_or_null, B.hits.ptr, (size_t)n, cudaMemcpyDeviceToHost, st));
+    } else {
+        DL_CUDA(cudaMemcpyAsync(hits_or_null, B.hits.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost, st));
+    }
+    DL_CUDA(cudaEventRecord(ctx->ev1, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.trace_ms = ms;
+}
+}  // namespace
+
+int dl_trace_closest_wavefront(dl_scene* S, const float* rays, int64_t n, int32_t* prim_id, float* t, float* u,
+                               float* v) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (rays && prim_id && t && u && v)), "bad ray buffers");
+        std::vector<float> h((size_t)std::max<int64_t>(n, 0) * 4);
+        trace_wavefront_host(S, false, rays, n, h.data(), nullptr);
+        for (int64_t i = 0; i < n; i++) {
+            t[i] = h[4 * i];
+            u[i] = h[4 * i + 1];
+            v[i] = h[4 * i + 2];
+            std::memcpy(&prim_id[i], &h[4 * i + 3], 4);
+        }
+    });
+}
+
+int dl_trace_any_wavefront(dl_scene* S, const float* rays, int64_t n, uint8_t* occluded) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    dl_context* ctx = S->ctx;
+    return guard(ctx, [&] {
+        need(n >= 0 && (n == 0 || (rays && occluded)), "bad ray buffers");
+        trace_wavefront_host(S, true, rays, n, nullptr, occluded);
+    });
+}
+
+int dl_bsdf_query(dl_context* ctx, const dl_material_desc* m, int64_t n, const float* wi, const float* wo,
+                  const float* smp, float* eval, float* pdf, float* s_wo, float* s_weight, float* s_eta,
+                  int32_t* s_measure) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    return guard(ctx, [&] {
+        need(m != nullptr, "material is NULL");
+        need(m->type >= DL_MAT_DIFFUSE && m->type <= DL_MAT_ANISO_GGX, "unknown material type");
+        need(n >= 0 && (n == 0 || (wi && wo && smp && eval && pdf && s_wo && s_weight && s_eta && s_measure)),
+             "bad query buffers");
+        dl::bsdf_query(ctx, *m, n, wi, wo, smp, eval, pdf, s_wo, s_weight, s_eta, s_measure);
+    });
+}
+
+int dl_scene_env_query(dl_scene* S, int64_t n, const float* xi, const float* nrm, const float* dirs, float* s_dir,
+                       float* s_pdf, float* s_value, float* pdf, float* value) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    return guard(S->ctx, [&] {
+        need(n >= 0 && (n == 0 || (xi && nrm && dirs && s_dir && s_pdf && s_value && pdf && value)),
+             "bad query buffers");
+        dl::env_query(S, n, xi, nrm, dirs, s_dir, s_pdf, s_value, pdf, value);
+    });
+}
+
 int dl_render_film_device(dl_scene* S, const dl_render_opts* opts, float* d_film) {
     if (!S) return DL_ERR_INVALID_ARG;
     return guard(S->ctx, [&] {

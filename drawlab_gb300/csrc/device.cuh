@@ -482,8 +482,10 @@ __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const BRec& r) {
     }
 }
 
+// `lobe`: aniso_ggx's third uniform number (aniso_ggx.cu:104-108, drawn
+// after the 2D sample; > 0.5 picks the diffuse lobe); unused by the others.
 template <int T>
-__device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, float2 s) {
+__device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, float2 s, float lobe) {
     const float3 zero = f3(0.f, 0.f, 0.f);
     switch (T) {
         case MAT_DIFFUSE:
@@ -530,13 +532,10 @@ __device__ __forceinline__ float3 bsdf_sample(const DevMaterial& m, BRec& r, flo
         case MAT_ANISO_GGX: {
             if (r.wi.z <= 0.f) return zero;
             r.measure = M_SOLID;
-            float2 ss = s;
-            if (s.x > 0.5f) {
-                ss.x = __fmul_rn(__fsub_rn(s.x, 0.5f), 2.0f);
-                r.wo = square_to_cosine_hemisphere(ss);
+            if (lobe > 0.5f) {
+                r.wo = square_to_cosine_hemisphere(s);
             } else {
-                ss.x = __fmul_rn(s.x, 2.0f);
-                r.wo = reflect(r.wi, square_to_ggx(ss, m.ax, m.ay));
+                r.wo = reflect(r.wi, square_to_ggx(s, m.ax, m.ay));
             }
             if (r.wo.z <= 0.f) return zero;
             return divs(scale(bsdf_eval<T>(m, r), r.wo.z), bsdf_pdf<T>(m, r));

@@ -155,6 +155,7 @@ struct RenderBuffers {
 
 struct TraceBuffers {
     DevBuf rays, hits, occ;
+    DevBuf wavefront;   // path slots, queues and counters of wavefront ray batches
     HostBuf stage;
 };
 

@@ -1035,7 +1035,9 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
                         prev_pdf = alpha * stored_mixture_pdf(lob, nd) + (1.f - alpha) * pb;
                         fcos_over_p = prev_pdf > 0.f ? scale(fv, fmaxf(q2.wo.z, 0.f) / prev_pdf) : f3(0.f, 0.f, 0.f);
                     } else {
-                        float3 wgt = bsdf_sample<T>(m, q2, g.next2d());
+                        const float2 s2 = g.next2d();
+                        const float lobe = T == MAT_ANISO_GGX ? g.next_float() : 0.f;
+                        float3 wgt = bsdf_sample<T>(m, q2, s2, lobe);
                         float pb = bsdf_pdf<T>(m, q2);
                         nd = to_world(fr, q2.wo);
                         if (T == MAT_ANISO_GGX) nd = normalize(nd);
@@ -1045,7 +1047,9 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
                     tp = mul(tp, fcos_over_p);
                     rec_pdf = prev_pdf;
                 } else {
-                    float3 f = bsdf_sample<T>(m, q2, g.next2d());
+                    const float2 s2 = g.next2d();
+                    const float lobe = T == MAT_ANISO_GGX ? g.next_float() : 0.f;
+                    float3 f = bsdf_sample<T>(m, q2, s2, lobe);
                     tp = mul(tp, f);
                     eta = __fmul_rn(eta, q2.eta);
                     prev_pdf = bsdf_pdf<T>(m, q2);
@@ -1960,6 +1964,109 @@ void resolve_film_cam(const DevCamera& cam, cudaStream_t st, const float* d_film
     k_resolve<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4*>(d_film),
                                                          cam.w + 2 * b, b, cam.w, cam.h, d_rgb);
     DL_CUDA(cudaGetLastError());
+}
+
+}  // namespace dl
+
+namespace dl {
+
+// ------------------------------------------------- rays through k_traverse
+// Ray batches through the renderer's own traversal kernels, the exact
+// template instances a single-scene render launches (k_traverse<false,
+// false, false> for closest hits, k_traverse<false, true, false> for shadow
+// rays) with the context's launch shape, so that ray-level parity tests
+// exercise the kernels dl_render runs.  Each ray gets a path slot: its ray
+// record (closest hit) or its shadow-queue entry with a unit contribution
+// aimed at sample i (any hit), in queue order 0..n-1.
+
+__global__ void k_wavefront_rays_setup(RenderParams P, const float4* __restrict__ rays, int n, int any) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = rays[2 * i], d = rays[2 * i + 1];
+        if (any) {
+            P.sh_o[i] = make_float4(o.x, o.y, o.z, __int_as_float(0));
+            P.sh_d[i] = d;
+            P.sh_c[i] = make_float4(1.f, 1.f, 1.f, __int_as_float(-1 - i));
+            P.li_L[3 * i] = 0.f;
+            P.li_L[3 * i + 1] = 0.f;
+            P.li_L[3 * i + 2] = 0.f;
+        } else {
+            RayRec r;
+            r.o = make_float4(o.x, o.y, o.z, __int_as_float(0));
+            r.d = d;
+            P.rec[i].ray = r;
+            P.ext_q[0][i] = i;
+        }
+    }
+}
+
+// hits (n x float4: t, u, v, original triangle id bits, -1 = miss) from the
+// hit records; occluded flags from the delivered unit contributions.
+__global__ void k_wavefront_rays_out(RenderParams P, int n, int any, float4* __restrict__ hits,
+                                     uint8_t* __restrict__ occ) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (any) {
+            occ[i] = P.li_L[3 * i] == 0.f ? 1 : 0;
+        } else {
+            const float4 h = P.rec[i].hit.h;
+            const int tri = __float_as_int(h.w);
+            const int prim = tri >= 0 ? __float_as_int(__ldg(P.r0.sc.tris + 3 * tri).w) : -1;
+            hits[i] = make_float4(tri >= 0 ? h.x : 0.f, tri >= 0 ? h.y : 0.f, tri >= 0 ? h.z : 0.f,
+                                  __int_as_float(prim));
+        }
+    }
+}
+
+size_t wavefront_rays_bytes(int64_t n) {
+    return kCounterBytes + 128 * (size_t)n + 3 * 16 * (size_t)n + 12 * (size_t)n +
+           4 * (size_t)n * (2 + kNumMaterialTypes + 1);
+}
+
+// d_rays: n x 8 floats (o, tmin, d, tmax) with tmin = kRayEps for every ray
+// (the renderer's constant ray start); `work` holds wavefront_rays_bytes(n).
+void trace_wavefront_launch(dl_scene* S, bool any, const float* d_rays, int64_t n, float* d_hits, uint8_t* d_occ,
+                            void* work) {
+    dl_context* ctx = S->ctx;
+    cudaStream_t st = ctx->stream;
+    if (n == 0) return;
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    dl_render_opts o;
+    std::memset(&o, 0, sizeof(o));
+    P.r0 = make_request(S, o);
+    P.mode = 1;
+    char* b = static_cast<char*>(work);
+    P.cnt = reinterpret_cast<RenderCounters*>(b);
+    b += kCounterBytes;
+    P.rec = reinterpret_cast<SlotRec*>(b);
+    b += 128 * (size_t)n;
+    float4** f4[] = {&P.sh_o, &P.sh_d, &P.sh_c};
+    for (float4** f : f4) {
+        *f = reinterpret_cast<float4*>(b);
+        b += 16 * (size_t)n;
+    }
+    P.li_L = reinterpret_cast<float*>(b);
+    b += 12 * (size_t)n;
+    int** iq[] = {&P.ext_q[0], &P.ext_q[1], &P.mat_q[0], &P.mat_q[1], &P.mat_q[2], &P.mat_q[3], &P.mat_q[4],
+                  &P.mat_q[5]};
+    for (int** q : iq) {
+        *q = reinterpret_cast<int*>(b);
+        b += 4 * (size_t)n;
+    }
+    DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
+    const int ni = (int)n;
+    DL_CUDA(cudaMemcpyAsync(any ? &P.cnt->shadow[0] : &P.cnt->ext[0], &ni, sizeof(int), cudaMemcpyHostToDevice, st));
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
+    const int g = (int)std::min<int64_t>((n + 127) / 128, (int64_t)sms * 16);
+    k_wavefront_rays_setup<<<g, 128, 0, st>>>(P, reinterpret_cast<const float4*>(d_rays), ni, any ? 1 : 0);
+    const int tb = sms * ctx->tune.trav_ctas_per_sm;
+    if (any) k_traverse<false, true, false><<<tb, 128, 0, st>>>(P, 0);
+    else k_traverse<false, false, false><<<tb, 128, 0, st>>>(P, 0);
+    k_wavefront_rays_out<<<g, 128, 0, st>>>(P, ni, any ? 1 : 0, reinterpret_cast<float4*>(d_hits), d_occ);
+    DL_CUDA(cudaGetLastError());
+    unsigned int err = 0;
+    DL_CUDA(cudaMemcpyAsync(&err, &P.cnt->err, sizeof(err), cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    if (err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
 }
 
 }  // namespace dl

@@ -14,6 +14,18 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
 
 void trace_closest_launch(dl_scene* S, const float* d_rays, int64_t n, float* d_hits, void* scratch, bool count);
 void trace_any_launch(dl_scene* S, const float* d_rays, int64_t n, uint8_t* d_occ, void* scratch, bool count);
+// The same queries through the renderer's own k_traverse kernels (render.cu);
+// every ray starts at t = kRayEps.  Synchronises; `work` holds
+// wavefront_rays_bytes(n).
+size_t wavefront_rays_bytes(int64_t n);
+void trace_wavefront_launch(dl_scene* S, bool any, const float* d_rays, int64_t n, float* d_hits, uint8_t* d_occ,
+                            void* work);
+
+// Device BSDF and envmap queries (query.cu); host buffers in and out.
+void bsdf_query(dl_context* ctx, const dl_material_desc& m, int64_t n, const float* wi, const float* wo,
+                const float* smp, float* eval, float* pdf, float* s_wo, float* s_w, float* s_eta, int32_t* s_measure);
+void env_query(dl_scene* S, int64_t n, const float* xi, const float* nrm, const float* dirs, float* s_dir,
+               float* s_pdf, float* s_val, float* pdf, float* val);
 
 int64_t film_floats(int w, int h, int filter);
 void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys, float* d_L,

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define DL_ABI_VERSION 7
+#define DL_ABI_VERSION 8
 
 /* ------------------------------------------------------------------ status */
 enum dl_status {
@@ -226,6 +226,17 @@ int dl_trace_any(dl_scene* scene, const float* rays, int64_t n, uint8_t* occlude
 int dl_trace_closest_device(dl_scene* scene, const float* d_rays, int64_t n, float* d_hits);
 int dl_trace_any_device(dl_scene* scene, const float* d_rays, int64_t n, uint8_t* d_occluded);
 
+/* The same two queries (same reference functions, same outputs) traced by
+ * the renderer's own persistent wavefront traversal kernels -- the kernels
+ * dl_render launches for extension and shadow rays -- instead of the
+ * stand-alone ray-batch kernels above.  Those kernels start every ray at
+ * the renderer's constant t = 1e-4 (the reference's Epsilon, scene.cpp:
+ * 165-169), so every ray's tmin must be 1e-4, else DL_ERR_INVALID_ARG.
+ * Host buffers; synchronous. */
+int dl_trace_closest_wavefront(dl_scene* scene, const float* rays, int64_t n,
+                               int32_t* prim_id, float* t, float* u, float* v);
+int dl_trace_any_wavefront(dl_scene* scene, const float* rays, int64_t n, uint8_t* occluded);
+
 /* -------------------------------------------------------------- rendering */
 
 enum dl_filter {
@@ -339,6 +350,31 @@ int dl_li(dl_scene* scene, const dl_render_opts* opts, int64_t n,
  * finish, with the status codes and messages of dl_li for the same faults. */
 int dl_li_static(dl_scene* scene, const dl_render_opts* opts, int64_t n,
                  const int32_t* d_xys, float* d_L, float* d_pos);
+
+/* BSDF::eval, BSDF::pdf and BSDF::sample (include/tracer/bsdf.h:62-104;
+ * for aniso_ggx the OptiX callables of src/optix/cuda/material/
+ * aniso_ggx.cu:37-121) of one material (its constant parameters; textures
+ * are not used) on n queries, evaluated on the GPU by the device code the
+ * material kernels run.  wi, wo: n x 3 local directions (eval and pdf of
+ * (wi, wo) in solid-angle measure); smp: n x 3 uniform numbers for sample(wi):
+ * the 2D sample, then the lobe coin that only aniso_ggx draws
+ * (aniso_ggx.cu:104-108).  Outputs: eval n x 3, pdf n, sampled wo n x 3,
+ * sample weight n x 3, eta n, measure n (0 unknown, 1 solid angle,
+ * 2 discrete).  Host buffers; synchronous. */
+int dl_bsdf_query(dl_context* ctx, const dl_material_desc* material, int64_t n,
+                  const float* wi, const float* wo, const float* smp,
+                  float* eval, float* pdf, float* s_wo, float* s_weight, float* s_eta,
+                  int32_t* s_measure);
+
+/* The scene's environment emitter on the GPU: Envmap::sampleDirection from
+ * three uniform numbers xi (n x 3) at shading normals nrm (n x 3) --
+ * direction s_dir, solid-angle pdf s_pdf, and cos * radiance / pdf s_value --
+ * and Envmap::pdfDirection / Envmap::eval of the directions dirs (n x 3)
+ * (include/optix/light/envmap.h:25-94).  DL_ERR_INVALID_ARG when the scene
+ * has no envmap.  Host buffers; synchronous. */
+int dl_scene_env_query(dl_scene* scene, int64_t n, const float* xi, const float* nrm,
+                       const float* dirs, float* s_dir, float* s_pdf, float* s_value,
+                       float* pdf, float* value);
 
 /* ----------------------------------------------------------------- batches */
 

@@ -4,9 +4,13 @@
   ``oracle/_build/liboracle.so`` (g++, no dependencies).  It builds on any
   host, including the Arm GPU machine.
 * ``build_ref()`` compiles the reference's own CPU hot-path sources from where
-  they lie (``$DRAWLAB_REFERENCE``, default ``/root/reference``) against the
-  stand-in headers in ``oracle/ref_shim`` and links them with
-  ``oracle/ref_driver.cpp`` into ``oracle/_ref/libdlref.so``.  When the
+  they lie (``$DRAWLAB_REFERENCE``, else a ``reference`` directory beside the
+  repository) against the stand-in headers in ``oracle/ref_shim`` and links
+  them with ``oracle/ref_driver.cpp`` and ``oracle/ref_host_setup.cpp`` into
+  ``oracle/_ref/libdlref.so``.  It also compiles the reference's OptiX-only
+  math (GGX material, envmap emitter, miss shader, OpenCV camera, hit data)
+  as host code through ``oracle/ref_optix.cpp`` against
+  ``oracle/ref_shim_optix`` into ``oracle/_ref/libdlref_optix.so``.  When the
   reference tree is absent it does nothing and returns None.
 
 Both use ``-O3 -ffp-contract=off`` so that no fused multiply-add changes the
@@ -43,6 +47,7 @@ REF_SOURCES = [
     "src/tracer/bsdf/diffuse.cpp",
     "src/tracer/bsdf/microfacet.cpp",
     "src/tracer/bsdf/mirror.cpp",
+    "src/tracer/camera/opencv.cpp",
     "src/tracer/camera/perspective.cpp",
     "src/tracer/camera/virtual.cpp",
     "src/tracer/emitter/area.cpp",
@@ -88,7 +93,7 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def reference_root() -> Path | None:
-    root = Path(os.environ.get("DRAWLAB_REFERENCE", "/root/reference"))
+    root = Path(os.environ.get("DRAWLAB_REFERENCE", str(REPO.parent / "reference")))
     return root if (root / "src" / "tracer" / "integrator" / "path.cpp").exists() else None
 
 
@@ -112,18 +117,39 @@ def build_ref(force: bool = False) -> Path | None:
         objs.append(obj)
         if force or _stale(obj, [src, *shim_files]):
             jobs.append([CXX, *flags, *inc, "-c", str(src), "-o", str(obj)])
-    own = [(HERE / "ref_driver.cpp", obj_dir / "ref_driver.o"),
-           (shim / "link_stubs.cpp", obj_dir / "link_stubs.o")]
-    for src, obj in own:
+    own = [(HERE / "ref_driver.cpp", obj_dir / "ref_driver.o", []),
+           (shim / "link_stubs.cpp", obj_dir / "link_stubs.o", []),
+           (HERE / "ref_host_setup.cpp", obj_dir / "ref_host_setup.o", [root / "src/tracer/emitter/envmap.cpp"])]
+    for src, obj, extra_deps in own:
         objs.append(obj)
-        if force or _stale(obj, [src, REPO / "include" / "drawlab.h", *shim_files]):
-            jobs.append([CXX, *flags, *inc, "-c", str(src), "-o", str(obj)])
+        if force or _stale(obj, [src, REPO / "include" / "drawlab.h", *shim_files, *extra_deps]):
+            jobs.append([CXX, *flags, *inc, "-I", str(root), "-c", str(src), "-o", str(obj)])
+    # The OptiX-only code: compiled as host C++ with __CUDACC__ defined (its
+    # host/device members compiled, the CUDA qualifiers ignored attributes),
+    # in a library of its own so its inline helpers never meet the CPU
+    # build's differently configured copies.
+    optix_shim = HERE / "ref_shim_optix"
+    optix_obj = obj_dir / "ref_optix.o"
+    optix_out = REF_DIR / "libdlref_optix.so"
+    optix_src = HERE / "ref_optix.cpp"
+    optix_deps = [optix_src, *optix_shim.glob("*.h"), *(root / "src/optix/cuda").rglob("*"),
+                  *(root / "include/optix").rglob("*.h")]
+    optix_job = None
+    if force or _stale(optix_obj, optix_deps):
+        optix_job = [CXX, *flags, "-D__CUDACC__", "-I", str(optix_shim), "-I", str(root / "include"),
+                     "-I", str(root / "src/optix/cuda"), "-I", "/usr/local/cuda/include",
+                     "-c", str(optix_src), "-o", str(optix_obj)]
+        jobs.append(optix_job)
     with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or not out.exists():
         tmp = out.with_suffix(".so.tmp%d" % os.getpid())
         _run([CXX, *COMMON_FLAGS, "-shared", *map(str, objs), "-o", str(tmp)])
         os.replace(tmp, out)
+    if force or optix_job or not optix_out.exists():
+        tmp = optix_out.with_suffix(".so.tmp%d" % os.getpid())
+        _run([CXX, *COMMON_FLAGS, "-shared", str(optix_obj), "-o", str(tmp)])
+        os.replace(tmp, optix_out)
     return out
 
 

@@ -598,24 +598,21 @@ V3 tex_bilinear(const Texture& T, float u, float v) {
     return tx(y0, x0) * (bx * by) + tx(y0, x1) * (ax * by) + tx(y1, x0) * (bx * ay) + tx(y1, x1) * (ax * ay);
 }
 
-// octree.cpp:153-212
-bool ray_intersect(const Scene& sc, const Ray& ray_in, Hit& its) {
-    Ray ray = ray_in;
-    std::pair<int, int> f(-1, -1);
-    P2 uv{0, 0};
-    float t = 0;
-    if (!closest(sc, sc.root, ray, uv, t, f)) return false;
-    const Mesh& m = sc.meshes[f.first];
+// The hit record of face `face` of mesh `mi` at barycentrics uv, distance t
+// (octree.cpp:186-212, with the OptiX shader's texture coordinates and
+// normal / tangent maps).
+void fill_hit(const Scene& sc, int mi, int face, P2 uv, float t, Hit& its) {
+    const Mesh& m = sc.meshes[mi];
     its.uv = uv;
     its.t = t;
-    its.mesh = f.first;
-    its.prim = m.prim_offset + f.second;
+    its.mesh = mi;
+    its.prim = m.prim_offset + face;
     V3 bary(1 - uv.x - uv.y, uv.x, uv.y);
-    V3 p0 = m.pos(f.second, 0), p1 = m.pos(f.second, 1), p2 = m.pos(f.second, 2);
+    V3 p0 = m.pos(face, 0), p1 = m.pos(face, 1), p2 = m.pos(face, 2);
     its.p = bary.x * p0 + bary.y * p1 + bary.z * p2;
     if (!m.UV.empty()) {
         auto tc = [&](int k) {
-            uint32_t p = m.F[3 * f.second + k];
+            uint32_t p = m.F[3 * face + k];
             return P2{m.UV[2 * p], m.UV[2 * p + 1]};
         };
         P2 a = tc(0), b = tc(1), c = tc(2);
@@ -625,24 +622,36 @@ bool ray_intersect(const Scene& sc, const Ray& ray_in, Hit& its) {
     its.geo = make_frame(normalized(cross(p1 - p0, p2 - p0)));
     if (!m.N.empty()) {
         // only the third normal term is normalised (octree.cpp:202-206)
-        V3 n = bary.x * m.nrm(f.second, 0) + bary.y * m.nrm(f.second, 1) +
-               bary.z * normalized(m.nrm(f.second, 2));
+        V3 n = bary.x * m.nrm(face, 0) + bary.y * m.nrm(face, 1) +
+               bary.z * normalized(m.nrm(face, 2));
         its.sh = make_frame(n);
     } else {
         its.sh = its.geo;
     }
+    its.tuv = P2{0.f, 0.f};
+    its.tan = V3();
     const Material& mat = sc.mats[m.material];
     if (mat.has_tex) {
         // texture coordinates as the OptiX shader (shader_common.h:38-45);
         // world-space normal / tangent maps of aniso_ggx (62-64, 104-107)
         its.tuv = m.UV.empty() ? P2{0.f, 0.f} : its.uv;
-        auto mapped = [&](int t) {
-            V3 c = tex_bilinear(sc.textures[t], its.tuv.x, its.tuv.y);
+        auto mapped = [&](int tx) {
+            V3 c = tex_bilinear(sc.textures[tx], its.tuv.x, its.tuv.y);
             return normalized(V3(c.x * 2.f - 1.f, c.y * 2.f - 1.f, c.z * 2.f - 1.f));
         };
         if (mat.type == DL_MAT_ANISO_GGX && mat.tex[3] >= 0) its.sh.n = mapped(mat.tex[3]);
         if (mat.type == DL_MAT_ANISO_GGX && mat.tex[4] >= 0) its.tan = mapped(mat.tex[4]);
     }
+}
+
+// octree.cpp:153-212
+bool ray_intersect(const Scene& sc, const Ray& ray_in, Hit& its) {
+    Ray ray = ray_in;
+    std::pair<int, int> f(-1, -1);
+    P2 uv{0, 0};
+    float t = 0;
+    if (!closest(sc, sc.root, ray, uv, t, f)) return false;
+    fill_hit(sc, f.first, f.second, uv, t, its);
     return true;
 }
 
@@ -760,7 +769,10 @@ float bsdf_pdf(const Material& m, const BRec& r) {
     }
 }
 
-V3 bsdf_sample(const Material& m, BRec& r, P2 s) {
+// `lobe` is the third uniform number of aniso_ggx's sample (aniso_ggx.cu:
+// 104-108: drawn after the 2D sample, > 0.5 picks the diffuse lobe); the
+// other materials ignore it.
+V3 bsdf_sample(const Material& m, BRec& r, P2 s, float lobe) {
     switch (m.type) {
         case DL_MAT_DIFFUSE:
             if (r.wi.z <= 0) return V3();
@@ -805,17 +817,14 @@ V3 bsdf_sample(const Material& m, BRec& r, P2 s) {
             return bsdf_eval(m, r) * r.wo.z / bsdf_pdf(m, r);
         }
         case DL_MAT_ANISO_GGX: {
-            // aniso_ggx.cu:91-121 with the lobe picked from sample.x (Nori
-            // style, as microfacet.cpp:82-95): x > 0.5 -> diffuse lobe.
+            // aniso_ggx.cu:89-121: the third number picks the lobe, the 2D
+            // sample drives it unchanged
             if (r.wi.z <= 0) return V3();
             r.measure = kSolidAngle;
-            P2 ss = s;
-            if (s.x > 0.5f) {
-                ss.x = (s.x - 0.5f) * 2.0f;
-                r.wo = square_to_cosine_hemisphere(ss);
+            if (lobe > 0.5f) {
+                r.wo = square_to_cosine_hemisphere(s);
             } else {
-                ss.x = s.x * 2.0f;
-                V3 wh = square_to_ggx(ss, m.ax, m.ay);
+                V3 wh = square_to_ggx(s, m.ax, m.ay);
                 r.wo = reflect(r.wi, wh);
             }
             if (r.wo.z <= 0) return V3();
@@ -1078,6 +1087,22 @@ inline float mis(float a, float b) {
     return a / (a + b);
 }
 
+// __miss__radiance (miss.cu:11-49) of a ray leaving along d: a camera ray
+// sees the envmap if "visual", else the background colour (weight 1); a
+// later ray gets the envmap's radiance with weight w, the MIS weight against
+// the pdf of the BSDF sample that made it when that BSDF is diffuse, else 1.
+V3 env_miss(const Scene& sc, V3 d, bool camera, bool diffuse, float bsdf_pdf, uint32_t flags, float& w) {
+    const Light& E = sc.lights[sc.env_light];
+    w = 1.f;
+    if (camera) return E.env_visual ? env_eval(E, d) : E.env_bg;
+    if (diffuse) {
+        DirSample hs;
+        hs.d = d;
+        w = mis(bsdf_pdf, pdf_emitter(sc, sc.env_light, hs, flags));
+    }
+    return env_eval(E, d);
+}
+
 inline V3 emitter_eval(const Light& L, const Hit& its, V3 wi) {
     if (L.type != DL_LIGHT_AREA) return V3();
     float c = to_local(its.sh, wi).z;
@@ -1111,10 +1136,8 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
     }
     if (!ray_intersect(sc, ray, its)) {
         // miss.cu:20-27: the camera sees the envmap if "visual", else bg_color
-        if (sc.env_light >= 0) {
-            const Light& E = sc.lights[sc.env_light];
-            result = E.env_visual ? env_eval(E, ray.d) : E.env_bg;
-        }
+        float w;
+        if (sc.env_light >= 0) result = env_miss(sc, ray.d, true, false, 0.f, o.flags, w);
         return result;
     }
     int light = sc.meshes[its.mesh].light;
@@ -1142,7 +1165,9 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
         }
         BRec bq;
         bq.wi = wi;
-        V3 f = bsdf_sample(bsdf, bq, rng.next2d());
+        const P2 s2 = rng.next2d();
+        const float lobe = bsdf.type == DL_MAT_ANISO_GGX ? rng.next1d() : 0.f;
+        V3 f = bsdf_sample(bsdf, bq, s2, lobe);
         tp = mul(tp, f);
         eta *= bq.eta;
         V3 nd = to_world(fr, bq.wo);
@@ -1162,13 +1187,9 @@ V3 Li(const Scene& sc, Pcg32& rng, const Ray& ray_in, const Opts& o) {
             // miss.cu:28-44: envmap radiance, MIS-weighted after a diffuse
             // bounce (a path with zero throughput adds nothing)
             if (sc.env_light >= 0 && (tp.x != 0.f || tp.y != 0.f || tp.z != 0.f)) {
-                V3 le = env_eval(sc.lights[sc.env_light], ray.d);
-                float w = 1.f;
-                if (is_diffuse(bsdf)) {
-                    DirSample hs;
-                    hs.d = ray.d;
-                    w = mis(bsdf_pdf(bsdf, bq), pdf_emitter(sc, sc.env_light, hs, o.flags));
-                }
+                const float bp = is_diffuse(bsdf) ? bsdf_pdf(bsdf, bq) : 0.f;
+                float w;
+                V3 le = env_miss(sc, ray.d, false, is_diffuse(bsdf), bp, o.flags, w);
                 result = result + mul(w * tp, le);
             }
             break;
@@ -1802,7 +1823,7 @@ int orc_bsdf_query(const dl_material_desc* md, int64_t n, const float* wi, const
         pdf[i] = bsdf_pdf(m, q);
         BRec s;
         s.wi = ld3(wi + 3 * i);
-        V3 w = bsdf_sample(m, s, P2{smp[2 * i], smp[2 * i + 1]});
+        V3 w = bsdf_sample(m, s, P2{smp[3 * i], smp[3 * i + 1]}, smp[3 * i + 2]);
         s_wo[3 * i] = s.wo.x; s_wo[3 * i + 1] = s.wo.y; s_wo[3 * i + 2] = s.wo.z;
         s_w[3 * i] = w.x; s_w[3 * i + 1] = w.y; s_w[3 * i + 2] = w.z;
         s_eta[i] = s.eta;
@@ -1850,6 +1871,70 @@ int orc_env_tables(void* p, float* q, uint32_t* alias, float* pdf) {
     std::copy(L.env_q.begin(), L.env_q.begin() + n, q);
     std::copy(L.env_alias.begin(), L.env_alias.begin() + n, alias);
     std::copy(L.env_pdf.begin(), L.env_pdf.begin() + n, pdf);
+    return 0;
+}
+
+int orc_env_query(void* p, int64_t n, const float* xi, const float* nrm, const float* dirs, float* s_dir,
+                  float* s_pdf, float* s_val, float* pdf, float* val) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    if (sc.env_light < 0) return 1;
+    const Light& L = sc.lights[sc.env_light];
+    for (int64_t i = 0; i < n; i++) {
+        Hit its;
+        its.sh = make_frame(ld3(nrm + 3 * i));
+        DirSample ds;
+        V3 r = env_sample(L, its, ld3(xi + 3 * i), ds);
+        s_dir[3 * i] = ds.d.x; s_dir[3 * i + 1] = ds.d.y; s_dir[3 * i + 2] = ds.d.z;
+        s_pdf[i] = ds.pdf;
+        s_val[3 * i] = r.x; s_val[3 * i + 1] = r.y; s_val[3 * i + 2] = r.z;
+        V3 d = ld3(dirs + 3 * i);
+        pdf[i] = env_pdf(L, d);
+        V3 v = env_eval(L, d);
+        val[3 * i] = v.x; val[3 * i + 1] = v.y; val[3 * i + 2] = v.z;
+    }
+    return 0;
+}
+
+int orc_env_miss(void* p, const dl_render_opts* opts, int64_t n, const float* dirs, const int32_t* depth,
+                 const float* bsdf_pdf, const uint8_t* is_diffuse, float* out) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    if (sc.env_light < 0) return 1;
+    uint32_t flags = opts ? opts->flags : 0;
+    for (int64_t i = 0; i < n; i++) {
+        float w;
+        V3 le = env_miss(sc, ld3(dirs + 3 * i), depth[i] == 0, is_diffuse[i] != 0, bsdf_pdf[i], flags, w);
+        out[3 * i] = w * le.x; out[3 * i + 1] = w * le.y; out[3 * i + 2] = w * le.z;
+    }
+    return 0;
+}
+
+int orc_camera_ray(void* p, int64_t n, const float* film, float* o, float* d) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    for (int64_t i = 0; i < n; i++) {
+        Ray r = camera_ray(sc.cam, P2{film[2 * i], film[2 * i + 1]});
+        o[3 * i] = r.o.x; o[3 * i + 1] = r.o.y; o[3 * i + 2] = r.o.z;
+        d[3 * i] = r.d.x; d[3 * i + 1] = r.d.y; d[3 * i + 2] = r.d.z;
+    }
+    return 0;
+}
+
+int orc_hit_data(void* p, int64_t n, const int32_t* prim, const float* bary, float* sn, float* gn, float* st,
+                 float* tuv) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    for (int64_t i = 0; i < n; i++) {
+        int mi = -1;
+        for (size_t k = 0; k < sc.meshes.size(); k++)
+            if (prim[i] >= sc.meshes[k].prim_offset &&
+                prim[i] < sc.meshes[k].prim_offset + (int64_t)sc.meshes[k].tri_count())
+                mi = (int)k;
+        if (mi < 0) return 1;
+        Hit its;
+        fill_hit(sc, mi, (int)(prim[i] - sc.meshes[mi].prim_offset), P2{bary[2 * i], bary[2 * i + 1]}, 1.f, its);
+        sn[3 * i] = its.sh.n.x; sn[3 * i + 1] = its.sh.n.y; sn[3 * i + 2] = its.sh.n.z;
+        gn[3 * i] = its.geo.n.x; gn[3 * i + 1] = its.geo.n.y; gn[3 * i + 2] = its.geo.n.z;
+        st[3 * i] = its.tan.x; st[3 * i + 1] = its.tan.y; st[3 * i + 2] = its.tan.z;
+        tuv[2 * i] = its.tuv.x; tuv[2 * i + 1] = its.tuv.y;
+    }
     return 0;
 }
 

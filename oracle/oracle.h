@@ -48,7 +48,9 @@ int orc_render_paths(void* scene, const dl_render_opts* opts, int32_t threads,
 int orc_li(void* scene, const dl_render_opts* opts, int64_t n, const int32_t* xys,
            float* L_out, float* pos_out, int32_t threads);
 
-/* BSDF::eval / pdf / sample on given local directions (see ref_bsdf_query). */
+/* BSDF::eval / pdf / sample on given local directions (see ref_bsdf_query);
+ * smp holds three uniform numbers per query: the 2D sample and the lobe
+ * coin that only aniso_ggx draws (aniso_ggx.cu:104-108). */
 int orc_bsdf_query(const dl_material_desc* m, int64_t n, const float* wi, const float* wo,
                    const float* smp, float* eval, float* pdf, float* s_wo, float* s_w,
                    float* s_eta, int32_t* s_measure);
@@ -64,6 +66,27 @@ int orc_emitter_sample(void* scene, const dl_render_opts* opts, int64_t n, const
 /* The envmap's alias table and pdf (src/tracer/emitter/envmap.cpp:59-141),
  * env_width x env_height entries each.  Returns nonzero without an envmap. */
 int orc_env_tables(void* scene, float* q, uint32_t* alias, float* pdf);
+
+/* Envmap::sampleDirection from three numbers xi at shading normals nrm, and
+ * pdfDirection / eval of dirs (include/optix/light/envmap.h:25-94).  Returns
+ * nonzero without an envmap. */
+int orc_env_query(void* scene, int64_t n, const float* xi, const float* nrm, const float* dirs,
+                  float* s_dir, float* s_pdf, float* s_val, float* pdf, float* val);
+
+/* __miss__radiance (src/optix/cuda/miss.cu:11-49): radiance of rays leaving
+ * along dirs after a bounce of depth[i] (0: camera ray) whose BSDF sample had
+ * pdf bsdf_pdf[i] and diffuse flag is_diffuse[i]. */
+int orc_env_miss(void* scene, const dl_render_opts* opts, int64_t n, const float* dirs,
+                 const int32_t* depth, const float* bsdf_pdf, const uint8_t* is_diffuse, float* out);
+
+/* Camera ray through film positions film (n x 2, pixel units). */
+int orc_camera_ray(void* scene, int64_t n, const float* film, float* o, float* d);
+
+/* Hit record of global triangle prim[i] at barycentrics bary[i]: shading
+ * normal, geometric normal, shading tangent (0: none) and texture
+ * coordinates (shader_common.h:21-143 for maps and texcoords). */
+int orc_hit_data(void* scene, int64_t n, const int32_t* prim, const float* bary, float* sn,
+                 float* gn, float* st, float* tuv);
 
 #ifdef __cplusplus
 }

@@ -162,6 +162,52 @@ class OracleScene:
             raise RuntimeError("oracle has no envmap tables")
         return q, alias, pdf
 
+    def env_query(self, xi, nrm, dirs):
+        """Envmap sampleDirection(xi, normal) -> s_dir, s_pdf, s_value and
+        pdfDirection / eval of dirs -> pdf, value."""
+        xi, nrm, dirs = (np.ascontiguousarray(a, np.float32) for a in (xi, nrm, dirs))
+        n = xi.shape[0]
+        out = dict(s_dir=np.empty((n, 3), np.float32), s_pdf=np.empty(n, np.float32),
+                   s_value=np.empty((n, 3), np.float32), pdf=np.empty(n, np.float32),
+                   value=np.empty((n, 3), np.float32))
+        if self.lib.orc_env_query(self.h, C.c_int64(n), _f(xi), _f(nrm), _f(dirs), _f(out["s_dir"]),
+                                  _f(out["s_pdf"]), _f(out["s_value"]), _f(out["pdf"]), _f(out["value"])) != 0:
+            raise RuntimeError("scene has no envmap")
+        return out
+
+    def env_miss(self, opts, dirs, depth, bsdf_pdf, is_diffuse):
+        """Radiance of rays that leave the scene along dirs (miss.cu)."""
+        dirs = np.ascontiguousarray(dirs, np.float32)
+        depth = np.ascontiguousarray(depth, np.int32)
+        bsdf_pdf = np.ascontiguousarray(bsdf_pdf, np.float32)
+        is_diffuse = np.ascontiguousarray(is_diffuse, np.uint8)
+        n = dirs.shape[0]
+        out = np.empty((n, 3), np.float32)
+        if self.lib.orc_env_miss(self.h, C.byref(opts), C.c_int64(n), _f(dirs), _f(depth), _f(bsdf_pdf),
+                                 _f(is_diffuse), _f(out)) != 0:
+            raise RuntimeError("scene has no envmap")
+        return out
+
+    def camera_ray(self, film):
+        film = np.ascontiguousarray(film, np.float32)
+        n = film.shape[0]
+        o = np.empty((n, 3), np.float32)
+        d = np.empty((n, 3), np.float32)
+        self.lib.orc_camera_ray(self.h, C.c_int64(n), _f(film), _f(o), _f(d))
+        return o, d
+
+    def hit_data(self, prim, bary):
+        """(shading normal, geometric normal, shading tangent, texcoords) of
+        global triangles prim at barycentrics bary."""
+        prim = np.ascontiguousarray(prim, np.int32)
+        bary = np.ascontiguousarray(bary, np.float32)
+        n = prim.shape[0]
+        sn, gn, st = (np.empty((n, 3), np.float32) for _ in range(3))
+        tuv = np.empty((n, 2), np.float32)
+        if self.lib.orc_hit_data(self.h, C.c_int64(n), _f(prim), _f(bary), _f(sn), _f(gn), _f(st), _f(tuv)) != 0:
+            raise RuntimeError("bad triangle index")
+        return sn, gn, st, tuv
+
 
 class RefScene:
     """The reference's own CPU code bound to one scene (x86 container only)."""
@@ -226,9 +272,16 @@ class RefScene:
 
 
 def bsdf_query(lib_kind: str, mat, wi, wo, smp):
-    """BSDF eval/pdf/sample through the oracle ("oracle") or the reference ("ref")."""
+    """BSDF eval/pdf/sample through the oracle ("oracle") or the reference's
+    CPU BSDFs ("ref").  smp: n x 2 (the 2D sample) or n x 3 (then the lobe
+    coin that only aniso_ggx draws; the reference's CPU BSDFs take the
+    first two)."""
     wi, wo, smp = (np.ascontiguousarray(a, np.float32) for a in (wi, wo, smp))
     n = wi.shape[0]
+    if lib_kind == "oracle" and smp.shape[1] == 2:
+        smp = np.ascontiguousarray(np.concatenate([smp, np.zeros((n, 1), np.float32)], axis=1))
+    elif lib_kind != "oracle" and smp.shape[1] == 3:
+        smp = np.ascontiguousarray(smp[:, :2])
     out = dict(eval=np.empty((n, 3), np.float32), pdf=np.empty(n, np.float32),
                wo=np.empty((n, 3), np.float32), weight=np.empty((n, 3), np.float32),
                eta=np.empty(n, np.float32), measure=np.empty(n, np.int32))

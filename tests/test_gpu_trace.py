@@ -1,6 +1,9 @@
-"""First-hit and shadow-ray parity of the GPU traversal (dl_trace_closest /
-dl_trace_any) against the oracle's octree (and the reference's golden
-vectors).
+"""First-hit and shadow-ray parity of the GPU traversal against the oracle's
+octree (and the reference's golden vectors), for both GPU traversal paths:
+"batch" -- the stand-alone ray-batch kernels of dl_trace_closest /
+dl_trace_any -- and "wavefront" -- dl_trace_closest_wavefront /
+dl_trace_any_wavefront, which run the renderer's own persistent k_traverse
+kernels, the ones dl_render launches for extension and shadow rays.
 
 Bar: the same triangle id for every ray, hit t/u/v bit-identical (the device
 runs the reference's Moller-Trumbore with the same float operations),
@@ -61,37 +64,43 @@ def scene_cases():
 
 
 CASES = scene_cases()
+KERNELS = ["batch", "wavefront"]
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_first_hit_matches_oracle(ctx, name):
+def test_first_hit_matches_oracle(ctx, name, kernel):
     sc = CASES[name]
     gs = api.Scene.from_data(ctx, sc)
     orc = po.OracleScene(sc)
+    wf = kernel == "wavefront"
     rays = mg.seeded_rays(sc, 60000, seed=17)
-    keep = compare_closest(gs.trace_closest(rays), orc.trace_closest(rays))
+    keep = compare_closest(gs.trace_closest(rays, wavefront=wf), orc.trace_closest(rays))
     # any-hit on the same rays with a finite tmax halfway to the closest hit
     prim, t, _, _ = orc.trace_closest(rays)
     r2 = rays.copy()
     hit = prim >= 0
     r2[hit, 7] = np.where(np.arange(hit.sum()) % 2 == 0, 0.5 * t[hit], 1.5 * t[hit])
-    g_occ = gs.trace_any(r2)
+    g_occ = gs.trace_any(r2, wavefront=wf)
     o_occ = orc.trace_any(r2)
     near_tmax = hit & (np.abs(r2[:, 7] - t) <= TIE * np.abs(t))
     ok = keep & ~near_tmax
     np.testing.assert_array_equal(g_occ[ok], o_occ[ok])
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("name", ["cornell", "refspheres"])
-def test_first_hit_matches_reference_golden(ctx, name):
+def test_first_hit_matches_reference_golden(ctx, name, kernel):
     sc = mg.fixture_scenes()[name]
     g = np.load(os.path.join(GOLDEN, f"{name}_trace.npz"))
     gs = api.Scene.from_data(ctx, sc)
-    compare_closest(gs.trace_closest(g["rays"]), (g["prim"], g["t"], g["u"], g["v"]))
-    np.testing.assert_array_equal(gs.trace_any(g["rays"]), g["occ"])
+    wf = kernel == "wavefront"
+    compare_closest(gs.trace_closest(g["rays"], wavefront=wf), (g["prim"], g["t"], g["u"], g["v"]))
+    np.testing.assert_array_equal(gs.trace_any(g["rays"], wavefront=wf), g["occ"])
 
 
-def test_full_material_scene_first_hits(ctx):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_full_material_scene_first_hits(ctx, kernel):
     # the 327,682-triangle scene, 100k seeded rays
     sc = scenes.material_spheres(width=320, height=180)
     gs = api.Scene.from_data(ctx, sc)
@@ -100,12 +109,25 @@ def test_full_material_scene_first_hits(ctx):
     assert info.bvh_depth <= 64
     orc = po.OracleScene(sc)
     rays = mg.seeded_rays(sc, 100000, seed=23)
-    compare_closest(gs.trace_closest(rays), orc.trace_closest(rays))
+    compare_closest(gs.trace_closest(rays, wavefront=kernel == "wavefront"), orc.trace_closest(rays))
 
 
-def test_edge_cases(ctx):
+def test_wavefront_rays_need_the_render_tmin(ctx):
     sc = scenes.cornell()
     gs = api.Scene.from_data(ctx, sc)
+    rays = mg.seeded_rays(sc, 64, seed=3)
+    rays[5, 3] = 1e-3
+    with pytest.raises(RuntimeError, match="tmin"):
+        gs.trace_closest(rays, wavefront=True)
+    with pytest.raises(RuntimeError, match="tmin"):
+        gs.trace_any(rays, wavefront=True)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_edge_cases(ctx, kernel):
+    sc = scenes.cornell()
+    gs = api.Scene.from_data(ctx, sc)
+    wf = kernel == "wavefront"
     orc = po.OracleScene(sc)
     rays = np.zeros((7, 8), np.float32)
     rays[:, 0:3] = (0.1, 0.2, 0.05)
@@ -122,17 +144,22 @@ def test_edge_cases(ctx):
     rays[5, 4:7] = (0, -1, 0)                # from above, through the ceiling
     rays[6, 0:3] = (0.0, 0.0, 0.0)
     rays[6, 4:7] = (0, 0, -1)                # exactly on the back wall's diagonal
-    g = gs.trace_closest(rays)
+    if wf:
+        # the renderer's traversal starts every ray at 1e-4: the tmin > tmax
+        # case becomes an empty [1e-4, 0] interval
+        rays[3, 3], rays[3, 7] = 1e-4, 0.0
+    g = gs.trace_closest(rays, wavefront=wf)
     o = orc.trace_closest(rays)
     keep = compare_closest(g, o, max_ambiguous=1.0 / 7)
     assert keep[:6].all()
     assert (g[0][[0, 3, 4]] == -1).all()
     assert g[0][6] >= 0                      # the diagonal ray hits one of the two triangles
-    assert gs.trace_closest(rays[:0])[0].shape == (0,)
-    np.testing.assert_array_equal(gs.trace_any(rays), orc.trace_any(rays))
+    assert gs.trace_closest(rays[:0], wavefront=wf)[0].shape == (0,)
+    np.testing.assert_array_equal(gs.trace_any(rays, wavefront=wf), orc.trace_any(rays))
 
 
-def test_empty_scene_misses(ctx):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_empty_scene_misses(ctx, kernel):
     sc = scenes.SceneData("empty")
     sc.materials.append(scenes.Material())
     sc.camera = scenes.Camera(width=8, height=8)
@@ -140,6 +167,8 @@ def test_empty_scene_misses(ctx):
     rays = np.zeros((4, 8), np.float32)
     rays[:, 6] = 1
     rays[:, 7] = np.inf
-    prim, t, u, v = gs.trace_closest(rays)
+    rays[:, 3] = 1e-4
+    wf = kernel == "wavefront"
+    prim, t, u, v = gs.trace_closest(rays, wavefront=wf)
     assert (prim == -1).all()
-    assert (gs.trace_any(rays) == 0).all()
+    assert (gs.trace_any(rays, wavefront=wf) == 0).all()
