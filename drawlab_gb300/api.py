@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import atexit
 import ctypes as C
+import os
 import weakref
 from pathlib import Path
 
@@ -16,7 +17,10 @@ import numpy as np
 from . import abi
 from .scenes import SceneData
 
-_LIB_PATH = Path(__file__).resolve().parent / "_build" / "libdlgpu.so"
+# the in-tree library; DRAWLAB_GB300_LIBRARY selects another build of it (the
+# bounds-checked variant of drawlab_gb300.build --checked)
+_LIB_PATH = Path(os.environ.get("DRAWLAB_GB300_LIBRARY",
+                                str(Path(__file__).resolve().parent / "_build" / "libdlgpu.so")))
 _lib = None
 
 # every entry point of include/drawlab.h: name -> (restype, argtypes)
@@ -41,6 +45,8 @@ SIGNATURES = {
     "dl_trace_any_wavefront": (C.c_int, [_vp, _vp, _i64, _vp]),
     "dl_bsdf_query": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "dl_scene_env_query": (C.c_int, [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "dl_measure_l2_read_bandwidth": (C.c_int, [_vp, _i64, _i32, _vp]),
+    "dl_scene_emitter_sample": (C.c_int, [_vp, C.c_uint32, _i64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "dl_render": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film": (C.c_int, [_vp, _vp, _vp]),
     "dl_render_film_device": (C.c_int, [_vp, _vp, _vp]),
@@ -170,6 +176,12 @@ class Context:
         s = abi.dl_stats()
         self.check(self.lib.dl_stats_get(self.h, C.byref(s)))
         return s
+
+    def l2_read_gbs(self, bytes_: int = 64 << 20, passes: int = 40) -> float:
+        """L2 -> SM read bandwidth (GB/s) measured by the library's probe."""
+        out = C.c_double()
+        self.check(self.lib.dl_measure_l2_read_bandwidth(self.h, bytes_, passes, C.byref(out)))
+        return out.value
 
     def bsdf_query(self, mat, wi, wo, smp):
         """BSDF eval / pdf of (wi, wo) and sample(wi) from smp (n x 3) of one
@@ -309,6 +321,21 @@ class Scene:
         fn = self.ctx.lib.dl_trace_any_wavefront if wavefront else self.ctx.lib.dl_trace_any
         self.ctx.check(fn(self.h, _ptr(rays), n, _ptr(occ)))
         return occ
+
+    def emitter_sample(self, opts, pts, nrm, smp):
+        """Scene::sampleEmitterDirection without visibility on the GPU:
+        (d, dist, pdf, spec, light)."""
+        pts, nrm, smp = (np.ascontiguousarray(a, np.float32) for a in (pts, nrm, smp))
+        n = pts.shape[0]
+        d = np.empty((n, 3), np.float32)
+        dist = np.empty(n, np.float32)
+        pdf = np.empty(n, np.float32)
+        spec = np.empty((n, 3), np.float32)
+        light = np.empty(n, np.int32)
+        self.ctx.check(self.ctx.lib.dl_scene_emitter_sample(self.h, opts.flags, n, _ptr(pts), _ptr(nrm), _ptr(smp),
+                                                            _ptr(d), _ptr(dist), _ptr(pdf), _ptr(spec),
+                                                            _ptr(light)))
+        return d, dist, pdf, spec, light
 
     def env_query(self, xi, nrm, dirs):
         """The envmap's sampleDirection(xi, normal) -> (dir, pdf, value) and

@@ -5,7 +5,12 @@ CUDA sources are compiled by nvcc for sm_103a only; host C++ by g++ with
 operations).  Translation units compile in parallel; nothing is rebuilt when
 sources are unchanged.
 
-    python -m drawlab_gb300.build [--force] [--verbose]
+    python -m drawlab_gb300.build [--force] [--verbose] [--checked]
+
+--checked builds the bounds-checked variant (-DDL_CHECKS: every queue, slot,
+path, node and triangle index checked before its access; a violation sets an
+error bit and the call fails with a message) into _build/checked/, for tests;
+DRAWLAB_GB300_LIBRARY points drawlab_gb300.api at it.
 """
 from __future__ import annotations
 
@@ -21,6 +26,8 @@ REPO = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libdlgpu.so"
+CHECKED_BUILD = BUILD / "checked"
+CHECKED_LIB = CHECKED_BUILD / "libdlgpu_checked.so"
 
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc") if (CUDA_HOME / "bin" / "nvcc").exists() else "nvcc"
@@ -53,39 +60,43 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link libdlgpu.so; returns its path."""
-    BUILD.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile and link libdlgpu.so (or, checked=True, the bounds-checked
+    libdlgpu_checked.so); returns its path."""
+    out_dir = CHECKED_BUILD if checked else BUILD
+    lib_path = CHECKED_LIB if checked else LIB
+    out_dir.mkdir(parents=True, exist_ok=True)
+    defs = ["-DDL_CHECKS"] if checked else []
     hdrs = _headers()
     jobs, objs = [], []
     for src in CU_SOURCES:
         s = CSRC / src
-        o = BUILD / (src + ".o")
+        o = out_dir / (src + ".o")
         objs.append(o)
         if force or _stale(o, [s, *hdrs]):
             extra = ["-Xptxas", "-v"] if verbose else []
-            jobs.append([NVCC, *NVCC_FLAGS, *extra, "-c", str(s), "-o", str(o)])
+            jobs.append([NVCC, *NVCC_FLAGS, *defs, *extra, "-c", str(s), "-o", str(o)])
     for src in CPP_SOURCES:
         s = CSRC / src
-        o = BUILD / (src + ".o")
+        o = out_dir / (src + ".o")
         objs.append(o)
         if force or _stale(o, [s, *hdrs]):
-            jobs.append([CXX, *CXX_FLAGS, "-c", str(s), "-o", str(o)])
+            jobs.append([CXX, *CXX_FLAGS, *defs, "-c", str(s), "-o", str(o)])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(_run, jobs))
-    if force or jobs or not LIB.exists():
-        tmp = LIB.with_suffix(".so.tmp%d" % os.getpid())
+    if force or jobs or not lib_path.exists():
+        tmp = lib_path.with_suffix(".so.tmp%d" % os.getpid())
         _run([NVCC, *GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "shared",
               "-Xcompiler", "-pthread"])
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib_path)
     if verbose:
         for l in logs:
             if l.strip():
                 print(l)
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="--verbose" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="--verbose" in sys.argv, checked="--checked" in sys.argv))

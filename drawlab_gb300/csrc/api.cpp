@@ -222,6 +222,9 @@ int dl_trace_closest(dl_scene* S, const float* rays, int64_t n, int32_t* prim_id
         DL_CUDA(cudaMemcpyAsync(&err, B.occ.ptr, 4, cudaMemcpyDeviceToHost, st));
         DL_CUDA(cudaEventRecord(ctx->ev1, st));
         DL_CUDA(cudaStreamSynchronize(st));
+        if (err & 4u)
+            throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "bounds check failed: a node or triangle index outside its array "
+                                                   "(bounds-checked build)");
         if (err) throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         const float* h = B.stage.as<float>();
         for (int64_t i = 0; i < n; i++) {
@@ -255,6 +258,9 @@ int dl_trace_any(dl_scene* S, const float* rays, int64_t n, uint8_t* occluded) {
         DL_CUDA(cudaMemcpyAsync(&err, B.occ.ptr, 4, cudaMemcpyDeviceToHost, st));
         DL_CUDA(cudaEventRecord(ctx->ev1, st));
         DL_CUDA(cudaStreamSynchronize(st));
+        if (err & 4u)
+            throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "bounds check failed: a node or triangle index outside its array "
+                                                   "(bounds-checked build)");
         if (err) throw dl::Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
@@ -340,6 +346,27 @@ int dl_scene_env_query(dl_scene* S, int64_t n, const float* xi, const float* nrm
         need(n >= 0 && (n == 0 || (xi && nrm && dirs && s_dir && s_pdf && s_value && pdf && value)),
              "bad query buffers");
         dl::env_query(S, n, xi, nrm, dirs, s_dir, s_pdf, s_value, pdf, value);
+    });
+}
+
+int dl_scene_emitter_sample(dl_scene* S, uint32_t flags, int64_t n, const float* pts, const float* nrm,
+                            const float* smp, float* d, float* dist, float* pdf, float* spec, int32_t* light) {
+    if (!S) return DL_ERR_INVALID_ARG;
+    return guard(S->ctx, [&] {
+        need(n >= 0 && n < ((int64_t)1 << 31) && (n == 0 || (pts && nrm && smp && d && dist && pdf && spec && light)),
+             "bad query buffers");
+        need((flags & ~(uint32_t)(DL_RENDER_FIX_POINT_LIGHT | DL_RENDER_POWER_LIGHT_PICK)) == 0, "unsupported flags");
+        dl::emitter_query(S, flags, n, pts, nrm, smp, d, dist, pdf, spec, light);
+    });
+}
+
+int dl_measure_l2_read_bandwidth(dl_context* ctx, int64_t bytes, int32_t passes, double* gbs) {
+    if (!ctx) return DL_ERR_INVALID_ARG;
+    return guard(ctx, [&] {
+        need(gbs != nullptr && bytes >= (1 << 20) && bytes <= ((int64_t)1 << 32) && passes >= 1 && passes <= 1000,
+             "bad L2 probe arguments");
+        DL_CUDA(cudaSetDevice(ctx->device));
+        *gbs = dl::measure_l2_read(ctx, bytes, passes);
     });
 }
 

@@ -164,6 +164,12 @@ __device__ __forceinline__ int trace_closest(const DevScene& sc, float3 o, float
     int node = 0;
     for (;;) {
         if (node >= 0) {
+#ifdef DL_CHECKS
+            if (node >= sc.num_nodes) {  // bounds-checked build: bit 4 of the error word
+                err |= 4u;
+                break;
+            }
+#endif
             const float4* np = sc.nodes + 4 * node;
             float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
             int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
@@ -189,6 +195,12 @@ __device__ __forceinline__ int trace_closest(const DevScene& sc, float3 o, float
         } else {
             int ref = ~node;
             int first = ref >> 4, count = (ref & 15) + 1;
+#ifdef DL_CHECKS
+            if (first < 0 || first + count > sc.num_tris) {
+                err |= 4u;
+                count = 0;
+            }
+#endif
             for (int k = 0; k < count; k++) {
                 const float4* tp = sc.tris + 3 * (first + k);
                 float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
@@ -221,6 +233,12 @@ __device__ __forceinline__ bool trace_any(const DevScene& sc, float3 o, float3 d
     int node = 0;
     for (;;) {
         if (node >= 0) {
+#ifdef DL_CHECKS
+            if (node >= sc.num_nodes) {  // bounds-checked build: bit 4 of the error word
+                err |= 4u;
+                break;
+            }
+#endif
             const float4* np = sc.nodes + 4 * node;
             float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
             int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
@@ -246,6 +264,12 @@ __device__ __forceinline__ bool trace_any(const DevScene& sc, float3 o, float3 d
         } else {
             int ref = ~node;
             int first = ref >> 4, count = (ref & 15) + 1;
+#ifdef DL_CHECKS
+            if (first < 0 || first + count > sc.num_tris) {
+                err |= 4u;
+                count = 0;
+            }
+#endif
             for (int k = 0; k < count; k++) {
                 const float4* tp = sc.tris + 3 * (first + k);
                 float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);

@@ -79,6 +79,7 @@ struct DevScene {
     const DevTexture* __restrict__ textures;
     const float2* __restrict__ texcoords;  // per vertex (global index)
     int num_tris;
+    int num_nodes;
     int num_lights;
     DevCamera cam;
     // environment light (env_light < 0: none).  Texels rgb+pad, row 0 at the

@@ -201,3 +201,52 @@ void env_query(dl_scene* S, int64_t n, const float* xi, const float* nrm, const 
 }
 
 }  // namespace dl
+
+namespace dl {
+
+// ------------------------------------------------------ L2 read bandwidth
+// Streams a buffer that fits in L2 with L2-only loads (ld.global.cg: no L1
+// allocation), `passes` times over, after one warm-up pass: the L2 -> SM
+// read bandwidth that bounds the traversal kernels' node and triangle
+// fetches when the BVH is L2-resident.  One pass reads the buffer once in
+// total over all threads; the xor of what a thread read is stored only if
+// it equals `sentinel` (never, in practice), which keeps the loads live.
+__global__ void __launch_bounds__(256) k_l2_read(const float4* __restrict__ buf, int64_t n4, int passes,
+                                                  unsigned sentinel, unsigned* __restrict__ out) {
+    unsigned acc = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int p = 0; p < passes; p++) {
+        // start each pass at a different offset so a thread reads other lines
+        const int64_t start = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x + (int64_t)p * 4099 * 32) % stride;
+        for (int64_t i = start; i < n4; i += stride) {
+            float4 v;
+            asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];"
+                         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                         : "l"(buf + i));
+            acc ^= __float_as_uint(v.x) ^ __float_as_uint(v.y) ^ __float_as_uint(v.z) ^ __float_as_uint(v.w);
+        }
+    }
+    if (acc == sentinel) out[0] = acc;
+}
+
+double measure_l2_read(dl_context* ctx, int64_t bytes, int passes) {
+    cudaStream_t st = ctx->stream;
+    const int64_t n4 = bytes / 16;
+    Scratch buf((size_t)n4 * 16 + 256);
+    float4* d = buf.at<float4>(0);
+    unsigned* out = buf.at<unsigned>((size_t)n4 * 16);
+    DL_CUDA(cudaMemsetAsync(d, 0x3c, (size_t)n4 * 16, st));
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
+    const int grid = sms * 8;
+    k_l2_read<<<grid, 256, 0, st>>>(d, n4, 1, 0x9e3779b9u, out);  // warm-up: the buffer into L2
+    DL_CUDA(cudaEventRecord(ctx->ev0, st));
+    k_l2_read<<<grid, 256, 0, st>>>(d, n4, passes, 0x9e3779b9u, out);
+    DL_CUDA(cudaEventRecord(ctx->ev1, st));
+    DL_CUDA(cudaGetLastError());
+    DL_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    DL_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    return (double)n4 * 16.0 * passes / (ms * 1e-3) / 1e9;
+}
+
+}  // namespace dl

@@ -105,6 +105,7 @@ struct __align__(32) GuideRec {
 
 struct RenderParams {
     DevRequest r0;                 // the request of a single render
+    int capacity;                  // path slots (queue and record arrays hold this many entries)
     const DevRequest* reqs;        // batch: request table (pid_first ascending)
     int num_reqs;
     SlotRec* rec;    // per slot: ray, hit, path state
@@ -132,6 +133,28 @@ template <bool kMulti>
 __device__ __forceinline__ const DevRequest& request(const RenderParams& P, int rid) {
     if (kMulti) return P.reqs[rid];
     return P.r0;
+}
+
+// Bounds-checked build (compiled with -DDL_CHECKS): before each access whose
+// index comes from a queue, a counter or a record -- path slots, queue
+// positions, path indices, BVH nodes and triangles -- the index is checked
+// against its array; a violation sets kErrBounds in the render's error word
+// and the access is skipped.  Without DL_CHECKS the checks compile to
+// nothing.
+constexpr unsigned kErrBounds = 4u;
+#ifdef DL_CHECKS
+__device__ __forceinline__ bool in_bounds(bool ok, unsigned int* err) {
+    if (!ok) atomicOr(err, kErrBounds);
+    return ok;
+}
+#define DL_IN_BOUNDS(cond, err) in_bounds((cond), (err))
+#else
+#define DL_IN_BOUNDS(cond, err) true
+#endif
+constexpr const char* kBoundsMessage = "bounds check failed: a queue, slot, path, node or triangle index "
+                                        "outside its array (bounds-checked build)";
+__device__ __forceinline__ bool slot_ok(const RenderParams& P, int slot) {
+    return DL_IN_BOUNDS(slot >= 0 && slot < P.capacity, &P.cnt->err);
 }
 
 // Request of batch path `pid`: the last request whose first path is <= pid.
@@ -196,6 +219,7 @@ __device__ __forceinline__ unsigned long long path_index(const int4& m) {
 // tmin = kRayEps).
 template <bool kMulti>
 __device__ void start_path(const RenderParams& P, int slot, unsigned long long pid) {
+    if (!slot_ok(P, slot) || !DL_IN_BOUNDS(pid < P.cnt->pass_total, &P.cnt->err)) return;
     const int rid = kMulti ? find_request(P, pid) : 0;
     const DevRequest& R = request<kMulti>(P, rid);
     const DevCamera& cam = R.sc.cam;
@@ -253,6 +277,7 @@ __device__ void start_path(const RenderParams& P, int slot, unsigned long long p
 // Radiance of ended path `pid` (slot `slot`): into the sample buffer at its
 // path index (the film kernel gathers it), or as its Li.
 __device__ __forceinline__ void store_sample(const RenderParams& P, unsigned long long pid, float3 L, int slot) {
+    if (!slot_ok(P, slot) || !DL_IN_BOUNDS(pid < P.cnt->pass_total, &P.cnt->err)) return;
     if (P.mode == 1) {
         P.li_L[3 * pid] = L.x;
         P.li_L[3 * pid + 1] = L.y;
@@ -268,6 +293,7 @@ __device__ __forceinline__ void store_sample(const RenderParams& P, unsigned lon
 // A shadow ray of an ended path was unoccluded: add its contribution to the
 // stored sample.  One shadow ray per path at a time, so no atomics.
 __device__ __forceinline__ void add_to_sample(const RenderParams& P, unsigned long long pid, float4 c) {
+    if (!DL_IN_BOUNDS(pid < P.cnt->pass_total, &P.cnt->err)) return;
     if (P.mode == 1) {
         P.li_L[3 * pid] = __fadd_rn(P.li_L[3 * pid], c.x);
         P.li_L[3 * pid + 1] = __fadd_rn(P.li_L[3 * pid + 1], c.y);
@@ -463,7 +489,8 @@ __device__ __forceinline__ float3 sample_emitter(const DevRequest& R, float3 its
 template <bool kMulti>
 __global__ void k_init(RenderParams P, int capacity) {
     const unsigned long long total = P.cnt->pass_total;
-    const int n = (int)min((unsigned long long)capacity, total);
+    int n = (int)min((unsigned long long)capacity, total);
+    if (!DL_IN_BOUNDS(capacity <= P.capacity, &P.cnt->err)) n = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         P.cnt->next_path = (unsigned long long)n;
         P.cnt->ext[0] = n;
@@ -496,7 +523,8 @@ constexpr int kSmemStack = 8;      // top traversal-stack entries per thread kep
 template <bool kCount, bool kAny, bool kMulti>
 __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
     const int q = p ^ 1;
-    const int n = kAny ? P.cnt->shadow[p] : P.cnt->ext[p];
+    int n = kAny ? P.cnt->shadow[p] : P.cnt->ext[p];
+    if (!DL_IN_BOUNDS(n >= 0 && n <= P.capacity, &P.cnt->err)) n = 0;
     unsigned int* work = kAny ? &P.cnt->work_sh : &P.cnt->work_ext;
     constexpr int kDests = kAny ? 1 : kNumMaterialTypes + 1;
     __shared__ int s_qbuf[kTraverseWarps][kDests][kStage];
@@ -566,15 +594,17 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
             if (need) {
                 idx = (int)min(mine, (unsigned)n);
                 if (mine < (unsigned)n) {
-                    float4 ro, rd;
+                    float4 ro = make_float4(0.f, 0.f, 0.f, 0.f), rd = make_float4(0.f, 0.f, 0.f, -1.f);
                     if (kAny) {
                         ro = P.sh_o[idx];
                         rd = P.sh_d[idx];
                     } else {
                         slot = P.ext_q[p][idx];
-                        RayRec r = P.rec[slot].ray;
-                        ro = r.o;
-                        rd = r.d;
+                        if (slot_ok(P, slot)) {
+                            RayRec r = P.rec[slot].ray;
+                            ro = r.o;
+                            rd = r.d;
+                        }
                     }
                     o = xyz(ro);
                     d = xyz(rd);
@@ -603,6 +633,13 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
         if (has) {
             // descend inner nodes until a leaf (or the end of the traversal)
             while (node >= 0 && node != kDone) {
+#ifdef DL_CHECKS
+                const int num_nodes = kMulti ? P.reqs[rid].sc.num_nodes : P.r0.sc.num_nodes;
+                if (!DL_IN_BOUNDS(node < num_nodes, &P.cnt->err)) {
+                    node = kDone;
+                    break;
+                }
+#endif
                 const float4* np = nodes + 4 * node;
                 float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
                 int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
@@ -630,6 +667,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 // leaf: test its triangles (the reference's Moller-Trumbore)
                 int ref = ~node;
                 int first = ref >> 4, count = (ref & 15) + 1;
+                if (!DL_IN_BOUNDS(first >= 0 && first + count <= ntris, &P.cnt->err)) count = 0;
                 bool any = false;
                 for (int k = 0; k < count; k++) {
                     const float4* tp = tris + 3 * (first + k);
@@ -663,12 +701,14 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         float4 c = P.sh_c[idx];
                         int target = __float_as_int(c.w);
                         if (target >= 0) {
-                            PathRec pr = P.rec[target].path;
-                            pr.L = make_float4(__fadd_rn(pr.L.x, c.x), __fadd_rn(pr.L.y, c.y),
-                                               __fadd_rn(pr.L.z, c.z), pr.L.w);
-                            P.rec[target].path = pr;
-                            // NEE at the newest guided vertex feeds the record before it
-                            if (P.guided) credit(P, P.grec[target], xyz(c), false);
+                            if (slot_ok(P, target)) {
+                                PathRec pr = P.rec[target].path;
+                                pr.L = make_float4(__fadd_rn(pr.L.x, c.x), __fadd_rn(pr.L.y, c.y),
+                                                   __fadd_rn(pr.L.z, c.z), pr.L.w);
+                                P.rec[target].path = pr;
+                                // NEE at the newest guided vertex feeds the record before it
+                                if (P.guided) credit(P, P.grec[target], xyz(c), false);
+                            }
                         } else {
                             add_to_sample(P, (unsigned long long)(unsigned)(-1 - target), c);
                         }
@@ -683,7 +723,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                         hr.h = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
                         dest = kMissQueue;
                     }
-                    P.rec[slot].hit = hr;
+                    if (slot_ok(P, slot)) P.rec[slot].hit = hr;
                 }
                 has = false;
             }
@@ -703,7 +743,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                     int base = 0;
                     if (lane == 0) base = atomicAdd(&P.cnt->mat[p][dd].n, 32);
                     base = __shfl_sync(0xffffffffu, base, 0);
-                    P.mat_q[dd][base + lane] = buf[lane];
+                    if (DL_IN_BOUNDS(base + 32 <= P.capacity, &P.cnt->err)) P.mat_q[dd][base + lane] = buf[lane];
                     const int rest = c - 32;
                     const int v = lane < rest ? buf[32 + lane] : 0;
                     __syncwarp();
@@ -723,7 +763,8 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
             int base = 0;
             if (lane == 0) base = atomicAdd(&P.cnt->mat[p][dd].n, c);
             base = __shfl_sync(0xffffffffu, base, 0);
-            if (lane < c) P.mat_q[dd][base + lane] = s_qbuf[warp][dd][lane];
+            if (lane < c && DL_IN_BOUNDS(base + c <= P.capacity, &P.cnt->err))
+                P.mat_q[dd][base + lane] = s_qbuf[warp][dd][lane];
         }
     }
     if (err) atomicOr(&P.cnt->err, err);
@@ -750,7 +791,8 @@ __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
         P.cnt->work_ext = 0;
         P.cnt->work_sh = 0;
     }
-    const int n = P.cnt->mat[p][kMissQueue].n;
+    int n = P.cnt->mat[p][kMissQueue].n;
+    if (!DL_IN_BOUNDS(n >= 0 && n <= P.capacity, &P.cnt->err)) n = 0;
     // Every queued miss starts a new path in its slot.  A warp's entries over
     // the whole launch are known (i0 = w0 + j * stride, all lanes but the
     // last round's tail), so it claims their path indices, and queue
@@ -775,6 +817,7 @@ __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
         int i = i0 + lane_id();
         bool active = i < n;
         int slot = active ? P.mat_q[kMissQueue][i] : 0;
+        if (active && !slot_ok(P, slot)) active = false;
         if (active) {
             PathRec pr = P.rec[slot].path;
             int4 m = P.rec[slot].meta.m;
@@ -805,7 +848,7 @@ __global__ void __launch_bounds__(kThreads) k_miss(RenderParams P, int p) {
         const unsigned long long pid = pid0 + (unsigned long long)r;
         if (active && pid < total) {
             start_path<kMulti>(P, slot, pid);
-            P.ext_q[q][e0 + r] = slot;
+            if (DL_IN_BOUNDS(e0 + r < P.capacity, &P.cnt->err)) P.ext_q[q][e0 + r] = slot;
         }
         done_before += min(32, n - i0);
     }
@@ -834,7 +877,8 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     const int q = p ^ 1;
     const int lane = lane_id();
-    const int n = P.cnt->mat[p][T].n;
+    int n = P.cnt->mat[p][T].n;
+    if (!DL_IN_BOUNDS(n >= 0 && n <= P.capacity, &P.cnt->err)) n = 0;
     // guided: each warpgroup walks whole 128-row tiles (every thread takes
     // part in the network's warpgroup-wide steps); otherwise each warp walks
     // 32 rows
@@ -853,6 +897,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
         int i = i0 + (kGuided ? tc_row() : lane);
         bool active = i < n;
         int slot = active ? P.mat_q[T][i] : 0;
+        if (active && !slot_ok(P, slot)) active = false;
         bool cont = false, emit = false, done = false;
         float4 sh_o = make_float4(0.f, 0.f, 0.f, 0.f), sh_d = sh_o, sh_c = sh_o;
         // ---- phase 1: emitter hit, Russian roulette, depth limit
@@ -885,6 +930,8 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
             rid = flags >> kReqShift;
             const DevRequest& R = request<kMulti>(P, rid);
             const DevScene& sc = R.sc;
+            if (!DL_IN_BOUNDS(__float_as_int(hit.w) >= 0 && __float_as_int(hit.w) < sc.num_tris, &P.cnt->err))
+                hit.w = __int_as_float(0);
             h = hit_info(sc, __float_as_int(hit.w), hit.y, hit.z);
             if (T == MAT_DIFFUSE || T == MAT_ANISO_GGX) {
                 const DevMaterial& mt = sc.materials[sc.meshes[h.mesh].material];
@@ -1113,7 +1160,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
             }
         }
         int sp = warp_push(&P.cnt->shadow[q], emit);
-        if (emit) {
+        if (emit && DL_IN_BOUNDS(sp < P.capacity, &P.cnt->err)) {
             P.sh_o[sp] = sh_o;
             P.sh_d[sp] = sh_d;
             P.sh_c[sp] = sh_c;
@@ -1121,7 +1168,7 @@ __global__ void __launch_bounds__(kGuided ? kTcThreads : kThreads) k_material(Re
         bool fresh = regenerate<kMulti>(P, slot, done);
         bool push = cont || fresh;
         int e = warp_push(&P.cnt->ext[q], push);
-        if (push) P.ext_q[q][e] = slot;
+        if (push && DL_IN_BOUNDS(e < P.capacity, &P.cnt->err)) P.ext_q[q][e] = slot;
     }
     if (kGuided) guide_tc_end(*reinterpret_cast<GuideTcSmem*>(dyn_smem), mma_phase);
 }
@@ -1390,6 +1437,7 @@ static void launch_iteration(const RenderParams& P, int p, cudaStream_t st, int 
 }
 
 static void bind_pool(RenderParams& P, const RenderBuffers& B) {
+    P.capacity = (int)B.capacity;
     P.rec = B.rec.as<SlotRec>();
     P.pos = B.pos.as<float2>();
     P.ext_q[0] = B.ext_q[0].as<int>();
@@ -1533,6 +1581,7 @@ static void run_wavefront(dl_context* ctx, RenderParams& P, int64_t cap, bool mu
                     kms[j] += ms;
                 }
         }
+        if (hc->err & kErrBounds) throw Error(DL_ERR_QUEUE_OVERFLOW, kBoundsMessage);
         if (hc->err & kErrTensorWait) throw Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in a guided kernel");
         if (hc->err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         if (hc->ext[0] == 0 && hc->shadow[0] == 0 && hc->next_path >= total) break;
@@ -1906,6 +1955,7 @@ void render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t s
     std::memset(&P, 0, sizeof(P));
     P.r0 = make_request(S, o);
     P.mode = 1;
+    P.capacity = (int)slots;
     size_t c = (size_t)slots;
     char* b = static_cast<char*>(pool);
     P.cnt = reinterpret_cast<RenderCounters*>(b);
@@ -1947,6 +1997,7 @@ void render_li_fixed(dl_scene* S, const dl_render_opts& o, void* pool, int64_t s
         DL_CUDA(cudaGetLastError());
         DL_CUDA(cudaMemcpyAsync(&hc, P.cnt, sizeof(RenderCounters), cudaMemcpyDeviceToHost, st));
         DL_CUDA(cudaStreamSynchronize(st));
+        if (hc.err & kErrBounds) throw Error(DL_ERR_QUEUE_OVERFLOW, kBoundsMessage);
         if (hc.err & kErrTensorWait) throw Error(DL_ERR_TIMEOUT, "tensor-core wait timed out in a guided kernel");
         if (hc.err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
         if (hc.ext[0] == 0 && hc.shadow[0] == 0 && hc.next_path >= (unsigned long long)li_n) break;
@@ -2034,6 +2085,7 @@ void trace_wavefront_launch(dl_scene* S, bool any, const float* d_rays, int64_t 
     std::memset(&o, 0, sizeof(o));
     P.r0 = make_request(S, o);
     P.mode = 1;
+    P.capacity = (int)n;
     char* b = static_cast<char*>(work);
     P.cnt = reinterpret_cast<RenderCounters*>(b);
     b += kCounterBytes;
@@ -2054,7 +2106,9 @@ void trace_wavefront_launch(dl_scene* S, bool any, const float* d_rays, int64_t 
     }
     DL_CUDA(cudaMemsetAsync(P.cnt, 0, sizeof(RenderCounters), st));
     const int ni = (int)n;
+    const unsigned long long total = (unsigned long long)n;  // path indices of the shadow targets: 0..n-1
     DL_CUDA(cudaMemcpyAsync(any ? &P.cnt->shadow[0] : &P.cnt->ext[0], &ni, sizeof(int), cudaMemcpyHostToDevice, st));
+    DL_CUDA(cudaMemcpyAsync(&P.cnt->pass_total, &total, sizeof(total), cudaMemcpyHostToDevice, st));
     const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
     const int g = (int)std::min<int64_t>((n + 127) / 128, (int64_t)sms * 16);
     k_wavefront_rays_setup<<<g, 128, 0, st>>>(P, reinterpret_cast<const float4*>(d_rays), ni, any ? 1 : 0);
@@ -2066,7 +2120,83 @@ void trace_wavefront_launch(dl_scene* S, bool any, const float* d_rays, int64_t 
     unsigned int err = 0;
     DL_CUDA(cudaMemcpyAsync(&err, &P.cnt->err, sizeof(err), cudaMemcpyDeviceToHost, st));
     DL_CUDA(cudaStreamSynchronize(st));
+    if (err & kErrBounds) throw Error(DL_ERR_QUEUE_OVERFLOW, kBoundsMessage);
     if (err) throw Error(DL_ERR_QUEUE_OVERFLOW, "traversal stack overflow");
+}
+
+}  // namespace dl
+
+namespace dl {
+
+// ------------------------------------------------------- emitter queries
+// Scene::sampleEmitterDirection without the visibility test, at given
+// points, normals and 2D samples, by the device function the material
+// kernels run (an envmap pick draws its three numbers from a pcg32 seeded
+// with the query index); `light` receives the picked emitter.
+__global__ void __launch_bounds__(128) k_emitter_query(DevRequest R, int n, const float* __restrict__ pts,
+                                                        const float* __restrict__ nrm, const float* __restrict__ smp,
+                                                        float* __restrict__ out, int* __restrict__ light) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float3 p = f3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        const float3 nn = f3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+        const float2 s = make_float2(smp[2 * i], smp[2 * i + 1]);
+        float sx = s.x;
+        light[i] = R.sc.num_lights > 0 ? pick_light(R, sx) : -1;
+        Pcg32 g;
+        g.seed((unsigned long long)i, 7ull);
+        float3 d;
+        float dist, pdf;
+        bool delta;
+        const float3 spec = sample_emitter(R, p, nn, s, g, d, dist, pdf, delta);
+        float* o = out + 8 * (size_t)i;
+        o[0] = d.x;
+        o[1] = d.y;
+        o[2] = d.z;
+        o[3] = dist;
+        o[4] = pdf;
+        o[5] = spec.x;
+        o[6] = spec.y;
+        o[7] = spec.z;
+    }
+}
+
+void emitter_query(dl_scene* S, uint32_t flags, int64_t n, const float* pts, const float* nrm, const float* smp,
+                   float* d, float* dist, float* pdf, float* spec, int32_t* light) {
+    if (n == 0) return;
+    dl_context* ctx = S->ctx;
+    cudaStream_t st = ctx->stream;
+    dl_render_opts o;
+    std::memset(&o, 0, sizeof(o));
+    o.flags = flags;
+    const DevRequest R = make_request(S, o);
+    const size_t f = sizeof(float) * (size_t)n;
+    DevBuf buf;
+    buf.ensure(f * (3 + 3 + 2 + 8 + 1));
+    float* d_pts = buf.as<float>();
+    float* d_nrm = d_pts + 3 * n;
+    float* d_smp = d_nrm + 3 * n;
+    float* d_out = d_smp + 2 * n;
+    int* d_light = reinterpret_cast<int*>(d_out + 8 * n);
+    DL_CUDA(cudaMemcpyAsync(d_pts, pts, 3 * f, cudaMemcpyHostToDevice, st));
+    DL_CUDA(cudaMemcpyAsync(d_nrm, nrm, 3 * f, cudaMemcpyHostToDevice, st));
+    DL_CUDA(cudaMemcpyAsync(d_smp, smp, 2 * f, cudaMemcpyHostToDevice, st));
+    const int sms = ctx->num_sms > 0 ? ctx->num_sms : 152;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 127) / 128, (int64_t)sms * 8));
+    k_emitter_query<<<g, 128, 0, st>>>(R, (int)n, d_pts, d_nrm, d_smp, d_out, d_light);
+    DL_CUDA(cudaGetLastError());
+    std::vector<float> h((size_t)n * 8);
+    DL_CUDA(cudaMemcpyAsync(h.data(), d_out, 8 * f, cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaMemcpyAsync(light, d_light, f, cudaMemcpyDeviceToHost, st));
+    DL_CUDA(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < n; i++) {
+        const float* q = &h[8 * (size_t)i];
+        for (int k = 0; k < 3; k++) {
+            d[3 * i + k] = q[k];
+            spec[3 * i + k] = q[5 + k];
+        }
+        dist[i] = q[3];
+        pdf[i] = q[4];
+    }
 }
 
 }  // namespace dl

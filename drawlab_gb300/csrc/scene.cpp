@@ -524,6 +524,7 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     D.textures = S->textures.as<DevTexture>();
     D.texcoords = S->texcoords.as<float2>();
     D.num_tris = (int)ntri;
+    D.num_nodes = (int)bvh.nodes.size();
     D.num_lights = nl;
     D.cam = make_camera(*cam);
     D.light_pick = S->light_pick.as<float4>();

@@ -26,6 +26,11 @@ void bsdf_query(dl_context* ctx, const dl_material_desc& m, int64_t n, const flo
                 const float* smp, float* eval, float* pdf, float* s_wo, float* s_w, float* s_eta, int32_t* s_measure);
 void env_query(dl_scene* S, int64_t n, const float* xi, const float* nrm, const float* dirs, float* s_dir,
                float* s_pdf, float* s_val, float* pdf, float* val);
+// Scene::sampleEmitterDirection without visibility at given points (render.cu).
+void emitter_query(dl_scene* S, uint32_t flags, int64_t n, const float* pts, const float* nrm, const float* smp,
+                   float* d, float* dist, float* pdf, float* spec, int32_t* light);
+// L2 -> SM read bandwidth (GB/s) of L2-only loads over an L2-resident buffer.
+double measure_l2_read(dl_context* ctx, int64_t bytes, int passes);
 
 int64_t film_floats(int w, int h, int filter);
 void render_run(dl_scene* S, const dl_render_opts& o, float* d_film, int64_t li_n, const int* d_xys, float* d_L,

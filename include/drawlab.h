@@ -376,6 +376,26 @@ int dl_scene_env_query(dl_scene* scene, int64_t n, const float* xi, const float*
                        const float* dirs, float* s_dir, float* s_pdf, float* s_value,
                        float* pdf, float* value);
 
+/* Scene::sampleEmitterDirection (src/tracer/scene/scene.cpp:139-170)
+ * without its visibility test, on the GPU, by the code the material kernels
+ * run: at points pts with shading normals nrm (n x 3 each) and 2D samples
+ * smp (n x 2), the emitter picked uniformly (the reference) or, with
+ * DL_RENDER_POWER_LIGHT_PICK in flags, by the power alias table; outputs the
+ * direction d (n x 3), distance, solid-angle pdf times the pick probability,
+ * the unoccluded spectrum / pdf (n x 3) and the picked emitter index.  An
+ * envmap pick draws its three numbers from a per-query pcg32.  Host
+ * buffers; synchronous. */
+int dl_scene_emitter_sample(dl_scene* scene, uint32_t flags, int64_t n, const float* pts,
+                            const float* nrm, const float* smp, float* d, float* dist, float* pdf,
+                            float* spec, int32_t* light);
+
+/* Measurement aid, no counterpart in the reference: the device's L2 -> SM
+ * read bandwidth in GB/s, from a kernel that streams an L2-resident buffer
+ * of `bytes` (1 MiB .. 4 GiB; 64 MiB fits the GB300's L2) `passes` times
+ * with L2-only loads after one warm-up pass.  The traversal kernels' node
+ * and triangle fetches are bounded by it when the BVH stays in L2. */
+int dl_measure_l2_read_bandwidth(dl_context* ctx, int64_t bytes, int32_t passes, double* gbs);
+
 /* ----------------------------------------------------------------- batches */
 
 /* One request of a batch: a scene of the context, its render options and at

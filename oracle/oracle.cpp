@@ -1704,14 +1704,15 @@ int orc_trace_any(void* p, const float* rays, int64_t n, uint8_t* occ, int32_t t
     return 0;
 }
 
-int orc_render_blocks(void* p, const dl_render_opts* opts, int32_t threads, int32_t max_blocks,
-                      float* rgb_out, float* film_out, double* seconds) {
-    const Scene& sc = *static_cast<Scene*>(p);
+// The block renderer over the listed blocks of the spiral order (all of
+// them when `list` is null), each block with its own pcg32 seeded from the
+// block offset as Independent::prepare does.
+static int render_block_list(const Scene& sc, const dl_render_opts* opts, int32_t threads,
+                             const std::vector<std::pair<int, int>>& blocks, float* rgb_out, float* film_out,
+                             double* seconds) {
     Opts o = opts_of(opts);
     int spp = opts ? opts->spp : 1;
     const int BS = 32;
-    auto blocks = spiral_blocks(sc.cam.w, sc.cam.h, BS);
-    if (max_blocks > 0 && (size_t)max_blocks < blocks.size()) blocks.resize(max_blocks);
     Film film;
     film.reset(0, 0, sc.cam.w, sc.cam.h, sc.filter.border);
     std::mutex mu;
@@ -1745,6 +1746,31 @@ int orc_render_blocks(void* p, const dl_render_opts* opts, int32_t threads, int3
     if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
     film_outputs(film, rgb_out, film_out);
     return 0;
+}
+
+int orc_render_blocks(void* p, const dl_render_opts* opts, int32_t threads, int32_t max_blocks,
+                      float* rgb_out, float* film_out, double* seconds) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    auto blocks = spiral_blocks(sc.cam.w, sc.cam.h, 32);
+    if (max_blocks > 0 && (size_t)max_blocks < blocks.size()) blocks.resize(max_blocks);
+    return render_block_list(sc, opts, threads, blocks, rgb_out, film_out, seconds);
+}
+
+int orc_render_block_subset(void* p, const dl_render_opts* opts, int32_t threads, int32_t n,
+                            const int32_t* spiral_index, float* rgb_out, float* film_out, double* seconds) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    auto all = spiral_blocks(sc.cam.w, sc.cam.h, 32);
+    std::vector<std::pair<int, int>> blocks;
+    for (int32_t i = 0; i < n; i++) {
+        if (spiral_index[i] < 0 || (size_t)spiral_index[i] >= all.size()) return 1;
+        blocks.push_back(all[spiral_index[i]]);
+    }
+    return render_block_list(sc, opts, threads, blocks, rgb_out, film_out, seconds);
+}
+
+int orc_num_blocks(void* p) {
+    const Scene& sc = *static_cast<Scene*>(p);
+    return (int)spiral_blocks(sc.cam.w, sc.cam.h, 32).size();
 }
 
 int orc_li(void* p, const dl_render_opts* opts, int64_t n, const int32_t* xys, float* L,
@@ -1934,6 +1960,17 @@ int orc_hit_data(void* p, int64_t n, const int32_t* prim, const float* bary, flo
         gn[3 * i] = its.geo.n.x; gn[3 * i + 1] = its.geo.n.y; gn[3 * i + 2] = its.geo.n.z;
         st[3 * i] = its.tan.x; st[3 * i + 1] = its.tan.y; st[3 * i + 2] = its.tan.z;
         tuv[2 * i] = its.tuv.x; tuv[2 * i + 1] = its.tuv.y;
+    }
+    return 0;
+}
+
+int orc_pcg32(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t* out, float* out_float) {
+    Pcg32 a, b;
+    a.seed(initstate, initseq);
+    b.seed(initstate, initseq);
+    for (int32_t i = 0; i < n; i++) {
+        out[i] = a.next_u32();
+        out_float[i] = b.next_float();
     }
     return 0;
 }

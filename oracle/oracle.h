@@ -39,6 +39,13 @@ int orc_trace_any(void* scene, const float* rays, int64_t n, uint8_t* occluded,
 int orc_render_blocks(void* scene, const dl_render_opts* opts, int32_t threads,
                       int32_t max_blocks, float* rgb_out, float* film_out, double* seconds);
 
+/* The block renderer over the blocks at the given positions of the spiral
+ * order (each with its own per-block pcg32); orc_num_blocks is the number of
+ * 32x32 blocks of the image.  Returns nonzero for an index out of range. */
+int orc_render_block_subset(void* scene, const dl_render_opts* opts, int32_t threads, int32_t n,
+                            const int32_t* spiral_index, float* rgb_out, float* film_out, double* seconds);
+int orc_num_blocks(void* scene);
+
 /* Per-path streams (the GPU renderer's sampling): every (x, y, s) path seeds
  * its own pcg32.  Film and rgb as dl_render_film / dl_render. */
 int orc_render_paths(void* scene, const dl_render_opts* opts, int32_t threads,
@@ -66,6 +73,10 @@ int orc_emitter_sample(void* scene, const dl_render_opts* opts, int64_t n, const
 /* The envmap's alias table and pdf (src/tracer/emitter/envmap.cpp:59-141),
  * env_width x env_height entries each.  Returns nonzero without an envmap. */
 int orc_env_tables(void* scene, float* q, uint32_t* alias, float* pdf);
+
+/* The oracle's pcg32: n outputs of seed(initstate, initseq) as nextUInt and
+ * as nextFloat (independent.cpp:31-45 with the wjakob/pcg32 interface). */
+int orc_pcg32(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t* out, float* out_float);
 
 /* Envmap::sampleDirection from three numbers xi at shading normals nrm, and
  * pdfDirection / eval of dirs (include/optix/light/envmap.h:25-94).  Returns

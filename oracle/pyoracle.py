@@ -121,6 +121,21 @@ class OracleScene:
                                    _f(fb), C.byref(sec))
         return (rgb, fb, sec.value) if film else (rgb, sec.value)
 
+    def num_blocks(self) -> int:
+        return int(self.lib.orc_num_blocks(self.h))
+
+    def render_block_subset(self, opts, blocks, threads=None, film=False):
+        """The block renderer over the listed blocks (positions in the
+        spiral order); returns (rgb[, film], seconds)."""
+        idx = np.ascontiguousarray(blocks, np.int32)
+        rgb = np.zeros((self.height, self.width, 3), np.float32)
+        fb = np.zeros((self.height + 2 * self.border, self.width + 2 * self.border, 4), np.float32)
+        sec = C.c_double()
+        if self.lib.orc_render_block_subset(self.h, C.byref(opts), _threads(threads), len(idx), _f(idx),
+                                            _f(rgb), _f(fb), C.byref(sec)) != 0:
+            raise ValueError("block index out of range")
+        return (rgb, fb, sec.value) if film else (rgb, sec.value)
+
     def render_paths(self, opts, threads=None, film=False):
         rgb = np.zeros((self.height, self.width, 3), np.float32)
         fb = np.zeros((self.height + 2 * self.border, self.width + 2 * self.border, 4), np.float32)

@@ -462,4 +462,16 @@ int ref_emitter_sample(void* p, int64_t n, const float* pts, const float* nrm, c
     return 0;
 }
 
+// The pcg32 the reference build links (oracle/ref_shim/pcg32.h, standing in
+// for the un-vendored ext/pcg32 submodule): n outputs of seed(initstate,
+// initseq) as nextUInt and as nextFloat.
+int ref_pcg32(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t* out, float* out_float) {
+    pcg32 a(initstate, initseq), b(initstate, initseq);
+    for (int32_t i = 0; i < n; i++) {
+        out[i] = a.nextUInt();
+        out_float[i] = b.nextFloat();
+    }
+    return 0;
+}
+
 }  // extern "C"

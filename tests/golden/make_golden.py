@@ -9,6 +9,8 @@ fixtures are its outputs on seeded inputs:
                       film position (PathIntegrator::Li)
   <scene>_blocks.npz  the block renderer (spiral 32x32 blocks, per-block
                       pcg32, Gaussian film): rgb image, 1 worker thread
+  cornell_hispp.npz   the block renderer on the 64x64 Cornell box at 4096
+                      spp (every core): a low-noise image of the reference
   <scene>_emit.npz    Scene::sampleEmitterDirection at seeded points
   bsdf.npz            BSDF eval/pdf/sample for diffuse, mirror, dielectric,
                       microfacet on seeded directions
@@ -36,7 +38,7 @@ and, from the reference's OptiX-only code compiled as host C++
 
 Run from the repository root:  python tests/golden/make_golden.py
 (``--only cameras`` writes perspective_normals.npz alone, ``--only optix``
-the optix_*.npz files alone).
+the optix_*.npz files alone, ``--only hispp`` cornell_hispp.npz alone).
 """
 from __future__ import annotations
 
@@ -316,6 +318,17 @@ def write_hit_fixture(rx, n=1024):
     print("optix_hit written")
 
 
+HISPP = 4096
+
+
+def write_hispp_fixture():
+    sc = scenes.cornell(width=64, height=64, spp=HISPP, max_depth=0)
+    ref = po.RefScene(sc, spp=HISPP)
+    rgb, sec = ref.render_blocks(threads=os.cpu_count())
+    np.savez_compressed(os.path.join(HERE, "cornell_hispp.npz"), rgb=rgb, spp=np.int32(HISPP))
+    print("cornell_hispp: %.1f s, mean %.5f" % (sec, rgb.mean()))
+
+
 def write_optix_fixtures():
     import pyref_optix as rx
     if rx.lib() is None:
@@ -334,6 +347,9 @@ def main():
         return
     if "--only" in sys.argv and "optix" in sys.argv:
         write_optix_fixtures()
+        return
+    if "--only" in sys.argv and "hispp" in sys.argv:
+        write_hispp_fixture()
         return
     for name, sc in fixture_scenes().items():
         ref = po.RefScene(sc, spp=sc.spp)
@@ -364,6 +380,7 @@ def main():
     print("bsdf fixtures written")
     write_camera_fixtures()
     write_optix_fixtures()
+    write_hispp_fixture()
 
 
 if __name__ == "__main__":

@@ -195,9 +195,9 @@ def test_no_bias_against_oracle_over_seeds(ctx):
 
 def test_image_matches_reference_block_renderer(ctx):
     # reference (golden, its own block renderer, 4 spp, 64x64) vs GPU at
-    # 256 spp: relMSE of the reference's noisy image against the converged GPU
-    # image equals the reference's own noise level (a biased renderer would
-    # add a floor).  Stated bound: relMSE < 0.1.
+    # 256 spp.  A loose check that the low-spp golden still fits; the tight
+    # image test against the reference's 4096-spp render is
+    # test_gpu_configs.py::test_c1_converged_image_matches_reference_renderer.
     sc = mg.fixture_scenes()["cornell"]
     g = np.load(os.path.join(GOLDEN, "cornell_blocks.npz"))
     gs = api.Scene.from_data(ctx, sc)
