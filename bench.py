@@ -9,15 +9,23 @@ One step = one full frame: 1920*1080*64 = 132.7M camera paths.  The scene
              between steps)
   e2e        the same metric through dl_render with a host output buffer
              (film resolve + device-to-host copy of the image inside the call)
-  roofline   closest-hit traversal kernel: algorithmic bytes (node and
+  roofline   closest-hit traversal kernel: algorithmic fetch bytes (node and
              triangle fetches counted by a counting replay of the same frame,
-             plus ray in / hit out) / its summed launch time, against the
-             measured HBM copy bandwidth
+             plus ray in / hit out) / its summed launch time, against the L2
+             read bandwidth measured live by the library's probe (the BVH
+             stays in L2); beside it the L2 -> L1 and DRAM bytes it really
+             moves (per ray, from an ncu capture) against the L2 and HBM
+             peaks
   cpu_baseline  the CPU restatement of the reference renderer (spiral 32x32
-             blocks, per-block pcg32) on a bounded set of blocks of the same
-             frame, all host cores
+             blocks, per-block pcg32) on 64 blocks of the same frame drawn
+             uniformly with a fixed seed, all host cores
+  c4_batch   the batched workload (64 requests, autotuned launch shape)
+  c5_guided  learned guiding vs plain at equal time (relMSE at 480x270
+             against a 64k-spp reference), the guided 1080p rate and the
+             network kernels against the tensor-core peak
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                 [--workload batch|guided] [--no-extras] [--profile-frame --spp S]
 
 Multi-GPU (torchrun, one rank per GPU): replicas render disjoint sample ranges
 (weak scaling), no collective on the data path.
@@ -46,11 +54,17 @@ METRIC = "samples/s (material-sphere scene 1920x1080, 64 spp, depth 16)"
 # algorithmic bytes per closest-hit ray: node = 64 B (both child boxes + refs),
 # triangle = 48 B (3 x float4), ray in 32 B, hit out 16 B
 NODE_BYTES, TRI_BYTES, RAY_IN, HIT_OUT = 64, 48, 32, 16
-# DRAM bytes (read + write) per closest-hit traversal launch of this workload,
-# from one ncu capture of the full-size launch list (dram__bytes_read.sum +
-# dram__bytes_write.sum over the 120 extension launches of that capture /
-# 120); a profile measurement, not a live one.
-TRAVERSE_DRAM_BYTES_PER_LAUNCH = (170.30e9 + 42.23e9) / 120
+# Per-ray cache and DRAM traffic of the traversal kernels, from one ncu
+# capture of every k_traverse launch of a 4-spp frame of this scene
+# (python bench.py --profile-frame --spp 4; profiles/k_traverse_l2_dram_material_spheres_1080p_4spp.md):
+# L2 -> L1 bytes (lts__t_sectors_srcunit_tex_op_read.sum x 32) and DRAM
+# bytes (dram__bytes_read.sum + dram__bytes_write.sum) summed over the
+# frame's launches of each kernel, divided by the frame's extension / shadow
+# rays.  Profile measurements, scaled here by the rays of the timed frames.
+EXT_L2_BYTES_PER_RAY = 158925079 * 32 / 14984872            # 339.4 B
+EXT_DRAM_BYTES_PER_RAY = (2181426688 + 471964416) / 14984872  # 177.1 B
+SH_L2_BYTES_PER_RAY = 63489526 * 32 / 5484823                 # 370.4 B
+SH_DRAM_BYTES_PER_RAY = (954967296 + 120330240) / 5484823     # 196.1 B
 
 
 def peaks():
@@ -183,9 +197,21 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_baseline(scene_data, seconds_target=15.0, max_blocks=None):
-    """Oracle block renderer (reference semantics) on the first blocks of the
-    spiral: samples/s with every host core."""
+# The CPU sample: 64 of the frame's 2040 32x32 blocks drawn uniformly (seed
+# 0) from the spiral order, each at the full 64 spp and depth 16.
+CPU_BLOCKS = 64
+CPU_BLOCK_SEED = 0
+
+
+def cpu_block_subset(n_blocks_total):
+    rng = np.random.default_rng(CPU_BLOCK_SEED)
+    return np.sort(rng.choice(n_blocks_total, size=CPU_BLOCKS, replace=False)).astype(np.int32)
+
+
+def cpu_baseline(scene_data):
+    """Oracle block renderer (reference semantics: per-block pcg32, spiral
+    order, Gaussian film) on the seeded 64-block subset of the frame, every
+    host core: samples/s."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle as po
     from drawlab_gb300 import abi
@@ -193,48 +219,54 @@ def cpu_baseline(scene_data, seconds_target=15.0, max_blocks=None):
     orc = po.OracleScene(scene_data)
     cores = os.cpu_count() or 1
     opts = abi.make_opts(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"])
-    # calibrate on a few blocks, then size the sample to ~seconds_target
-    blocks = max(cores, 4)
-    _, sec = orc.render_blocks(opts, threads=cores, max_blocks=blocks)
-    if max_blocks is None:
-        per_block = sec / blocks * cores
-        max_blocks = int(max(cores, min(400, seconds_target * cores / max(per_block, 1e-6))))
-    _, sec = orc.render_blocks(opts, threads=cores, max_blocks=max_blocks)
-    samples = max_blocks * 32 * 32 * WORKLOAD["spp"]
+    blocks = cpu_block_subset(orc.num_blocks())
+    _, sec = orc.render_block_subset(opts, blocks, threads=cores)
+    samples = len(blocks) * 32 * 32 * WORKLOAD["spp"]
     return {"value": samples / sec, "unit": "samples/s", "cores": cores, "kind": "port",
-            "sample": "%d of the 2040 32x32 blocks (spiral order from the image centre), 64 spp, "
-                      "depth 16, %.1f s" % (max_blocks, sec)}, orc
+            "sample": "%d of the %d 32x32 blocks drawn uniformly (seed %d), 64 spp, depth 16, %.1f s"
+                      % (len(blocks), orc.num_blocks(), CPU_BLOCK_SEED, sec)}, orc
+
+
+REF_BLOCKS_PER_STEP = 8
 
 
 def run_reference(args):
+    """The reference's CPU renderer on the bench's frame: each step renders
+    8 blocks of the seeded 64-block subset (steps cycle through it), all
+    host cores.  The reference sources do not travel to the GPU host, so its
+    CPU restatement (bit-exact with the reference on the golden vectors)
+    runs."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from drawlab_gb300 import scenes
-    sc = scenes.material_spheres()
-    base, orc = cpu_baseline(sc, seconds_target=6.0)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
-    from drawlab_gb300 import abi
+    import pyoracle as po
+    from drawlab_gb300 import abi, scenes
+    sc = scenes.material_spheres()
+    orc = po.OracleScene(sc)
     cores = os.cpu_count() or 1
     opts = abi.make_opts(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"])
-    blocks = max(cores, 16)
-    for _ in range(args.warmup):
-        orc.render_blocks(opts, threads=cores, max_blocks=blocks)
+    subset = cpu_block_subset(orc.num_blocks())
+    chunks = [subset[k:k + REF_BLOCKS_PER_STEP] for k in range(0, len(subset), REF_BLOCKS_PER_STEP)]
+    for w in range(args.warmup):
+        orc.render_block_subset(opts, chunks[w % len(chunks)][:2], threads=cores)
     tot_s = 0.0
-    for _ in range(args.steps):
-        _, s = orc.render_blocks(opts, threads=cores, max_blocks=blocks)
+    for k in range(args.steps):
+        _, s = orc.render_block_subset(opts, chunks[k % len(chunks)], threads=cores)
         tot_s += s
-    samples = blocks * 32 * 32 * WORKLOAD["spp"] * args.steps
+    samples = REF_BLOCKS_PER_STEP * 32 * 32 * WORKLOAD["spp"] * args.steps
     value = samples / tot_s
+    sample = ("%d blocks per step, cycling through %d of the frame's %d 32x32 blocks drawn uniformly (seed %d); "
+              "64 spp, depth 16; the reference sources do not travel to this host, so the CPU restatement "
+              "(bit-exact with the reference on its golden vectors) runs"
+              % (REF_BLOCKS_PER_STEP, len(subset), orc.num_blocks(), CPU_BLOCK_SEED))
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seed 2)",
             "impl": "reference",
-            "config": dict(WORKLOAD, step="%d blocks of 32x32 pixels at 64 spp" % blocks),
+            "config": dict(WORKLOAD, step="%d blocks of 32x32 pixels at 64 spp" % REF_BLOCKS_PER_STEP),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
-                             "sample": "%d blocks per step (spiral order), 64 spp, depth 16; the reference "
-                                       "sources do not travel to this host, so the CPU restatement "
-                                       "(bit-exact with the reference elsewhere) runs" % blocks},
+                             "sample": sample},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -250,7 +282,14 @@ def main():
     ap.add_argument("--workload", default="material_spheres", choices=["material_spheres", "batch", "guided"],
                     help="material_spheres: the headline frame; batch: 64 requests in one wavefront; "
                          "guided: learned proposal vs plain at equal time")
+    ap.add_argument("--guided-res", default="480x270", help="guided workload: resolution of the relMSE comparison")
+    ap.add_argument("--ref-spp", type=int, default=REF_SPP, help="guided workload: spp of the plain reference")
+    ap.add_argument("--no-extras", action="store_true", help="headline line without the c4_batch / c5_guided keys")
+    ap.add_argument("--profile-frame", action="store_true",
+                    help="render one frame of the headline scene at --spp and print its ray counts (for ncu)")
     args = ap.parse_args()
+    if args.profile_frame:
+        return run_profile_frame(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
@@ -350,6 +389,9 @@ def main():
     sh_tri = counts.shadow_triangle_tests / max(1, counts.shadow_rays)
     sh_bytes = sh_node * NODE_BYTES + sh_tri * TRI_BYTES + 48 + 1
     sh_achieved = t_sh_rays * sh_bytes / (sh_ms / 1000.0) / 1e9 if sh_ms > 0 else 0.0
+    l2_peak = ctx.l2_read_gbs(64 << 20, 200)
+    roofline = traversal_roofline(hbm, peak_kind, l2_peak, ext_ms, sh_ms, t_ext_rays, t_sh_rays, ext_launches,
+                                  bytes_per_ray, n_node, n_tri, achieved, sh_bytes, sh_node, sh_tri, sh_achieved)
 
     if rank == 0:
         base = None
@@ -373,30 +415,64 @@ def main():
             "e2e": {"value": e2e_value, "unit": "samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": W * H * 3 * 4,
                     "call": "dl_render (render options by value; image returned to host memory)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "traffic": TRAVERSE_DRAM_BYTES_PER_LAUNCH,
-                         "traffic_note": "ncu DRAM bytes per extension launch (profile capture)",
-                         "algorithmic_bytes_per_launch": bytes_per_ray * t_ext_rays / max(1, ext_launches),
-                         "kernel": "k_traverse<extension> (closest-hit traversal)",
-                         "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": n_node,
-                         "tri_tests_per_ray": n_tri,
-                         "note": "algorithmic node+triangle fetch bytes (64 B node, 48 B triangle, 32 B ray, "
-                                 "16 B hit) per extension ray; the 30 MB BVH is L2-resident, so most fetches "
-                                 "are served by L1/L2, not DRAM",
-                         "shadow": {"achieved": sh_achieved, "frac": sh_achieved / hbm,
-                                    "bytes_per_ray": sh_bytes, "node_visits_per_ray": sh_node,
-                                    "tri_tests_per_ray": sh_tri}},
+            "roofline": roofline,
             "clocks": ck,
             "scene": {"triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
                       "bvh_depth": info.bvh_depth, "bvh_build_s": info.bvh_build_seconds,
                       "sah_cost": info.bvh_sah_cost},
             "cpu_baseline": base,
         }
+        if ws == 1 and not args.no_extras:
+            gs.close()
+            line["c4_batch"] = batch_measure(ctx, steps=2, warmup=1)
+            line["c5_guided"] = guided_measure(ctx, reps=3, warmup=1)
+            line["c5_guided"]["config"]["relmse_resolution_note"] = (
+                "480x270: a 64k-spp plain reference at 1920x1080 is 136 G samples (about 2 minutes of GPU time "
+                "per bench run); the 1080p throughput is measured on the full frame (guided_1080p)")
         print(json.dumps(line))
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def traversal_roofline(hbm, peak_kind, l2_peak, ext_ms, sh_ms, ext_rays, sh_rays, ext_launches, bytes_per_ray,
+                       n_node, n_tri, alg_gbs, sh_bytes, sh_node, sh_tri, sh_alg_gbs):
+    """The closest-hit traversal against the memory level that bounds it.
+    The BVH of this scene (~28 MB) stays in L2, so every node and triangle
+    fetch is served by L1 or L2, not DRAM: achieved = the kernel's
+    algorithmic fetch bytes (counted node visits and triangle tests of the
+    same frame) over its launch time, against the L2 read bandwidth measured
+    live.  Beside it: the L2 -> L1 bytes the kernel really moves and its
+    DRAM bytes (per ray, from the profile), against the same L2 peak and the
+    measured HBM bandwidth."""
+    ext_s, sh_s = ext_ms / 1e3, sh_ms / 1e3
+    l2_gbs = ext_rays * EXT_L2_BYTES_PER_RAY / ext_s / 1e9 if ext_s > 0 else 0.0
+    dram_gbs = ext_rays * EXT_DRAM_BYTES_PER_RAY / ext_s / 1e9 if ext_s > 0 else 0.0
+    r = {"bound": "l2", "kernel": "k_traverse<extension> (closest-hit traversal)", "unit": "GB/s",
+         "achieved": alg_gbs, "peak": l2_peak, "frac": alg_gbs / l2_peak,
+         "peak_kind": "measured live (dl_measure_l2_read_bandwidth: 64 MiB L2-resident buffer, L2-only loads, "
+                      "200 passes)",
+         "achieved_note": "algorithmic bytes per ray (64 B per node visit, 48 B per triangle test, 32 B ray, "
+                          "16 B hit) x rays / summed launch time",
+         "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": n_node, "tri_tests_per_ray": n_tri,
+         "algorithmic_bytes_per_launch": bytes_per_ray * ext_rays / max(1, ext_launches),
+         "traffic": EXT_DRAM_BYTES_PER_RAY * ext_rays / max(1, ext_launches),
+         "traffic_note": "DRAM bytes per launch: the profile's DRAM bytes per ray (177 B) x this frame's rays per "
+                         "launch",
+         "l2_traffic": {"bytes_per_ray": EXT_L2_BYTES_PER_RAY, "achieved": l2_gbs, "frac": l2_gbs / l2_peak,
+                        "l1_served_fraction": 1.0 - EXT_L2_BYTES_PER_RAY / bytes_per_ray,
+                        "note": "L2 -> L1 bytes the kernel moves (lts__t_sectors_srcunit_tex_op_read x 32 per ray)"},
+         "dram": {"bytes_per_ray": EXT_DRAM_BYTES_PER_RAY, "achieved": dram_gbs, "peak": hbm,
+                  "frac": dram_gbs / hbm, "peak_kind": peak_kind}}
+    sh = {"achieved": sh_alg_gbs, "frac": sh_alg_gbs / l2_peak, "bytes_per_ray": sh_bytes,
+          "node_visits_per_ray": sh_node, "tri_tests_per_ray": sh_tri}
+    if sh_s > 0:
+        sh_l2 = sh_rays * SH_L2_BYTES_PER_RAY / sh_s / 1e9
+        sh_dram = sh_rays * SH_DRAM_BYTES_PER_RAY / sh_s / 1e9
+        sh.update({"l2_traffic": {"bytes_per_ray": SH_L2_BYTES_PER_RAY, "achieved": sh_l2, "frac": sh_l2 / l2_peak},
+                   "dram": {"bytes_per_ray": SH_DRAM_BYTES_PER_RAY, "achieved": sh_dram, "frac": sh_dram / hbm}})
+    r["shadow"] = sh
+    return r
 
 
 def _device_setup():
@@ -410,17 +486,13 @@ def _device_setup():
     return local
 
 
-def run_batch(args):
+def batch_measure(ctx, steps, warmup):
     """64 requests (seed 4) of 1k-2M-triangle scenes, 128^2..1080p, 4..256
     spp, half under the 2048x1024 sky, rendered by one dl_render_batch call
     per step (images to host memory).  The launch shape comes from
     dl_autotune on an eighth of the samples, outside the timed region."""
-    local = _device_setup()
-    if local is None:
-        return
     from drawlab_gb300 import abi, api, scenes
     scene_list, reqs = scenes.batch_workload(seed=4)
-    ctx = api.Context(local)
     gscenes = [api.Scene.from_data(ctx, s) for s in scene_list]
     items = [(gscenes[si], abi.make_opts(spp=spp, max_depth=8, seed=17 + k), cam)
              for k, (si, spp, cam) in enumerate(reqs)]
@@ -428,11 +500,11 @@ def run_batch(args):
     t_tune = time.perf_counter()
     tune, trials = ctx.autotune(items, trial_spp=0)
     t_tune = time.perf_counter() - t_tune
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.render_batch(items)
     dev_ms, wall, launches = 0.0, 0.0, 0
-    with ClockSampler(local) as clocks:
-        for _ in range(args.steps):
+    with ClockSampler(ctx_device(ctx)) as clocks:
+        for _ in range(steps):
             t0 = time.perf_counter()
             ctx.render_batch(items)
             wall += time.perf_counter() - t0
@@ -441,11 +513,10 @@ def run_batch(args):
             launches += st.kernel_launches
     ck = clocks.summary()
     tris = [int(sum(m.indices.shape[0] for m in s.meshes)) for s in scene_list]
-    line = {"metric": "samples/s (64 batched requests, seed 4)", "value": samples * args.steps / (dev_ms / 1e3),
-            "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (procedural scenes and sky, seed 4)",
+    for gsc in gscenes:
+        gsc.close()
+    return {"metric": "samples/s (64 batched requests, seed 4)", "value": samples * steps / (dev_ms / 1e3),
+            "unit": "samples/s", "steps": steps, "warmup": warmup, "ms_per_step": dev_ms / steps,
             "config": {"workload": "batch", "requests": len(reqs), "samples_per_step": samples,
                        "scene_triangles": tris, "resolutions": "128^2..1920x1080", "spp": "4..256",
                        "max_depth": 8, "l2_flush": "inputs larger than L2 (BVHs 2.6 GB, samples 4 GB)"},
@@ -453,31 +524,45 @@ def run_batch(args):
             "autotune": {"paths_in_flight": tune.paths_in_flight, "traverse_ctas_per_sm": tune.traverse_ctas_per_sm,
                          "shade_ctas_per_sm": tune.shade_ctas_per_sm, "shade_threads": tune.shade_threads,
                          "iterations_per_graph": tune.iterations_per_graph, "trials": trials, "seconds": t_tune},
-            "e2e": {"value": samples * args.steps / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
+            "e2e": {"value": samples * steps / wall, "unit": "samples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": sum(c.width * c.height * 12 for _, _, c in reqs),
                     "call": "dl_render_batch (64 requests; images returned to host memory)"},
             "clocks": ck}
+
+
+def ctx_device(ctx):
+    import torch
+    return torch.cuda.current_device()
+
+
+def run_batch(args):
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import api
+    ctx = api.Context(local)
+    r = batch_measure(ctx, args.steps, args.warmup)
+    line = dict(r, n_gpus=1, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+                data="synthetic (procedural scenes and sky, seed 4)")
     print(json.dumps(line))
 
 
 REF_SPP = 65536  # plain reference of the equal-time comparison
 
 
-def run_guided(args):
+def guided_measure(ctx, reps, warmup, width=480, height=270, ref_spp=REF_SPP, spp_g=256, big=True):
     """Learned guiding at equal time on the window-lit room (2M triangles,
-    depth 12): relMSE of guided vs plain against a 64k-spp plain reference at
-    480x270; throughput of the guided render at 1920x1080; the network
-    kernels against the tensor-core peak."""
-    local = _device_setup()
-    if local is None:
-        return
+    depth 12): relMSE of guided vs plain against a ref_spp plain reference
+    at width x height (median over `reps` runs); throughput of the guided
+    render at 1920x1080 (big=True); the network kernels against the
+    tensor-core peak."""
     from drawlab_gb300 import abi, api, metrics, scenes
-    ctx = api.Context(local)
-    small = api.Scene.from_data(ctx, scenes.guiding_room(width=480, height=270))
-    ref = small.render(abi.make_opts(spp=REF_SPP, max_depth=12, seed=1000))
-    spp_g = 256
+    small = api.Scene.from_data(ctx, scenes.guiding_room(width=width, height=height))
+    t0 = time.perf_counter()
+    ref = small.render(abi.make_opts(spp=ref_spp, max_depth=12, seed=1000))
+    ref_s = time.perf_counter() - t0
     results = []
-    for rep in range(max(1, args.steps)):
+    for rep in range(max(1, reps)):
         g = api.Guide(ctx, seed=40 + rep)
         img_g = small.render_guided(abi.make_opts(spp=spp_g, max_depth=12, seed=50 + rep), g)
         st = ctx.stats()
@@ -489,43 +574,74 @@ def run_guided(args):
         t_p = ctx.stats().render_ms
         results.append((metrics.relmse(img_g, ref), metrics.relmse(img_p, ref), t_g, t_p, spp_p, train_ms,
                         metrics.relmse_robust(img_g, ref), metrics.relmse_robust(img_p, ref)))
+    small.close()
     e_g = float(np.median([r[0] for r in results]))
     e_p = float(np.median([r[1] for r in results]))
     r_g = float(np.median([r[6] for r in results]))
     r_p = float(np.median([r[7] for r in results]))
-    big = api.Scene.from_data(ctx, scenes.guiding_room())
-    g = api.Guide(ctx, seed=99)
-    for _ in range(args.warmup):
-        big.render_guided(abi.make_opts(spp=4, max_depth=12, seed=5), g)
-    with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        big.render_guided(abi.make_opts(spp=16, max_depth=12, seed=6), g)
-        wall = time.perf_counter() - t0
-        st = ctx.stats()
-    ck = clocks.summary()
-    samples = 1920 * 1080 * 16
-    net = network_roofline(ctx, api)
-    line = {"metric": "relMSE ratio plain/guided at equal time (window-lit room, 2M triangles)",
-            "value": e_p / e_g, "unit": "x (median over runs)", "n_gpus": 1, "steps": len(results), "warmup": args.warmup,
-            "ms_per_step": float(np.mean([r[2] for r in results])), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network fp16 in, fp32 accumulate)",
-            "data": "synthetic (procedural room and sky)",
-            "config": {"workload": "guided", "triangles": 1960090, "relmse_resolution": "480x270",
-                       "reference": "plain, %d spp" % REF_SPP, "guided_spp": spp_g, "max_depth": 12,
-                       "l2_flush": "inputs larger than L2 (BVH + samples)"},
-            "relmse": {"guided": e_g, "plain": e_p, "runs": [
-                {"guided": r[0], "plain": r[1], "guided_ms": r[2], "plain_ms": r[3], "plain_spp": r[4],
-                 "train_ms": r[5], "robust_guided": r[6], "robust_plain": r[7]} for r in results]},
-            "relmse_robust": {"guided": r_g, "plain": r_p, "ratio": r_p / r_g,
-                              "note": "relMSE without the 0.1 % largest per-pixel errors (sun-edge fireflies)"},
-            "guided_1080p": {"samples_per_s": samples / (st.render_ms / 1e3), "ms": st.render_ms,
-                             "records": st.guide_records, "train_ms": st.guide_train_ms},
-            "network": net,
-            "gpu_launches": st.kernel_launches,
-            "e2e": {"value": samples / wall, "unit": "samples/s (guided 1080p, 16 spp)", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 1920 * 1080 * 12, "call": "dl_render_guided"},
-            "clocks": ck}
+    out = {"metric": "relMSE ratio plain/guided at equal time (window-lit room, 2M triangles)",
+           "value": e_p / e_g, "unit": "x (median over runs)", "steps": len(results),
+           "ms_per_step": float(np.mean([r[2] for r in results])),
+           "config": {"workload": "guided", "triangles": 1960090, "relmse_resolution": "%dx%d" % (width, height),
+                      "reference": "plain, %d spp (%.1f s)" % (ref_spp, ref_s), "guided_spp": spp_g,
+                      "max_depth": 12, "l2_flush": "inputs larger than L2 (BVH + samples)"},
+           "relmse": {"guided": e_g, "plain": e_p, "runs": [
+               {"guided": r[0], "plain": r[1], "guided_ms": r[2], "plain_ms": r[3], "plain_spp": r[4],
+                "train_ms": r[5], "robust_guided": r[6], "robust_plain": r[7]} for r in results]},
+           "relmse_robust": {"guided": r_g, "plain": r_p, "ratio": r_p / r_g,
+                             "note": "relMSE without the 0.1 % largest per-pixel errors (sun-edge fireflies)"}}
+    if big:
+        bigs = api.Scene.from_data(ctx, scenes.guiding_room())
+        g = api.Guide(ctx, seed=99)
+        for _ in range(warmup):
+            bigs.render_guided(abi.make_opts(spp=4, max_depth=12, seed=5), g)
+        with ClockSampler(ctx_device(ctx)) as clocks:
+            t0 = time.perf_counter()
+            bigs.render_guided(abi.make_opts(spp=16, max_depth=12, seed=6), g)
+            wall = time.perf_counter() - t0
+            st = ctx.stats()
+        bigs.close()
+        samples = 1920 * 1080 * 16
+        out["guided_1080p"] = {"samples_per_s": samples / (st.render_ms / 1e3), "ms": st.render_ms,
+                               "records": st.guide_records, "train_ms": st.guide_train_ms}
+        out["gpu_launches"] = st.kernel_launches
+        out["e2e"] = {"value": samples / wall, "unit": "samples/s (guided 1080p, 16 spp)", "h2d_bytes_per_step": 0,
+                      "d2h_bytes_per_step": 1920 * 1080 * 12, "call": "dl_render_guided"}
+        out["clocks"] = clocks.summary()
+    out["network"] = network_roofline(ctx, api)
+    return out
+
+
+def run_guided(args):
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import api
+    ctx = api.Context(local)
+    w, h = (int(v) for v in args.guided_res.split("x"))
+    r = guided_measure(ctx, max(1, args.steps), args.warmup, w, h, args.ref_spp)
+    line = dict(r, n_gpus=1, warmup=args.warmup, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="f32 (network fp16 in, fp32 accumulate)", data="synthetic (procedural room and sky)")
     print(json.dumps(line))
+
+
+def run_profile_frame(args):
+    """One frame of the headline scene at --spp samples per pixel and nothing
+    else (no warm-up, no extra frames): the command under ncu for the
+    traversal kernels' cache and DRAM counters.  Prints the frame's ray
+    counts, which turn the counters into per-ray figures."""
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import abi, api, scenes
+    sc = scenes.material_spheres()
+    ctx = api.Context(local)
+    gs = api.Scene.from_data(ctx, sc)
+    gs.render(abi.make_opts(spp=args.spp, max_depth=WORKLOAD["max_depth"], seed=0))
+    st = ctx.stats()
+    print(json.dumps({"profile_frame": {"spp": args.spp, "camera_rays": st.camera_rays,
+                                        "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
+                                        "iterations": st.iterations, "render_ms": st.render_ms}}))
 
 
 if __name__ == "__main__":
