@@ -25,7 +25,7 @@ One step = one full frame: 1920*1080*64 = 132.7M camera paths.  The scene
              network kernels against the tensor-core peak
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                 [--workload batch|guided] [--no-extras] [--profile-frame --spp S]
+                 [--workload batch|guided|network] [--no-extras] [--profile-frame --spp S]
 
 Multi-GPU (torchrun, one rank per GPU): replicas render disjoint sample ranges
 (weak scaling), no collective on the data path.
@@ -92,10 +92,11 @@ NET_MAC_FWD = 144 * 64 + 64 * 64 + 64 * 48
 NET_MAC_TRAIN = NET_MAC_FWD + (48 * 64 + 64 * 64) + NET_MAC_FWD
 
 
-def network_roofline(ctx, api):
+def network_roofline(ctx, api, train_rows=(32768, 131072)):
     """Device time of the network kernels alone (dl_guide_forward on 4M rows;
-    dl_guide_gradient on one 32768-record training batch), as FLOP/s against
-    the measured tensor peak and as bytes/s against HBM."""
+    dl_guide_gradient on training batches of train_rows records, the first
+    the renderer's default batch), as FLOP/s against the measured tensor
+    peak and as bytes/s against HBM."""
     tpk, tkind = tensor_peak()
     hbm, hkind = peaks()
     rng = np.random.default_rng(3)
@@ -108,28 +109,40 @@ def network_roofline(ctx, api):
         g.forward(inp)
         times.append(ctx.stats().guide_ms)
     t_inf = float(np.median(times[1:]))
-    nb = 32768
-    rec = np.zeros((nb, 12), np.float32)
-    rec[:, :6] = inp[:nb]
-    w = rng.normal(size=(nb, 3))
-    rec[:, 6:9] = w / np.linalg.norm(w, axis=1, keepdims=True)
-    rec[:, 9] = rng.uniform(0.05, 2.0, nb)
-    rec[:, 10] = rng.uniform(0.0, 3.0, nb)
-    times = []
-    for _ in range(6):
-        g.gradient(rec)
-        times.append(ctx.stats().guide_ms)
-    t_tr = float(np.median(times[1:]))
+    train = []
+    for nb in train_rows:
+        rec = np.zeros((nb, 12), np.float32)
+        rec[:, :6] = inp[:nb]
+        w = rng.normal(size=(nb, 3))
+        rec[:, 6:9] = w / np.linalg.norm(w, axis=1, keepdims=True)
+        rec[:, 9] = rng.uniform(0.05, 2.0, nb)
+        rec[:, 10] = rng.uniform(0.0, 3.0, nb)
+        times = []
+        for _ in range(6):
+            g.gradient(rec)
+            times.append(ctx.stats().guide_ms)
+        t_tr = float(np.median(times[1:]))
+        tr_tf = 2.0 * NET_MAC_TRAIN * nb / (t_tr * 1e-3) / 1e12
+        train.append({"kernels": "k_guide_weight_sum + k_guide_fwdbwd + k_guide_wgrad + k_guide_grad_reduce "
+                                 "(tcgen05)", "rows": nb, "ms": t_tr, "tflops": tr_tf, "frac_tensor": tr_tf / tpk,
+                      "flop_per_row": 2 * NET_MAC_TRAIN})
     inf_tf = 2.0 * NET_MAC_FWD * n / (t_inf * 1e-3) / 1e12
-    tr_tf = 2.0 * NET_MAC_TRAIN * nb / (t_tr * 1e-3) / 1e12
     inf_gbs = (24 + 160) * n / (t_inf * 1e-3) / 1e9
     return {"inference": {"kernel": "k_guide_infer (tcgen05)", "rows": n, "ms": t_inf, "tflops": inf_tf,
                           "frac_tensor": inf_tf / tpk, "gbs": inf_gbs, "frac_hbm": inf_gbs / hbm,
                           "bytes_per_row": 184, "flop_per_row": 2 * NET_MAC_FWD},
-            "training_batch": {"kernels": "k_guide_weight_sum + k_guide_train_tc (tcgen05)", "rows": nb,
-                               "ms": t_tr, "tflops": tr_tf, "frac_tensor": tr_tf / tpk,
-                               "flop_per_row": 2 * NET_MAC_TRAIN},
+            "training_batch": train[0], "training_batches": train,
             "peak_tflops": tpk, "peak_kind": tkind, "hbm_peak": hbm, "hbm_kind": hkind}
+
+
+def run_network(args):
+    """The network kernels alone (the command under ncu for their launch list)."""
+    local = _device_setup()
+    if local is None:
+        return
+    from drawlab_gb300 import api
+    ctx = api.Context(local)
+    print(json.dumps({"network": network_roofline(ctx, api)}))
 
 
 class ClockSampler:
@@ -279,9 +292,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--spp", type=int, default=WORKLOAD["spp"])
-    ap.add_argument("--workload", default="material_spheres", choices=["material_spheres", "batch", "guided"],
+    ap.add_argument("--workload", default="material_spheres",
+                    choices=["material_spheres", "batch", "guided", "network"],
                     help="material_spheres: the headline frame; batch: 64 requests in one wavefront; "
-                         "guided: learned proposal vs plain at equal time")
+                         "guided: learned proposal vs plain at equal time; network: the guiding network's "
+                         "kernels alone")
     ap.add_argument("--guided-res", default="480x270", help="guided workload: resolution of the relMSE comparison")
     ap.add_argument("--ref-spp", type=int, default=REF_SPP, help="guided workload: spp of the plain reference")
     ap.add_argument("--no-extras", action="store_true", help="headline line without the c4_batch / c5_guided keys")
@@ -296,6 +311,8 @@ def main():
         return run_batch(args)
     if args.workload == "guided":
         return run_guided(args)
+    if args.workload == "network":
+        return run_network(args)
 
     ws, rank, local = dist_env()
     import torch

@@ -757,6 +757,7 @@ int dl_guide_gradient(dl_guide* G, int64_t n, const float* records, float* grad,
         DL_CUDA(cudaMemcpyAsync(G->recs.ptr, records, (size_t)n * 48, cudaMemcpyHostToDevice, ctx->stream));
         DL_CUDA(cudaMemsetAsync(G->grad.ptr, 0, dl::kGuideParams * 4, ctx->stream));
         guide_err_reset(G, ctx->stream);
+        dl::guide_reserve(G, n);
         DL_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
         dl::guide_gradient(G, G->recs.ptr, n, 1, ctx->stream);
         DL_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -7,8 +7,11 @@
 // (an estimate of the KL divergence from the normalised incident radiance to
 // the mixture q, up to a constant), then one Adam update.  Kernels:
 //   k_guide_weight_sum   mean(L / p) over the batch
-//   k_guide_train_tc     forward, loss gradient, backward and the weight and
-//                        bias gradients of the whole batch (tcgen05.mma)
+//   k_guide_fwdbwd       forward, loss gradient and backward per 128-record
+//                        tile (tcgen05.mma), activations staged in global memory
+//   k_guide_wgrad        the weight and bias gradients of the whole batch as
+//                        one split-K tensor-core product over the staged tiles
+//   k_guide_grad_reduce  the blocks' partial gradients summed
 //   k_guide_adam         Adam on the fp32 master weights; refreshes the fp16
 //                        copy and the tensor cores' weight image
 // Inference (k_guide_infer, and the guided material kernels in render.cu)
@@ -116,55 +119,56 @@ __device__ __forceinline__ float record_grad(const float* o, const GuideRecord& 
     return -scale * logf(q);
 }
 
-// One training batch on the tensor cores (k_guide_train_tc).  A persistent
-// 128-thread block walks 128-record tiles; per tile, each thread owns one
-// record and every product is a tcgen05.mma issued by thread 0 with the
-// accumulator in tensor memory:
-//   forward   x -> h1 -> h2 -> outputs (3 products, as in inference)
-//   loss      dLoss/dOutput of the thread's record: d0 (fp16)
-//   backward  d2 = (d0 W3) * [h2 > 0],  d1 = (d2 W2) * [h1 > 0]
-//             (B operands W3^T, W2^T from the weight image)
-//   weights   [dW1 | . | g_b1 ; . | dW2 | g_b2] += [d1 | d2]^T [x | h1 | 1]
-//             [g_b3 | dW3] += d0^T [1 | h2]
-// The two weight-gradient products read the activation tiles written for
-// the forward and backward products as MN-major operands (M or N = the
-// features, K = the tile's 128 records) and accumulate over all of the
-// block's tiles in tensor memory; bias gradients come from the columns of
-// ones.  At the end each warp reads its 32 accumulator lanes and adds them
-// to the gradient in global memory.
+// One training batch on the tensor cores, in three kernels:
+//
+//   k_guide_fwdbwd   per 128-record tile (one per block, two blocks per SM,
+//                    so two tiles' chains of dependent products overlap):
+//                    forward x -> h1 -> h2 -> outputs (3 products), the loss
+//                    and dLoss/dOutput of each thread's record (d0, fp16),
+//                    backward d2 = (d0 W3) * [h2 > 0] and d1 = (d2 W2) *
+//                    [h1 > 0] (B operands W3^T, W2^T from the weight image).
+//                    Every product is a tcgen05.mma issued by thread 0, the
+//                    accumulator in tensor memory.  The activations the
+//                    weight gradients need are written to global staging in
+//                    the tensor cores' canonical layout, one 128-record tile
+//                    after another: Z = [x | h1 | 1 | h2] (288 halves per
+//                    record) and D = [d0 | d1 | d2] (176 halves).
+//   k_guide_wgrad    the weight and bias gradients as one split-K product
+//                    over the records: [dW1 | . | g_b1 ; . | dW2 | g_b2] =
+//                    [d1 | d2]^T [x | h1 | 1] and [g_b3 | dW3] = d0^T [1 | h2],
+//                    Z and D read as MN-major operands (M or N = features, K =
+//                    records).  Each block streams its range of 64-record
+//                    slices through a three-stage pipeline (bulk copies into
+//                    shared memory, completion on mbarriers; the products of
+//                    one slice run while the next slices load) and writes its
+//                    partial sums from tensor memory to global memory, in the
+//                    parameter layout.
+//   k_guide_grad_reduce  sums the blocks' partials into the gradient (no
+//                    atomics), applying the loss's 1/n.
 //
 // Loss scaling: the fp16 activation gradients leave out the loss's 1/n
 // (with n ~ 3e4 records most of them would be fp16 subnormals); they
-// saturate at the fp16 range, and the 1/n is applied, in fp32, when the
-// accumulators are added to the gradient.
-//
-// Shared memory: the weight image (47,808 B), Z = [x | h1 | 1 | h2] (288
-// halves per record) and D = [d0 | d1 | d2] (176 halves per record), both in
-// the canonical layout.  166 KB per block: one block per SM, and no other
-// tensor-core kernel of this library (70 KB each) fits beside it, so its 512
-// tensor-memory columns are always free.
+// saturate at the fp16 range, and the 1/n is applied, in fp32, in the
+// reduction.
 constexpr int kZK = 288, kDK = 176;                    // halves per record in Z and D
 constexpr int kZx = 0, kZh1 = 144, kZones = 208, kZh2 = 224;
 constexpr int kDd0 = 0, kDd1 = 48, kDd2 = 112;
-constexpr int kTrainCols = 512;
-constexpr int kAccW12 = 64, kAccW3 = kAccW12 + 224;   // accumulator columns ([0, 64): layer products)
+constexpr int kFbCols = 64;                            // tensor-memory columns of a forward/backward block
 constexpr float kHalfMax = 65504.f;
 
-struct GuideTrainSmem {
+struct GuideFbSmem {
     __half w[kGImgHalves];
     float bias[kGImgBiases];
     __half w2t[kGHid * kGHid];
     __half w3t[kGHid * kGOutPad];
-    alignas(128) __half z[kTcRows * kZK];
-    alignas(128) __half d[kTcRows * kDK];
-    uint64_t bar_w, bar_mma, bar_g;
+    alignas(128) __half p[kTcRows * kGEnc];   // x (K = 144), then h2 (K = 64), then d2 (K = 64)
+    alignas(128) __half q[kTcRows * kGHid];   // h1 (K = 64), then d0 (K = 48)
+    uint64_t bar_w, bar_mma;
     uint32_t tmem;
     int fail;
 };
-static_assert(offsetof(GuideTrainSmem, w2t) == kGImgW2T && offsetof(GuideTrainSmem, w3t) == kGImgW3T,
-              "image layout");
-static_assert(sizeof(GuideTrainSmem) > 116 * 1024 + 1024, "one training block per SM");
-static_assert(sizeof(GuideTrainSmem) + sizeof(GuideTcSmem) > 228 * 1024, "no inference block beside it");
+static_assert(offsetof(GuideFbSmem, w2t) == kGImgW2T && offsetof(GuideFbSmem, w3t) == kGImgW3T, "image layout");
+static_assert(2 * (sizeof(GuideFbSmem) + 1024) <= 228 * 1024, "two forward/backward blocks per SM");
 
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
     __half2 h = __floats2half2_rn(a, b);
@@ -174,9 +178,20 @@ __device__ __forceinline__ uint32_t pack_h2_sat(float a, float b) {
     return pack_h2(fminf(fmaxf(a, -kHalfMax), kHalfMax), fminf(fmaxf(b, -kHalfMax), kHalfMax));
 }
 
-// Bias + ReLU of 64 accumulator columns into Z at feature f0 (fp16);
-// returns the mask of the outputs that are > 0 after rounding.
-__device__ __forceinline__ uint64_t train_hidden_epilogue(GuideTrainSmem& S, uint32_t t, const float* bias, int f0) {
+// One 16-byte chunk (features fs..fs+7 of row r in a shared operand with
+// rows of K halves, none when smem is null; features fg..fg+7 of row r in
+// the global staging tile with rows of G halves).
+__device__ __forceinline__ void put_chunk(__half* smem, int K, __half* glob, int G, int r, int fs, int fg,
+                                          uint4 v) {
+    if (smem) *reinterpret_cast<uint4*>(smem + canon_index(r, fs, K)) = v;
+    *reinterpret_cast<uint4*>(glob + canon_index(r, fg, G)) = v;
+}
+
+// Bias + ReLU of 64 accumulator columns: into shared memory (K = 64 rows,
+// feature 0) and the Z staging tile at feature zf; returns the mask of the
+// outputs that are > 0 after rounding.
+__device__ __forceinline__ uint64_t fb_hidden_epilogue(uint32_t t, const float* bias, __half* smem, __half* zt,
+                                                       int zf) {
     const int r = threadIdx.x;
     uint64_t mask = 0;
 #pragma unroll
@@ -192,14 +207,15 @@ __device__ __forceinline__ uint64_t train_hidden_epilogue(GuideTrainSmem& S, uin
             if (__high2float(h) > 0.f) mask |= 1ull << (c0 + 2 * j + 1);
             p[j] = *reinterpret_cast<const uint32_t*>(&h);
         }
-        *reinterpret_cast<uint4*>(S.z + canon_index(r, f0 + c0, kZK)) = make_uint4(p[0], p[1], p[2], p[3]);
-        *reinterpret_cast<uint4*>(S.z + canon_index(r, f0 + c0 + 8, kZK)) = make_uint4(p[4], p[5], p[6], p[7]);
+        put_chunk(smem, kGHid, zt, kZK, r, c0, zf + c0, make_uint4(p[0], p[1], p[2], p[3]));
+        put_chunk(smem, kGHid, zt, kZK, r, c0 + 8, zf + c0 + 8, make_uint4(p[4], p[5], p[6], p[7]));
     }
     return mask;
 }
 
-// 64 accumulator columns masked by `mask` into D at feature f0 (fp16).
-__device__ __forceinline__ void train_backward_epilogue(GuideTrainSmem& S, uint32_t t, uint64_t mask, int f0) {
+// 64 accumulator columns masked by `mask`: into shared memory (K = 64,
+// feature 0; none when smem is null) and the D staging tile at feature df.
+__device__ __forceinline__ void fb_backward_epilogue(uint32_t t, uint64_t mask, __half* smem, __half* dt, int df) {
     const int r = threadIdx.x;
 #pragma unroll
     for (int c0 = 0; c0 < kGHid; c0 += 16) {
@@ -212,113 +228,120 @@ __device__ __forceinline__ void train_backward_epilogue(GuideTrainSmem& S, uint3
             const float b = (mask >> (c0 + 2 * j + 1)) & 1ull ? v[2 * j + 1] : 0.f;
             p[j] = pack_h2_sat(a, b);
         }
-        *reinterpret_cast<uint4*>(S.d + canon_index(r, f0 + c0, kDK)) = make_uint4(p[0], p[1], p[2], p[3]);
-        *reinterpret_cast<uint4*>(S.d + canon_index(r, f0 + c0 + 8, kDK)) = make_uint4(p[4], p[5], p[6], p[7]);
+        put_chunk(smem, kGHid, dt, kDK, r, c0, df + c0, make_uint4(p[0], p[1], p[2], p[3]));
+        put_chunk(smem, kGHid, dt, kDK, r, c0 + 8, df + c0 + 8, make_uint4(p[4], p[5], p[6], p[7]));
     }
 }
 
-// K-major product of one layer: acc (128 x N) = A (Z or D at feature f0,
-// rows of `a_rowlen` halves) x W^T, W [N][K] at `w` (rows of K halves).
+// K-major product of one layer: acc (128 x N) = A (rows of K halves at
+// a_base) x W^T, W [N][K] at `w` (rows of K halves); completion on `bar`.
 template <int K, int N>
-__device__ __forceinline__ void train_issue(uint32_t acc, uint32_t a_base, int a_rowlen, int f0, uint32_t w) {
+__device__ __forceinline__ void fb_issue(uint32_t acc, uint32_t a_base, uint32_t w, uint64_t* bar) {
     constexpr uint32_t idesc = tc::idesc_f16_f32(kTcRows, N);
     tc::fence_after_sync();
 #pragma unroll
     for (int ks = 0; ks < K / 16; ks++)
-        tc::mma_f16(acc, tc::smem_desc(a_base + (f0 / 8 + 2 * ks) * 128, 128, a_rowlen * 16),
-                    tc::smem_desc(w + ks * 256, 128, K * 16), idesc, ks > 0 ? 1u : 0u);
+        tc::mma_f16(acc, tc::smem_desc(a_base + ks * 256, 128, K * 16), tc::smem_desc(w + ks * 256, 128, K * 16),
+                    idesc, ks > 0 ? 1u : 0u);
+    tc::commit(bar);
 }
 
-__global__ void __launch_bounds__(kTcRows) k_guide_train_tc(const void* image, const GuideRecord* s, int n,
-                                                             int stride, const float* wsum, float* grad,
-                                                             float* loss, unsigned* err) {
+__global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, const GuideRecord* s, int n, int stride,
+                                                           const float* wsum, __half* zg, __half* dg, float* loss,
+                                                           unsigned* err) {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
-    GuideTrainSmem& S = *reinterpret_cast<GuideTrainSmem*>(dyn_smem);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    GuideFbSmem& S = *reinterpret_cast<GuideFbSmem*>(dyn_smem);
+    const int tid = threadIdx.x;
     const int ntiles = (n + kTcRows - 1) / kTcRows;
     if ((int)blockIdx.x >= ntiles) return;
     if (tid == 0) {
         tc::mbar_init(&S.bar_w, 1);
         tc::mbar_init(&S.bar_mma, 1);
-        tc::mbar_init(&S.bar_g, 1);
         S.fail = 0;
     }
-    if (tid < 32) tc::tmem_alloc(&S.tmem, kTrainCols);
-    {   // the columns of ones (features 208..223 of every record)
-        const uint32_t one2 = pack_h2(1.f, 1.f);
-        *reinterpret_cast<uint4*>(S.z + canon_index(tid, kZones, kZK)) = make_uint4(one2, one2, one2, one2);
-        *reinterpret_cast<uint4*>(S.z + canon_index(tid, kZones + 8, kZK)) = make_uint4(one2, one2, one2, one2);
-    }
+    if (tid < 32) tc::tmem_alloc(&S.tmem, kFbCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    // the weight copy lands while the first records load and encode; every
+    // thread waits for it before the first product
     if (tid == 0) tc::bulk_load(S.w, image, kGImgTrainBytes, &S.bar_w);
-    bool failed = !tc::mbar_wait(&S.bar_w, 0, kTcWaitNs);
-    if (failed) {
-        S.fail = 1;
-        atomicOr(err, kErrTensorWait);
-    }
-    uint32_t ph = 0, phg = 0;
-    auto wait = [&](uint64_t* bar, uint32_t& parity) {
-        if (!tc::mbar_wait(bar, parity, kTcWaitNs)) {
+    bool failed = false, weights = false;
+    uint32_t ph = 0;
+    auto wait = [&]() {
+        if (!tc::mbar_wait(&S.bar_mma, ph, kTcWaitNs)) {
             failed = true;
             S.fail = 1;
             atomicOr(err, kErrTensorWait);
         } else {
-            parity ^= 1u;
+            ph ^= 1u;
         }
         tc::fence_after_sync();
     };
+    // all threads done with the step's shared and tensor memory: returns
+    // true (in every thread) when a wait has failed
+    auto step_sync = [&]() {
+        tc::fence_smem_to_async();
+        tc::fence_before_sync();
+        return __syncthreads_or(failed) != 0;
+    };
     const uint32_t T = S.tmem;
     const uint32_t tl = T + ((uint32_t)(tid & ~31) << 16);  // this warp's lanes, column 0
-    const uint32_t za = tc::smem_addr(S.z), da = tc::smem_addr(S.d), wa = tc::smem_addr(S.w);
+    const uint32_t pa = tc::smem_addr(S.p), qa = tc::smem_addr(S.q), wa = tc::smem_addr(S.w);
     const float mean = *wsum / (float)n;
-    const float inv_n = 1.f / (float)n;
     float lacc = 0.f;
-    bool pending = false, first = true;
+    const uint32_t one2 = pack_h2(1.f, 1.f);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int r = tile * kTcRows + tid;
+        __half* zt = zg + (size_t)tile * kTcRows * kZK;
+        __half* dt = dg + (size_t)tile * kTcRows * kDK;
         GuideRecord rec = {};
         float sc = 0.f;  // the record's loss weight times n
         if (r < n) {
             rec = s[(size_t)r * stride];
             if (rec.pdf > 0.f && mean > 0.f) sc = fminf(rec.L / rec.pdf / mean, kGTargetClamp);
         }
-        // the previous tile's weight-gradient products read Z and D
-        if (pending) wait(&S.bar_g, phg);
-        pending = false;
-        encode_row_tc(rec.in, S.z, tid, kZK);
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        // forward
-        if (tid == 0) {
-            train_issue<kGEnc, kGHid>(T, za, kZK, kZx, wa + 2 * kGImgW1);
-            tc::commit(&S.bar_mma);
+        // x: the encoding, into P (K = 144) and Z; the columns of ones into Z
+#pragma unroll 1
+        for (int i = 0; i < kGIn; i++) {
+            __half2 h[kGFreq];
+            encode_scalar_h2(rec.in[i], h);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                uint4 v;
+                v.x = *reinterpret_cast<const uint32_t*>(&h[4 * c]);
+                v.y = *reinterpret_cast<const uint32_t*>(&h[4 * c + 1]);
+                v.z = *reinterpret_cast<const uint32_t*>(&h[4 * c + 2]);
+                v.w = *reinterpret_cast<const uint32_t*>(&h[4 * c + 3]);
+                const int f = i * 2 * kGFreq + 8 * c;
+                put_chunk(S.p, kGEnc, zt, kZK, tid, f, kZx + f, v);
+            }
         }
-        wait(&S.bar_mma, ph);
-        const uint64_t m1 = train_hidden_epilogue(S, tl, S.bias + kGImgB1, kZh1);
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        if (tid == 0) {
-            train_issue<kGHid, kGHid>(T, za, kZK, kZh1, wa + 2 * kGImgW2);
-            tc::commit(&S.bar_mma);
+        put_chunk(nullptr, 0, zt, kZK, tid, 0, kZones, make_uint4(one2, one2, one2, one2));
+        put_chunk(nullptr, 0, zt, kZK, tid, 0, kZones + 8, make_uint4(one2, one2, one2, one2));
+        if (!weights) {
+            weights = true;
+            if (!tc::mbar_wait(&S.bar_w, 0, kTcWaitNs)) {
+                failed = true;
+                S.fail = 1;
+                atomicOr(err, kErrTensorWait);
+            }
         }
-        wait(&S.bar_mma, ph);
-        const uint64_t m2 = train_hidden_epilogue(S, tl, S.bias + kGImgB2, kZh2);
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        if (tid == 0) {
-            train_issue<kGHid, kGOutPad>(T, za, kZK, kZh2, wa + 2 * kGImgW3);
-            tc::commit(&S.bar_mma);
-        }
-        wait(&S.bar_mma, ph);
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        tc::fence_after_sync();
-        {   // loss and dLoss/dOutput of this thread's record (times n)
+        if (step_sync()) break;
+        // layer 1: P (x) -> h1 into Q and Z
+        if (tid == 0) fb_issue<kGEnc, kGHid>(T, pa, wa + 2 * kGImgW1, &S.bar_mma);
+        wait();
+        const uint64_t m1 = fb_hidden_epilogue(tl, S.bias + kGImgB1, S.q, zt, kZh1);
+        if (step_sync()) break;
+        // layer 2: Q (h1) -> h2 into P and Z
+        if (tid == 0) fb_issue<kGHid, kGHid>(T, qa, wa + 2 * kGImgW2, &S.bar_mma);
+        wait();
+        const uint64_t m2 = fb_hidden_epilogue(tl, S.bias + kGImgB2, S.p, zt, kZh2);
+        if (step_sync()) break;
+        // layer 3: P (h2) -> outputs
+        if (tid == 0) fb_issue<kGHid, kGOutPad>(T, pa, wa + 2 * kGImgW3, &S.bar_mma);
+        wait();
+        {   // loss and dLoss/dOutput of this thread's record (times n) into Q (K = 48) and D
             float o[kGOutPad];
 #pragma unroll
             for (int c0 = 0; c0 < kGOutPad; c0 += 16) tc::ld_32x32b_x16(tl + c0, o + c0);
@@ -334,99 +357,204 @@ __global__ void __launch_bounds__(kTcRows) k_guide_train_tc(const void* image, c
                     const int k = c + 2 * j;
                     p[j] = pack_h2_sat(k < kGOut ? dd[k] : 0.f, k + 1 < kGOut ? dd[k + 1] : 0.f);
                 }
-                *reinterpret_cast<uint4*>(S.d + canon_index(tid, kDd0 + c, kDK)) = make_uint4(p[0], p[1], p[2], p[3]);
+                put_chunk(S.q, kGOutPad, dt, kDK, tid, c, kDd0 + c, make_uint4(p[0], p[1], p[2], p[3]));
             }
         }
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        // backward through layer 3, then layer 2
-        if (tid == 0) {
-            train_issue<kGOutPad, kGHid>(T, da, kDK, kDd0, wa + kGImgW3T);
-            tc::commit(&S.bar_mma);
-        }
-        wait(&S.bar_mma, ph);
-        train_backward_epilogue(S, tl, m2, kDd2);
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        if (tid == 0) {
-            train_issue<kGHid, kGHid>(T, da, kDK, kDd2, wa + kGImgW2T);
-            tc::commit(&S.bar_mma);
-        }
-        wait(&S.bar_mma, ph);
-        train_backward_epilogue(S, tl, m1, kDd1);
-        tc::fence_smem_to_async();
-        tc::fence_before_sync();
-        if (__syncthreads_or(failed)) break;
-        // weight and bias gradients over the tile's 128 records (MN-major
-        // operands, 16 records per instruction), accumulated across tiles
-        if (tid == 0) {
-            tc::fence_after_sync();
-            constexpr uint32_t id12 = tc::idesc_f16_f32(kTcRows, 224, true, true);
-            constexpr uint32_t id3 = tc::idesc_f16_f32(kTcRows, 80, true, true);
-#pragma unroll
-            for (int ks = 0; ks < kTcRows / 16; ks++) {
-                const uint32_t acc = first && ks == 0 ? 0u : 1u;
-                tc::mma_f16(T + kAccW12, tc::smem_desc(da + (kDd1 / 8) * 128 + ks * 2 * kDK * 16, kDK * 16, 128),
-                            tc::smem_desc(za + ks * 2 * kZK * 16, kZK * 16, 128), id12, acc);
-                tc::mma_f16(T + kAccW3, tc::smem_desc(da + ks * 2 * kDK * 16, kDK * 16, 128),
-                            tc::smem_desc(za + (kZones / 8) * 128 + ks * 2 * kZK * 16, kZK * 16, 128), id3, acc);
-            }
-            tc::commit(&S.bar_g);
-        }
-        pending = true;
-        first = false;
-    }
-    if (pending) wait(&S.bar_g, phg);
-    tc::fence_before_sync();
-    const bool bad = __syncthreads_or(failed) != 0;
-    tc::fence_after_sync();
-    if (!bad && !first) {
-        // accumulator lane m: rows 0..63 = units of layer 1 (dW1, b1), 64..127
-        // = units of layer 2 (dW2, b2); of the second product rows 0..39 =
-        // the outputs (b3 in column 0, dW3 in columns 16..79)
-        const int m = tid;
-        float v[16];
-        if (warp < 2) {
-            for (int c0 = 0; c0 < kGEnc; c0 += 16) {
-                tc::ld_32x32b_x16(tl + kAccW12 + c0, v);
-#pragma unroll
-                for (int j = 0; j < 16; j++) atomicAdd(grad + kGW1 + m * kGEnc + c0 + j, v[j] * inv_n);
-            }
-        } else {
-            for (int c0 = 0; c0 < kGHid; c0 += 16) {
-                tc::ld_32x32b_x16(tl + kAccW12 + kZh1 + c0, v);
-#pragma unroll
-                for (int j = 0; j < 16; j++) atomicAdd(grad + kGW2 + (m - kGHid) * kGHid + c0 + j, v[j] * inv_n);
-            }
-        }
-        tc::ld_32x32b_x16(tl + kAccW12 + kZones, v);
-        atomicAdd(grad + (warp < 2 ? kGB1 + m : kGB2 + m - kGHid), v[0] * inv_n);
-        for (int c0 = 0; c0 < 80; c0 += 16) {
-            tc::ld_32x32b_x16(tl + kAccW3 + c0, v);
-            if (m < kGOut) {
-                if (c0 == 0) {
-                    atomicAdd(grad + kGB3 + m, v[0] * inv_n);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; j++) atomicAdd(grad + kGW3 + m * kGHid + c0 - 16 + j, v[j] * inv_n);
-                }
-            }
-        }
+        if (step_sync()) break;
+        // backward through layer 3: Q (d0) x W3 -> d2 into P and D
+        if (tid == 0) fb_issue<kGOutPad, kGHid>(T, qa, wa + kGImgW3T, &S.bar_mma);
+        wait();
+        fb_backward_epilogue(tl, m2, S.p, dt, kDd2);
+        if (step_sync()) break;
+        // backward through layer 2: P (d2) x W2 -> d1 into D
+        if (tid == 0) fb_issue<kGHid, kGHid>(T, pa, wa + kGImgW2T, &S.bar_mma);
+        wait();
+        fb_backward_epilogue(tl, m1, nullptr, dt, kDd1);
+        if (step_sync()) break;
     }
     for (int o = 16; o; o >>= 1) lacc += __shfl_xor_sync(0xffffffffu, lacc, o);
-    if ((tid & 31) == 0) atomicAdd(loss, lacc * inv_n);
+    if ((tid & 31) == 0) atomicAdd(loss, lacc / (float)n);
     tc::fence_before_sync();
     __syncthreads();
     if (S.fail) {
         (void)tc::mbar_wait(&S.bar_w, 0, kTcWaitNs);
         (void)tc::mbar_wait(&S.bar_mma, ph, kTcWaitNs);
-        (void)tc::mbar_wait(&S.bar_g, phg, kTcWaitNs);
     }
     if (tid < 32) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(T, kTrainCols);
+        tc::tmem_dealloc(T, kFbCols);
+    }
+}
+
+// Weight gradients: split-K over 64-record slices of the staged Z and D.
+constexpr int kWgRecs = 64;                            // records per pipeline stage
+constexpr int kWgStages = 3;
+constexpr uint32_t kWgZBytes = kWgRecs * kZK * 2;      // 36,864
+constexpr uint32_t kWgDBytes = kWgRecs * kDK * 2;      // 22,528
+constexpr int kWgCols = 512;                           // tensor memory: 224 + 80 accumulator columns
+constexpr int kAcc12 = 0, kAcc3 = 224;
+
+struct GuideWgSmem {
+    alignas(128) __half z[kWgStages][kWgRecs * kZK];
+    alignas(128) __half d[kWgStages][kWgRecs * kDK];
+    uint64_t full[kWgStages], empty[kWgStages], done;
+    uint32_t tmem;
+    int fail;
+};
+// no other tensor-memory user of this library (the guided material and
+// inference blocks, 107 KB) fits beside a block: its 512 columns are free
+static_assert(sizeof(GuideWgSmem) + 1024 + 107 * 1024 > 228 * 1024, "one tensor-memory user per SM");
+
+__global__ void __launch_bounds__(kTcRows) k_guide_wgrad(const __half* zg, const __half* dg, int nslices,
+                                                          float* partial, unsigned* err) {
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    GuideWgSmem& S = *reinterpret_cast<GuideWgSmem*>(dyn_smem);
+    const int tid = threadIdx.x;
+    // this block's slices [s0, s1)
+    const int per = nslices / (int)gridDim.x, extra = nslices % (int)gridDim.x;
+    const int b = blockIdx.x;
+    const int s0 = b * per + min(b, extra), s1 = s0 + per + (b < extra ? 1 : 0);
+    const int steps = s1 - s0;
+    if (tid == 0) {
+        for (int k = 0; k < kWgStages; k++) {
+            tc::mbar_init(&S.full[k], 1);
+            tc::mbar_init(&S.empty[k], 1);
+        }
+        tc::mbar_init(&S.done, 1);
+        S.fail = 0;
+    }
+    if (tid < 32) tc::tmem_alloc(&S.tmem, kWgCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t T = S.tmem;
+    if (tid == 0 && steps > 0) {
+        bool failed = false;
+        // per stage: the parity of its copy in flight, -1 for none (a stage
+        // is refilled only after its previous copy was waited for)
+        int inflight[kWgStages];
+        for (int k = 0; k < kWgStages; k++) inflight[k] = -1;
+        auto load = [&](int i) {  // slice s0 + i into stage i % kWgStages
+            const int st = i % kWgStages;
+            const size_t sl = (size_t)(s0 + i);
+            inflight[st] = (i / kWgStages) & 1;
+            tc::mbar_expect_tx(&S.full[st], kWgZBytes + kWgDBytes);
+            tc::bulk_copy(S.z[st], zg + sl * kWgRecs * kZK, kWgZBytes, &S.full[st]);
+            tc::bulk_copy(S.d[st], dg + sl * kWgRecs * kDK, kWgDBytes, &S.full[st]);
+        };
+        auto fail_now = [&]() {
+            failed = true;
+            S.fail = 1;
+            atomicOr(err, kErrTensorWait);
+        };
+        for (int i = 0; i < min(kWgStages, steps); i++) load(i);
+        constexpr uint32_t id12 = tc::idesc_f16_f32(kTcRows, 224, true, true);
+        constexpr uint32_t id3 = tc::idesc_f16_f32(kTcRows, 80, true, true);
+        for (int i = 0; i < steps && !failed; i++) {
+            const int st = i % kWgStages;
+            if (!tc::mbar_wait(&S.full[st], (uint32_t)(i / kWgStages) & 1u, kTcWaitNs)) {
+                fail_now();
+                break;
+            }
+            inflight[st] = -1;
+            tc::fence_after_sync();
+            const uint32_t za = tc::smem_addr(S.z[st]), da = tc::smem_addr(S.d[st]);
+#pragma unroll
+            for (int ks = 0; ks < kWgRecs / 16; ks++) {
+                const uint32_t acc = i == 0 && ks == 0 ? 0u : 1u;
+                tc::mma_f16(T + kAcc12, tc::smem_desc(da + (kDd1 / 8) * 128 + ks * 2 * kDK * 16, kDK * 16, 128),
+                            tc::smem_desc(za + ks * 2 * kZK * 16, kZK * 16, 128), id12, acc);
+                tc::mma_f16(T + kAcc3, tc::smem_desc(da + ks * 2 * kDK * 16, kDK * 16, 128),
+                            tc::smem_desc(za + (kZones / 8) * 128 + ks * 2 * kZK * 16, kZK * 16, 128), id3, acc);
+            }
+            tc::commit(&S.empty[st]);
+            // refill the stage the previous slice used, once its products are
+            // done (this slice's products queue behind them meanwhile)
+            const int j = i - 1;
+            if (j >= 0 && j + kWgStages < steps) {
+                const int sj = j % kWgStages;
+                if (!tc::mbar_wait(&S.empty[sj], (uint32_t)(j / kWgStages) & 1u, kTcWaitNs)) {
+                    fail_now();
+                    break;
+                }
+                load(j + kWgStages);
+            }
+        }
+        tc::commit(&S.done);
+        if (!tc::mbar_wait(&S.done, 0, kTcWaitNs)) fail_now();
+        if (failed) {
+            // let every copy in flight land before the block frees its
+            // shared memory (bounded waits)
+            for (int k = 0; k < kWgStages; k++)
+                if (inflight[k] >= 0) (void)tc::mbar_wait(&S.full[k], (uint32_t)inflight[k], kTcWaitNs);
+        }
+    }
+    tc::fence_before_sync();
+    const bool bad = __syncthreads_or(tid == 0 ? S.fail : 0) != 0;
+    tc::fence_after_sync();
+    // the block's partial sums, in the parameter layout (each thread writes
+    // its accumulator lane's entries as contiguous runs)
+    float* out = partial + (size_t)b * kGParams;
+    const uint32_t tl = T + ((uint32_t)(tid & ~31) << 16);
+    const bool live = steps > 0 && !bad;
+    auto lane_run = [&](uint32_t col, int dst) {  // 16 columns of this lane -> out[dst .. dst + 16)
+        float v[16];
+        if (live) {
+            tc::ld_32x32b_x16(tl + col, v);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = 0.f;
+        }
+        if (dst >= 0) {
+#pragma unroll
+            for (int j = 0; j < 16; j += 4)
+                *reinterpret_cast<float4*>(out + dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+        }
+        return v[0];
+    };
+    const int m = tid;
+    // lanes 0..63: units of layer 1 (dW1 rows, b1); 64..127: layer 2 (dW2, b2)
+    for (int c0 = 0; c0 < kGEnc; c0 += 16) (void)lane_run(kAcc12 + c0, m < kGHid ? kGW1 + m * kGEnc + c0 : -1);
+    for (int c0 = 0; c0 < kGHid; c0 += 16)
+        (void)lane_run(kAcc12 + kZh1 + c0, m >= kGHid ? kGW2 + (m - kGHid) * kGHid + c0 : -1);
+    const float gb = lane_run(kAcc12 + kZones, -1);
+    out[m < kGHid ? kGB1 + m : kGB2 + m - kGHid] = gb;
+    // lanes 0..39 of the second product: the outputs (b3 in column 0, dW3 in 16..79)
+    const float g3 = lane_run(kAcc3, -1);
+    if (m < kGOut) out[kGB3 + m] = g3;
+    for (int c0 = 16; c0 < 80; c0 += 16)
+        (void)lane_run(kAcc3 + c0, m < kGOut ? kGW3 + m * kGHid + (c0 - 16) : -1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid < 32) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(T, kWgCols);
+    }
+}
+
+// grad[i] = (1/n) sum over the weight-gradient blocks of their partial
+// sums (parameter layout).  A block takes 32 consecutive parameters; its 8
+// warps split the partials and add their sums in shared memory.  The padding
+// outputs of layer 3 (rows 40..47) have no entries and stay as they are.
+constexpr int kRedWarps = 8;
+__global__ void __launch_bounds__(32 * kRedWarps) k_guide_grad_reduce(const float* partial, int nblocks, float inv_n,
+                                                                        float* grad) {
+    __shared__ float s_sum[kRedWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + lane;
+    const bool pad = (i >= kGW3 + kGOut * kGHid && i < kGB3) || i >= kGB3 + kGOut;
+    float acc = 0.f;
+    if (i < kGParams && !pad) {
+#pragma unroll 4
+        for (int b = w; b < nblocks; b += kRedWarps) acc += partial[(size_t)b * kGParams + i];
+    }
+    s_sum[w][lane] = acc;
+    __syncthreads();
+    if (w == 0 && i < kGParams && !pad) {
+        float t = 0.f;
+#pragma unroll
+        for (int k = 0; k < kRedWarps; k++) t += s_sum[k][lane];
+        grad[i] = t * inv_n;
     }
 }
 
@@ -499,24 +627,51 @@ void guide_upload_params(dl_guide* G, const float* host) {
     DL_CUDA(cudaGetLastError());
 }
 
-// Gradient of the loss over `n` device records (every `stride`-th) added to
-// G->grad; the loss sum lands in scratch[1].
+// Device buffers of a training batch of up to n records: the staged
+// activations (Z, D) and the weight-gradient partial sums.  Called before
+// any training launch, outside graph captures and render loops.
+void guide_reserve(dl_guide* G, int64_t n) {
+    const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
+    G->stage_z.ensure((size_t)ntiles * kTcRows * kZK * 2);
+    G->stage_d.ensure((size_t)ntiles * kTcRows * kDK * 2);
+    const int64_t nslices = ntiles * (kTcRows / kWgRecs);
+    const int64_t nb = std::min<int64_t>(nslices, std::max(1, G->ctx->num_sms));
+    G->partial.ensure((size_t)nb * kGParams * 4);
+}
+
+// Gradient of the loss over `n` device records (every `stride`-th) written
+// to G->grad (entries outside the network's parameters untouched); the
+// loss sum lands in scratch[1].  guide_reserve(G, n) must have run.
 void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cudaStream_t st) {
     static const bool setup = [] {
-        DL_CUDA(cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(GuideTrainSmem)));
+        DL_CUDA(cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(GuideFbSmem)));
+        DL_CUDA(cudaFuncSetAttribute(k_guide_fwdbwd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        DL_CUDA(cudaFuncSetAttribute(k_guide_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(GuideWgSmem)));
         return true;
     }();
     (void)setup;
+    const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
+    const int64_t nslices = ntiles * (kTcRows / kWgRecs);
+    const int sms = std::max(1, G->ctx->num_sms);
+    const int nb = (int)std::min<int64_t>(nslices, sms);
+    if (G->stage_z.bytes < (size_t)ntiles * kTcRows * kZK * 2 || G->stage_d.bytes < (size_t)ntiles * kTcRows * kDK * 2 ||
+        G->partial.bytes < (size_t)nb * kGParams * 4)
+        throw Error(DL_ERR_INVALID_ARG, "guide training buffers not reserved for this batch");
     float* sc = G->scratch.as<float>();
     unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
     DL_CUDA(cudaMemsetAsync(sc, 0, 2 * sizeof(float), st));
     const GuideRecord* R = static_cast<const GuideRecord*>(d_recs);
     k_guide_weight_sum<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(R, (int)n, stride, sc);
-    const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
-    const int blocks = (int)std::min<int64_t>(ntiles, G->ctx->num_sms);
-    k_guide_train_tc<<<blocks, kTcRows, sizeof(GuideTrainSmem), st>>>(G->image.ptr, R, (int)n, stride, sc,
-                                                                       G->grad.as<float>(), sc + 1, err);
+    const int fb_blocks = (int)std::min<int64_t>(ntiles, 2 * (int64_t)sms);
+    k_guide_fwdbwd<<<fb_blocks, kTcRows, sizeof(GuideFbSmem), st>>>(G->image.ptr, R, (int)n, stride, sc,
+                                                                     G->stage_z.as<__half>(), G->stage_d.as<__half>(),
+                                                                     sc + 1, err);
+    k_guide_wgrad<<<nb, kTcRows, sizeof(GuideWgSmem), st>>>(G->stage_z.as<__half>(), G->stage_d.as<__half>(),
+                                                            (int)nslices, G->partial.as<float>(), err);
+    k_guide_grad_reduce<<<(kGParams + 31) / 32, 32 * kRedWarps, 0, st>>>(G->partial.as<float>(), nb, 1.f / (float)n,
+                                                                         G->grad.as<float>());
     DL_CUDA(cudaGetLastError());
 }
 
@@ -535,6 +690,7 @@ void guide_adam(dl_guide* G, cudaStream_t st) {
 float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps) {
     cudaStream_t st = G->ctx->stream;
     float loss = 0.f;
+    guide_reserve(G, n);
     for (int k = 0; k < steps; k++) {
         guide_gradient(G, d_recs, n, 1, st);
         guide_adam(G, st);

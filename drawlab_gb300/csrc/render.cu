@@ -1765,6 +1765,8 @@ void render_guided(dl_scene* S, const dl_render_opts& o, dl_guide* G, float* d_f
     const int64_t rec_cap = std::min<int64_t>((int64_t)G->cfg.batch * std::max(1, G->cfg.steps_per_pass), 1 << 23);
     GuideRecord* rec_half[2] = {nullptr, nullptr};
     if (train) {
+        // a training step takes at most ceil(rec_cap / steps) records
+        guide_reserve(G, (rec_cap + std::max(1, G->cfg.steps_per_pass) - 1) / std::max(1, G->cfg.steps_per_pass));
         // two halves: pass k writes half k % 2 while the training stream
         // learns from the other half (the previous pass)
         G->pass_recs.ensure(2 * (size_t)rec_cap * sizeof(GuideRecord));

@@ -55,6 +55,7 @@ constexpr int kGuideImageBytes = 47808;   // fp16 weights in the tensor cores' l
 constexpr int kGuideErrOffset = 64;       // byte offset of the error word in dl_guide::scratch
 void guide_init_params(uint64_t seed, std::vector<float>& w);
 void guide_upload_params(dl_guide* G, const float* host);
+void guide_reserve(dl_guide* G, int64_t n);   // training buffers for batches of up to n records
 void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cudaStream_t st);
 void guide_adam(dl_guide* G, cudaStream_t st);
 float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps);

@@ -130,6 +130,17 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
 }
 
+// Bulk copies that share one transaction count: arm the barrier once with
+// the total bytes, then issue the copies (each completes its bytes on it).
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(smem_addr(mbar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
+}
+
 // 32 lanes x 16 consecutive 32-bit columns: thread l of the warp receives
 // TMEM lane (warp's lane base + l), columns [col, col + 16).
 __device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, float* v) {
