@@ -92,11 +92,11 @@ NET_MAC_FWD = 144 * 64 + 64 * 64 + 64 * 48
 NET_MAC_TRAIN = NET_MAC_FWD + (48 * 64 + 64 * 64) + NET_MAC_FWD
 
 
-def network_roofline(ctx, api, train_rows=(32768, 131072)):
+def network_roofline(ctx, api, train_rows=(131072, 32768)):
     """Device time of the network kernels alone (dl_guide_forward on 4M rows;
     dl_guide_gradient on training batches of train_rows records, the first
-    the renderer's default batch), as FLOP/s against the measured tensor
-    peak and as bytes/s against HBM."""
+    the renderer's default batch, 131072), as FLOP/s against the measured
+    tensor peak and as bytes/s against HBM."""
     tpk, tkind = tensor_peak()
     hbm, hkind = peaks()
     rng = np.random.default_rng(3)

@@ -631,7 +631,7 @@ int dl_guide_default_config(dl_guide_config* cfg) {
     std::memset(cfg, 0, sizeof(*cfg));
     cfg->learning_rate = 2e-3f;
     cfg->guide_fraction = 0.5f;
-    cfg->batch = 32768;
+    cfg->batch = 131072;
     cfg->steps_per_pass = 16;
     cfg->max_guided_depth = 6;
     cfg->seed = 1;

@@ -75,48 +75,95 @@ __global__ void __launch_bounds__(kTcThreads) k_guide_infer(const void* image, c
 // whole gradient of a batch.
 constexpr float kGTargetClamp = 20.f;
 
-__global__ void k_guide_weight_sum(const GuideRecord* s, int n, int stride, float* sum) {
+// Per block of 256 threads, the sum of L / p over its records into
+// part[blockIdx.x] (the training kernel adds the blocks' sums); block 0
+// also clears the batch's loss accumulator.
+constexpr int kWsumThreads = 256, kWsumMaxBlocks = 1024;
+__global__ void __launch_bounds__(kWsumThreads) k_guide_weight_sum(const GuideRecord* s, int n, int stride,
+                                                                    float* part, float* loss) {
+    tc::pdl_launch_dependents();
+    __shared__ float s_w[kWsumThreads / 32];
     float acc = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const GuideRecord& r = s[(size_t)i * stride];
         acc += r.pdf > 0.f ? r.L / r.pdf : 0.f;
     }
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int k = 0; k < kWsumThreads / 32; k++) t += s_w[k];
+        part[blockIdx.x] = t;
+        if (blockIdx.x == 0) *loss = 0.f;
+    }
 }
 
-// The loss of one record and dLoss/dOutput (40 values, scaled by `scale`).
+// The loss of one record and dLoss/dOutput (40 values, scaled by `scale`):
+// the lobes decoded as decode_lobes does and the mixture's pdf as vmf_pdf
+// (guide.cuh), here with the hardware's fast exponential, logarithm and
+// division -- this runs once per record and training step, latency-bound,
+// and the gradients stay within the oracle's 1e-2 -- where the renderer's
+// sampling keeps the accurate forms.
 __device__ __forceinline__ float record_grad(const float* o, const GuideRecord& s, float scale, float* d) {
-    VmfLobe L[kGLobes];
-    decode_lobes(o, L);
     const float3 w = f3(s.w[0], s.w[1], s.w[2]);
-    float pj[kGLobes], q = 0.f;
+    float mx = -1e30f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) mx = fmaxf(mx, o[5 * j + 4]);
+    float3 mu[kGLobes];
+    float kap[kGLobes], lam[kGLobes], inv_len[kGLobes], pj[kGLobes];
+    bool clamped[kGLobes];
+    float lsum = 0.f;
 #pragma unroll
     for (int j = 0; j < kGLobes; j++) {
-        pj[j] = L[j].lambda * vmf_pdf(L[j].mu, L[j].kappa, w);
+        const float3 m = f3(o[5 * j], o[5 * j + 1], o[5 * j + 2]);
+        const float len2 = m.x * m.x + m.y * m.y + m.z * m.z;
+        if (len2 > 1e-12f) {
+            inv_len[j] = rsqrtf(len2);
+            mu[j] = f3(m.x * inv_len[j], m.y * inv_len[j], m.z * inv_len[j]);
+        } else {
+            inv_len[j] = 0.f;
+            mu[j] = f3(0.f, 0.f, 1.f);
+        }
+        const float lk = o[5 * j + 3];
+        clamped[j] = lk < kGLogKappaMin || lk > kGLogKappaMax;
+        kap[j] = __expf(fminf(fmaxf(lk, kGLogKappaMin), kGLogKappaMax));
+        lam[j] = __expf(o[5 * j + 4] - mx);
+        lsum += lam[j];
+    }
+    const float inv_sum = __fdividef(1.f, lsum);
+    float q = 0.f;
+#pragma unroll
+    for (int j = 0; j < kGLobes; j++) {
+        lam[j] *= inv_sum;
+        const float k = kap[j];
+        const float dot = mu[j].x * w.x + mu[j].y * w.y + mu[j].z * w.z;
+        const float pdf = k < 1e-4f ? 0.25f * kInvPiF
+                                    : k * __fdividef(1.f, 2.f * kPiF * (1.f - __expf(-2.f * k))) * __expf(k * (dot - 1.f));
+        pj[j] = lam[j] * pdf;
         q += pj[j];
     }
     for (int j = 0; j < kGOut; j++) d[j] = 0.f;
     if (!(q > 1e-30f) || !(scale > 0.f) || !isfinite(scale)) return 0.f;
+    const float inv_q = __fdividef(1.f, q);
 #pragma unroll
     for (int j = 0; j < kGLobes; j++) {
-        const float r = pj[j] / q, k = L[j].kappa;
-        const float3 mu = L[j].mu;
-        const float dot = mu.x * w.x + mu.y * w.y + mu.z * w.z;
+        const float r = pj[j] * inv_q, k = kap[j];
+        const float dot = mu[j].x * w.x + mu[j].y * w.y + mu[j].z * w.z;
         // d(-log q)/d(logit_j) = -(r_j - lambda_j)
-        d[5 * j + 4] = -scale * (r - L[j].lambda);
+        d[5 * j + 4] = -scale * (r - lam[j]);
         // d(-log q)/d(log kappa_j) = -r_j (1 - 2k / (e^{2k} - 1) + k (mu.w - 1))
-        if (!L[j].clamped) {
-            float t = k < 1e-4f ? 0.f : 1.f - 2.f * k / expm1f(2.f * k) + k * (dot - 1.f);
+        if (!clamped[j]) {
+            const float t = k < 1e-4f ? 0.f : 1.f - __fdividef(2.f * k, __expf(2.f * k) - 1.f) + k * (dot - 1.f);
             d[5 * j + 3] = -scale * r * t;
         }
         // d(-log q)/dm_j = -r_j kappa_j (w - (mu.w) mu) / |m_j|
-        const float f = -scale * r * k * L[j].inv_len;
-        d[5 * j + 0] = f * (w.x - dot * mu.x);
-        d[5 * j + 1] = f * (w.y - dot * mu.y);
-        d[5 * j + 2] = f * (w.z - dot * mu.z);
+        const float f = -scale * r * k * inv_len[j];
+        d[5 * j + 0] = f * (w.x - dot * mu[j].x);
+        d[5 * j + 1] = f * (w.y - dot * mu[j].y);
+        d[5 * j + 2] = f * (w.z - dot * mu[j].z);
     }
-    return -scale * logf(q);
+    return -scale * __logf(q);
 }
 
 // One training batch on the tensor cores, in three kernels:
@@ -247,8 +294,8 @@ __device__ __forceinline__ void fb_issue(uint32_t acc, uint32_t a_base, uint32_t
 }
 
 __global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, const GuideRecord* s, int n, int stride,
-                                                           const float* wsum, __half* zg, __half* dg, float* loss,
-                                                           unsigned* err) {
+                                                           const float* wsum, int nwsum, __half* zg, __half* dg,
+                                                           float* loss, unsigned* err) {
     extern __shared__ __align__(128) unsigned char dyn_smem[];
     GuideFbSmem& S = *reinterpret_cast<GuideFbSmem*>(dyn_smem);
     const int tid = threadIdx.x;
@@ -260,6 +307,7 @@ __global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, con
         S.fail = 0;
     }
     if (tid < 32) tc::tmem_alloc(&S.tmem, kFbCols);
+    tc::pdl_launch_dependents();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -288,7 +336,7 @@ __global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, con
     const uint32_t T = S.tmem;
     const uint32_t tl = T + ((uint32_t)(tid & ~31) << 16);  // this warp's lanes, column 0
     const uint32_t pa = tc::smem_addr(S.p), qa = tc::smem_addr(S.q), wa = tc::smem_addr(S.w);
-    const float mean = *wsum / (float)n;
+    float mean = 0.f;   // read once the batch's weight sum is complete
     float lacc = 0.f;
     const uint32_t one2 = pack_h2(1.f, 1.f);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -296,13 +344,9 @@ __global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, con
         __half* zt = zg + (size_t)tile * kTcRows * kZK;
         __half* dt = dg + (size_t)tile * kTcRows * kDK;
         GuideRecord rec = {};
-        float sc = 0.f;  // the record's loss weight times n
-        if (r < n) {
-            rec = s[(size_t)r * stride];
-            if (rec.pdf > 0.f && mean > 0.f) sc = fminf(rec.L / rec.pdf / mean, kGTargetClamp);
-        }
+        if (r < n) rec = s[(size_t)r * stride];
         // x: the encoding, into P (K = 144) and Z; the columns of ones into Z
-#pragma unroll 1
+#pragma unroll
         for (int i = 0; i < kGIn; i++) {
             __half2 h[kGFreq];
             encode_scalar_h2(rec.in[i], h);
@@ -326,7 +370,13 @@ __global__ void __launch_bounds__(kTcRows) k_guide_fwdbwd(const void* image, con
                 S.fail = 1;
                 atomicOr(err, kErrTensorWait);
             }
+            tc::pdl_wait();   // k_guide_weight_sum has finished
+            float sum = 0.f;
+            for (int k = 0; k < nwsum; k++) sum += wsum[k];   // the same order in every block
+            mean = sum / (float)n;
         }
+        // the record's loss weight times n
+        const float sc = r < n && rec.pdf > 0.f && mean > 0.f ? fminf(rec.L / rec.pdf / mean, kGTargetClamp) : 0.f;
         if (step_sync()) break;
         // layer 1: P (x) -> h1 into Q and Z
         if (tid == 0) fb_issue<kGEnc, kGHid>(T, pa, wa + 2 * kGImgW1, &S.bar_mma);
@@ -424,10 +474,12 @@ __global__ void __launch_bounds__(kTcRows) k_guide_wgrad(const __half* zg, const
         S.fail = 0;
     }
     if (tid < 32) tc::tmem_alloc(&S.tmem, kWgCols);
+    tc::pdl_launch_dependents();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t T = S.tmem;
+    tc::pdl_wait();   // k_guide_fwdbwd has staged every tile (and the previous reduction read the partials)
     if (tid == 0 && steps > 0) {
         bool failed = false;
         // per stage: the parity of its copy in flight, -1 for none (a stage
@@ -493,37 +545,43 @@ __global__ void __launch_bounds__(kTcRows) k_guide_wgrad(const __half* zg, const
     const bool bad = __syncthreads_or(tid == 0 ? S.fail : 0) != 0;
     tc::fence_after_sync();
     // the block's partial sums, in the parameter layout (each thread writes
-    // its accumulator lane's entries as contiguous runs)
+    // its accumulator lane's entries as contiguous runs); which columns a
+    // warp reads depends on its lanes' units, the same for all its lanes
     float* out = partial + (size_t)b * kGParams;
     const uint32_t tl = T + ((uint32_t)(tid & ~31) << 16);
     const bool live = steps > 0 && !bad;
-    auto lane_run = [&](uint32_t col, int dst) {  // 16 columns of this lane -> out[dst .. dst + 16)
-        float v[16];
-        if (live) {
-            tc::ld_32x32b_x16(tl + col, v);
+    const int m = tid, warp = tid >> 5;
+    auto run = [&](uint32_t col, int ncols, int dst, bool keep) {  // ncols (16 or 32) columns -> out[dst ..)
+        float v[32];
+        if (!live) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) v[j] = 0.f;
+        } else if (ncols == 32) {
+            tc::ld_32x32b_x32(tl + col, v);
         } else {
-#pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = 0.f;
+            tc::ld_32x32b_x16(tl + col, v);
         }
-        if (dst >= 0) {
-#pragma unroll
-            for (int j = 0; j < 16; j += 4)
+        if (keep)
+            for (int j = 0; j < ncols; j += 4)
                 *reinterpret_cast<float4*>(out + dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-        }
         return v[0];
     };
-    const int m = tid;
-    // lanes 0..63: units of layer 1 (dW1 rows, b1); 64..127: layer 2 (dW2, b2)
-    for (int c0 = 0; c0 < kGEnc; c0 += 16) (void)lane_run(kAcc12 + c0, m < kGHid ? kGW1 + m * kGEnc + c0 : -1);
-    for (int c0 = 0; c0 < kGHid; c0 += 16)
-        (void)lane_run(kAcc12 + kZh1 + c0, m >= kGHid ? kGW2 + (m - kGHid) * kGHid + c0 : -1);
-    const float gb = lane_run(kAcc12 + kZones, -1);
-    out[m < kGHid ? kGB1 + m : kGB2 + m - kGHid] = gb;
-    // lanes 0..39 of the second product: the outputs (b3 in column 0, dW3 in 16..79)
-    const float g3 = lane_run(kAcc3, -1);
-    if (m < kGOut) out[kGB3 + m] = g3;
-    for (int c0 = 16; c0 < 80; c0 += 16)
-        (void)lane_run(kAcc3 + c0, m < kGOut ? kGW3 + m * kGHid + (c0 - 16) : -1);
+    if (warp < 2) {
+        // lanes 0..63: units of layer 1 (dW1 rows from the x columns, b1)
+        for (int c0 = 0; c0 < 128; c0 += 32) (void)run(kAcc12 + c0, 32, kGW1 + m * kGEnc + c0, true);
+        (void)run(kAcc12 + 128, 16, kGW1 + m * kGEnc + 128, true);
+        out[kGB1 + m] = run(kAcc12 + kZones, 16, 0, false);
+        // lanes 0..39 of the second product: the outputs (b3 in column 0, dW3 in 16..79)
+        const bool o = m < kGOut;
+        const float g3 = run(kAcc3, 16, 0, false);
+        if (o) out[kGB3 + m] = g3;
+        for (int c0 = 16; c0 < 80; c0 += 32) (void)run(kAcc3 + c0, 32, kGW3 + m * kGHid + (c0 - 16), o);
+    } else {
+        // lanes 64..127: units of layer 2 (dW2 rows from the h1 columns, b2)
+        for (int c0 = 0; c0 < kGHid; c0 += 32)
+            (void)run(kAcc12 + kZh1 + c0, 32, kGW2 + (m - kGHid) * kGHid + c0, true);
+        out[kGB2 + m - kGHid] = run(kAcc12 + kZones, 16, 0, false);
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (tid < 32) {
@@ -540,6 +598,7 @@ constexpr int kRedWarps = 8;
 __global__ void __launch_bounds__(32 * kRedWarps) k_guide_grad_reduce(const float* partial, int nblocks, float inv_n,
                                                                         float* grad) {
     __shared__ float s_sum[kRedWarps][32];
+    tc::pdl_wait();   // k_guide_wgrad has written every block's partials
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int i = blockIdx.x * 32 + lane;
     const bool pad = (i >= kGW3 + kGOut * kGHid && i < kGB3) || i >= kGB3 + kGOut;
@@ -627,6 +686,25 @@ void guide_upload_params(dl_guide* G, const float* host) {
     DL_CUDA(cudaGetLastError());
 }
 
+// A launch on `st` that may begin while the previous kernel of the stream is
+// still running (programmatic stream serialization); the kernel waits for
+// that kernel (griddepcontrol.wait) before it reads what it wrote.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Device buffers of a training batch of up to n records: the staged
 // activations (Z, D) and the weight-gradient partial sums.  Called before
 // any training launch, outside graph captures and render loops.
@@ -637,6 +715,7 @@ void guide_reserve(dl_guide* G, int64_t n) {
     const int64_t nslices = ntiles * (kTcRows / kWgRecs);
     const int64_t nb = std::min<int64_t>(nslices, std::max(1, G->ctx->num_sms));
     G->partial.ensure((size_t)nb * kGParams * 4);
+    G->wsum.ensure(kWsumMaxBlocks * sizeof(float));
 }
 
 // Gradient of the loss over `n` device records (every `stride`-th) written
@@ -657,21 +736,31 @@ void guide_gradient(dl_guide* G, const void* d_recs, int64_t n, int stride, cuda
     const int sms = std::max(1, G->ctx->num_sms);
     const int nb = (int)std::min<int64_t>(nslices, sms);
     if (G->stage_z.bytes < (size_t)ntiles * kTcRows * kZK * 2 || G->stage_d.bytes < (size_t)ntiles * kTcRows * kDK * 2 ||
-        G->partial.bytes < (size_t)nb * kGParams * 4)
+        G->partial.bytes < (size_t)nb * kGParams * 4 || G->wsum.bytes < kWsumMaxBlocks * sizeof(float))
         throw Error(DL_ERR_INVALID_ARG, "guide training buffers not reserved for this batch");
-    float* sc = G->scratch.as<float>();
+    float* sc = G->scratch.as<float>();   // [1]: the loss
     unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
-    DL_CUDA(cudaMemsetAsync(sc, 0, 2 * sizeof(float), st));
     const GuideRecord* R = static_cast<const GuideRecord*>(d_recs);
-    k_guide_weight_sum<<<(int)std::min<int64_t>(1024, (n + 255) / 256), 256, 0, st>>>(R, (int)n, stride, sc);
+    const int nws = (int)std::min<int64_t>(kWsumMaxBlocks, (n + kWsumThreads - 1) / kWsumThreads);
+    float* wsum = G->wsum.as<float>();
+    k_guide_weight_sum<<<nws, kWsumThreads, 0, st>>>(R, (int)n, stride, wsum, sc + 1);
+    // the next three kernels start their prologues while their predecessor
+    // runs (programmatic dependent launch); each waits for it before using
+    // what it wrote
     const int fb_blocks = (int)std::min<int64_t>(ntiles, 2 * (int64_t)sms);
-    k_guide_fwdbwd<<<fb_blocks, kTcRows, sizeof(GuideFbSmem), st>>>(G->image.ptr, R, (int)n, stride, sc,
-                                                                     G->stage_z.as<__half>(), G->stage_d.as<__half>(),
-                                                                     sc + 1, err);
-    k_guide_wgrad<<<nb, kTcRows, sizeof(GuideWgSmem), st>>>(G->stage_z.as<__half>(), G->stage_d.as<__half>(),
-                                                            (int)nslices, G->partial.as<float>(), err);
-    k_guide_grad_reduce<<<(kGParams + 31) / 32, 32 * kRedWarps, 0, st>>>(G->partial.as<float>(), nb, 1.f / (float)n,
-                                                                         G->grad.as<float>());
+    __half* zg = G->stage_z.as<__half>();
+    __half* dg = G->stage_d.as<__half>();
+    float* part = G->partial.as<float>();
+    float* grad = G->grad.as<float>();
+    const void* img = G->image.ptr;
+    const int ni = (int)n, ns = (int)nslices;
+    const float inv_n = 1.f / (float)n;
+    DL_CUDA(launch_dependent(k_guide_fwdbwd, dim3(fb_blocks), dim3(kTcRows), sizeof(GuideFbSmem), st, img, R, ni,
+                             stride, (const float*)wsum, nws, zg, dg, sc + 1, err));
+    DL_CUDA(launch_dependent(k_guide_wgrad, dim3(nb), dim3(kTcRows), sizeof(GuideWgSmem), st, (const __half*)zg,
+                             (const __half*)dg, ns, part, err));
+    DL_CUDA(launch_dependent(k_guide_grad_reduce, dim3((kGParams + 31) / 32), dim3(32 * kRedWarps), 0, st,
+                             (const float*)part, nb, inv_n, grad));
     DL_CUDA(cudaGetLastError());
 }
 

@@ -463,7 +463,7 @@ typedef struct dl_guide dl_guide;
 typedef struct dl_guide_config {
     float learning_rate;     /* Adam step size (2e-3) */
     float guide_fraction;    /* probability of sampling the learned proposal at a guided vertex (0.5) */
-    int32_t batch;           /* training records per Adam step (32768) */
+    int32_t batch;           /* training records per Adam step (131072) */
     int32_t steps_per_pass;  /* Adam steps after each pass of dl_render_guided (16) */
     int32_t max_guided_depth; /* vertices at this depth or deeper sample the BSDF alone (6) */
     int32_t reserved;
