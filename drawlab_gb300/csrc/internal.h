@@ -202,7 +202,7 @@ struct dl_guide {
     dl::DevBuf w32, w16, grad, m, v, scratch, recs, io_in, io_out;
     dl::DevBuf image;       // the weights as the tensor-core kernels load them (guide_tc.cuh)
     dl::DevBuf pass_recs;   // training records of guided render passes (two halves, alternating)
-    dl::DevBuf stage_z, stage_d, partial;  // a training batch's staged activations and gradient partial sums
+    dl::DevBuf partial;                    // a training batch's per-block gradient sums
     dl::DevBuf wsum;                       // per-block sums of L / p of a training batch
     int64_t step = 0;
     // training runs on its own stream, overlapping the next pass

@@ -40,10 +40,11 @@ def test_forward_matches_oracle(ctx, n):
 @pytest.mark.parametrize("n", [1000, 16384, 37, 100000])
 def test_gradient_matches_oracle(ctx, n):
     """Loss and gradients against the oracle: 37 records fill part of one
-    tile (the weight-gradient product then sums a slice of padding records);
-    100000 records take several tiles per forward/backward block and
-    several 64-record slices per weight-gradient block, whose partial sums
-    the reduction adds."""
+    tile (the weight-gradient products then sum padding records, whose
+    gradients are zero); 1000 and 16384 records give each training block
+    one tile; 100000 records give a block five or six tiles (the two
+    encoding buffers alternate, the gradient sums accumulate in tensor
+    memory), whose partial sums the reduction adds."""
     g = api.Guide(ctx)
     p = random_params(7).astype(np.float32)
     g.set_params(p)
