@@ -239,15 +239,20 @@ def cpu_baseline(scene_data):
                       % (len(blocks), orc.num_blocks(), CPU_BLOCK_SEED, sec)}, orc
 
 
-REF_BLOCKS_PER_STEP = 8
+def ref_blocks_per_step(cores, steps):
+    """Blocks of the 64-block subset one reference step renders: at least one
+    per host core (so no core idles), up to four per core while K steps stay
+    within a few minutes (about 0.5 s of one core per block)."""
+    per_core = max(1, min(4, 16 // max(1, steps)))
+    return max(1, min(CPU_BLOCKS, cores * per_core))
 
 
 def run_reference(args):
     """The reference's CPU renderer on the bench's frame: each step renders
-    8 blocks of the seeded 64-block subset (steps cycle through it), all
-    host cores.  The reference sources do not travel to the GPU host, so its
-    CPU restatement (bit-exact with the reference on the golden vectors)
-    runs."""
+    a chunk of the seeded 64-block subset (steps cycle through it) on all
+    host cores, one or more blocks per core.  The reference sources do not
+    travel to the GPU host, so its CPU restatement (bit-exact with the
+    reference on the golden vectors) runs."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -259,24 +264,25 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     opts = abi.make_opts(spp=WORKLOAD["spp"], max_depth=WORKLOAD["max_depth"])
     subset = cpu_block_subset(orc.num_blocks())
-    chunks = [subset[k:k + REF_BLOCKS_PER_STEP] for k in range(0, len(subset), REF_BLOCKS_PER_STEP)]
+    per_step = ref_blocks_per_step(cores, args.steps)
+    chunks = [np.resize(np.roll(subset, -k), per_step) for k in range(0, len(subset), per_step)]
     for w in range(args.warmup):
         orc.render_block_subset(opts, chunks[w % len(chunks)][:2], threads=cores)
     tot_s = 0.0
     for k in range(args.steps):
         _, s = orc.render_block_subset(opts, chunks[k % len(chunks)], threads=cores)
         tot_s += s
-    samples = REF_BLOCKS_PER_STEP * 32 * 32 * WORKLOAD["spp"] * args.steps
+    samples = per_step * 32 * 32 * WORKLOAD["spp"] * args.steps
     value = samples / tot_s
     sample = ("%d blocks per step, cycling through %d of the frame's %d 32x32 blocks drawn uniformly (seed %d); "
               "64 spp, depth 16; the reference sources do not travel to this host, so the CPU restatement "
               "(bit-exact with the reference on its golden vectors) runs"
-              % (REF_BLOCKS_PER_STEP, len(subset), orc.num_blocks(), CPU_BLOCK_SEED))
+              % (per_step, len(subset), orc.num_blocks(), CPU_BLOCK_SEED))
     line = {"metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seed 2)",
             "impl": "reference",
-            "config": dict(WORKLOAD, step="%d blocks of 32x32 pixels at 64 spp" % REF_BLOCKS_PER_STEP),
+            "config": dict(WORKLOAD, step="%d blocks of 32x32 pixels at 64 spp" % per_step),
             "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -441,7 +447,7 @@ def main():
         if ws == 1 and not args.no_extras:
             gs.close()
             line["c4_batch"] = batch_measure(ctx, steps=2, warmup=1)
-            line["c5_guided"] = guided_measure(ctx, reps=3, warmup=1)
+            line["c5_guided"] = guided_measure(ctx, reps=9, warmup=1)
             line["c5_guided"]["config"]["relmse_resolution_note"] = (
                 "480x270: a 64k-spp plain reference at 1920x1080 is 136 G samples (about 2 minutes of GPU time "
                 "per bench run); the 1080p throughput is measured on the full frame (guided_1080p)")
