@@ -31,8 +31,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cmath>
 #include <chrono>
+#include <climits>
+#include <cmath>
 #include <cstring>
 
 #include "device.cuh"
@@ -501,7 +502,9 @@ __global__ void k_init(RenderParams P, int capacity) {
     }
 }
 
-constexpr int kDone = kEmptyChild;  // traversal state: ray finished
+// traversal state: ray finished (below every leaf reference: scenes hold
+// fewer than 2^27 triangles)
+constexpr int kDone = INT_MIN;
 
 // Persistent traversal over a ray queue.  Each lane holds one ray's
 // traversal state (node, stack); a lane whose ray finishes takes the next ray
@@ -632,7 +635,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
         int dest = 0;
         if (has) {
             // descend inner nodes until a leaf (or the end of the traversal)
-            while (node >= 0 && node != kDone) {
+            while (node >= 0) {
 #ifdef DL_CHECKS
                 const int num_nodes = kMulti ? P.reqs[rid].sc.num_nodes : P.r0.sc.num_nodes;
                 if (!DL_IN_BOUNDS(node < num_nodes, &P.cnt->err)) {
@@ -652,7 +655,11 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 if (h0 && h1) {
                     int near = ch.x, far = ch.y;
                     if (t1 < t0) { near = ch.y; far = ch.x; }
+#ifdef DL_CHECKS
                     if (sp < kStackSize) push(far); else err |= 1u;
+#else
+                    push(far);   // depth <= kStackSize + 1: checked when the scene is built
+#endif
                     node = near;
                 } else if (h0) {
                     node = ch.x;
@@ -1276,16 +1283,17 @@ __global__ void __launch_bounds__(kFilmThreads) k_film_gather(FilmParams F) {
 #pragma unroll
             for (int dx = 0; dx < kFilmTaps; dx++) {
                 const int c = (kFilmRows * ty + r) * kFilmRegion + tx + dx;
-                const float R = s_r[c], G = s_g[c], B = s_b[c], wx = s_wx[dx * kFilmCells + c];
+                const float wx = s_wx[dx * kFilmCells + c];
+                const float R = __fmul_rn(s_r[c], wx), G = __fmul_rn(s_g[c], wx), B = __fmul_rn(s_b[c], wx);
 #pragma unroll
                 for (int j = 0; j < kFilmRows; j++) {
                     const int dy = r - j;
                     if (dy < 0 || dy >= kFilmTaps) continue;
                     const float wy = s_wy[dy * kFilmCells + c];
-                    ar[j] = __fadd_rn(ar[j], __fmul_rn(__fmul_rn(R, wx), wy));
-                    ag[j] = __fadd_rn(ag[j], __fmul_rn(__fmul_rn(G, wx), wy));
-                    ab[j] = __fadd_rn(ab[j], __fmul_rn(__fmul_rn(B, wx), wy));
-                    aw[j] = __fadd_rn(aw[j], __fmul_rn(wx, wy));
+                    ar[j] = __fmaf_rn(R, wy, ar[j]);
+                    ag[j] = __fmaf_rn(G, wy, ag[j]);
+                    ab[j] = __fmaf_rn(B, wy, ab[j]);
+                    aw[j] = __fmaf_rn(wx, wy, aw[j]);
                 }
             }
         }

@@ -337,6 +337,10 @@ void build_scene(dl_scene* S, const dl_mesh_desc* meshes, int32_t nm, const dl_m
     }
     BvhBuildOptions bo;
     BvhResult bvh = build_bvh(tri9.data(), ntri, bo);
+    // the traversal kernels push at most one entry per inner level
+    if (bvh.depth - 1 > kStackSize)
+        throw Error(DL_ERR_INVALID_ARG, "BVH depth " + std::to_string(bvh.depth) + " exceeds the traversal stack (" +
+                                            std::to_string(kStackSize) + " entries)");
     std::vector<int4> vidx((size_t)std::max<int64_t>(ntri, 1));
     for (size_t k = 0; k < bvh.tri_order.size(); k++) vidx[k] = vidx_orig[bvh.tri_order[k]];
 
