@@ -257,9 +257,13 @@ BvhResult build_bvh(const float* tris, int64_t n, const BvhBuildOptions& opt) {
     std::memset(&empty_node, 0, sizeof(empty_node));
     Box nobox;
     if (n == 0 || R.left < 0) {
+        // a one-leaf tree references its leaf from both slots (the traversal
+        // kernels take both children of a node as present); an empty tree's
+        // root is never visited
         GpuNode g = empty_node;
-        set_child(g, 0, n > 0 ? R.box : nobox, n > 0 ? leaf_ref(R) : kEmptyRef);
-        set_child(g, 1, nobox, kEmptyRef);
+        const int32_t ref = n > 0 ? leaf_ref(R) : kEmptyRef;
+        set_child(g, 0, n > 0 ? R.box : nobox, ref);
+        set_child(g, 1, n > 0 ? R.box : nobox, ref);
         res.nodes.push_back(g);
         res.depth = 1;
         res.leaves = n > 0 ? 1 : 0;

@@ -20,7 +20,9 @@ namespace dl {
 //   d = (child0, child1, 0, 0) as int bits
 // child >= 0: index of an inner node; child < 0: leaf ~((first << 4) | (count - 1)),
 // first = index of the first triangle in the leaf-ordered triangle array,
-// count in [1, 16].  An empty child slot holds an inverted (empty) box.
+// count in [1, 16].  Both slots of every node hold a child (a one-leaf tree
+// references its leaf twice); only the root of an empty tree holds kEmptyRef
+// (with inverted boxes), and the traversal never visits it.
 struct alignas(16) GpuNode {
     float a[4];
     float b[4];

@@ -650,9 +650,7 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 bool h0, h1;
                 float t0, t1;
                 box2(rb, tmin, tmax, a, b, c, h0, h1, t0, t1);
-                h0 = h0 && ch.x != kEmptyChild;
-                h1 = h1 && ch.y != kEmptyChild;
-                if (h0 && h1) {
+                if (h0 && h1) {   // (both slots always hold a child: see bvh.h)
                     int near = ch.x, far = ch.y;
                     if (t1 < t0) { near = ch.y; far = ch.x; }
 #ifdef DL_CHECKS

@@ -172,3 +172,30 @@ def test_empty_scene_misses(ctx, kernel):
     prim, t, u, v = gs.trace_closest(rays, wavefront=wf)
     assert (prim == -1).all()
     assert (gs.trace_any(rays, wavefront=wf) == 0).all()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_one_leaf_scene(ctx, kernel):
+    # two triangles make a one-leaf tree, whose root references the leaf
+    # from both child slots: hits and misses still match the oracle
+    sc = scenes.SceneData("one_leaf")
+    m = sc.add_material(scenes.Material())
+    p, f, n = scenes.rectangle((-1.0, -1.0, 0.0), (2.0, 0.0, 0.0), (0.0, 2.0, 0.0))
+    sc.add_mesh(scenes.Mesh(p, f, n, material=m))
+    sc.camera = scenes.Camera(width=8, height=8)
+    gs = api.Scene.from_data(ctx, sc)
+    assert gs.info().num_bvh_nodes == 1
+    orc = po.OracleScene(sc)
+    rng = np.random.default_rng(17)
+    rays = np.zeros((512, 8), np.float32)
+    rays[:, 0:2] = rng.uniform(-1.5, 1.5, (512, 2))
+    rays[:, 2] = 2.0
+    rays[:, 3] = 1e-4
+    rays[:, 6] = -1.0
+    rays[:, 7] = np.inf
+    wf = kernel == "wavefront"
+    g = gs.trace_closest(rays, wavefront=wf)
+    o = orc.trace_closest(rays)
+    compare_closest(g, o)
+    assert (g[0] >= 0).any() and (g[0] == -1).any()
+    np.testing.assert_array_equal(gs.trace_any(rays, wavefront=wf), orc.trace_any(rays))
