@@ -154,6 +154,12 @@ __device__ __forceinline__ bool in_bounds(bool ok, unsigned int* err) {
 #endif
 constexpr const char* kBoundsMessage = "bounds check failed: a queue, slot, path, node or triangle index "
                                         "outside its array (bounds-checked build)";
+// 32 bytes (32-byte aligned) of read-only global data in one load.
+__device__ __forceinline__ void ld_nc_256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
 __device__ __forceinline__ bool slot_ok(const RenderParams& P, int slot) {
     return DL_IN_BOUNDS(slot >= 0 && slot < P.capacity, &P.cnt->err);
 }
@@ -644,8 +650,10 @@ __global__ void __launch_bounds__(128) k_traverse(RenderParams P, int p) {
                 }
 #endif
                 const float4* np = nodes + 4 * node;
-                float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-                int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
+                float4 a, b, c, dd;
+                ld_nc_256(np, a, b);        // a node is two 32-byte halves
+                ld_nc_256(np + 2, c, dd);
+                const int2 ch = make_int2(__float_as_int(dd.x), __float_as_int(dd.y));
                 if (kCount) nn++;
                 bool h0, h1;
                 float t0, t1;
