@@ -492,7 +492,7 @@ namespace dl {
 // Portable float map (PF: RGB, Pf: grey), rows stored bottom to top, scale
 // sign = byte order.  Returns rows top to bottom, RGB.  The reference reads
 // envmaps through its Bitmap class (EXR via OpenEXR, LDR/HDR via stb_image,
-// src/core/bitmap/bitmap.cpp:30-140); this build reads PFM.
+// src/core/bitmap/bitmap.cpp:30-140); this library reads PFM.
 std::vector<float> load_pfm(const std::string& path, int& w, int& h) {
     std::ifstream in(path, std::ios::binary);
     if (!in) throw Error(DL_ERR_IO, "cannot open image \"" + path + "\"");

@@ -2,7 +2,7 @@
 
 * ``build_oracle()`` compiles the CPU restatement ``oracle/oracle.cpp`` into
   ``oracle/_build/liboracle.so`` (g++, no dependencies).  It builds on any
-  host, including the Arm GPU machine.
+  host, x86_64 or Arm.
 * ``build_ref()`` compiles the reference's own CPU hot-path sources from where
   they lie (``$DRAWLAB_REFERENCE``, else a ``reference`` directory beside the
   repository) against the stand-in headers in ``oracle/ref_shim`` and links

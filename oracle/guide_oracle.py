@@ -1,8 +1,8 @@
 """CPU restatement of the learned guiding proposal (network, vMF mixture,
 loss and its gradient, Adam) in numpy.
 
-TEST INFRASTRUCTURE ONLY: the checker of the GPU kernels in
-drawlab_gb300/csrc/guide.{cuh,cu}.  The network has no counterpart in the
+TEST INFRASTRUCTURE ONLY: the oracle the tests compare the GPU kernels of
+drawlab_gb300/csrc/guide.{cuh,cu} against.  The network has no counterpart in the
 reference (its guiding code is absent); this file states the model the GPU
 implements, in float64, with the GPU's fp16 rounding points emulated where
 asked (`fp16=True`): weights, encodings and hidden activations are fp16,

@@ -1,7 +1,7 @@
 // CPU restatement of the xuxmin/DrawLab path-tracer hot path.
 //
-// TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for the GPU path and
-// the timed CPU baseline.  Nothing in the product links this file.
+// TEST INFRASTRUCTURE ONLY (see oracle.h): the oracle the GPU path is tested
+// against, and the timed CPU baseline.  Nothing in the product links this file.
 //
 // It restates, step for step and in the same float/double operation order,
 // the reference CPU backend (paths relative to the reference project root):

@@ -2,7 +2,7 @@
  * oracle.h -- CPU restatement of the xuxmin/DrawLab path-tracer hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Tests, __graft_entry__.smoke() and bench.py's
- * CPU baseline call it as the checker; the product never links it.
+ * CPU baseline call it as the oracle; the product never links it.
  *
  * Scene input is the dl_*_desc arrays of include/drawlab.h.  Every entry
  * point restates the reference function named beside it (paths relative to

@@ -102,7 +102,8 @@ void st3(float* p, float3 v) {
 // below repeat the shaders' own expressions, make_float3(rnd(seed),
 // rnd(seed), rnd(seed)) (envmap.h:35) and make_float2(x + rnd(seed), y +
 // rnd(seed)) (opencv.h:39), whose argument evaluation order C++ leaves to
-// the compiler: repeating the expression records the order this build uses.
+// the compiler: repeating the expression records the order the compiler
+// chose for this harness.
 float3 peek3(unsigned int seed) {
     float a = rnd(seed);
     float b = rnd(seed);

@@ -3,7 +3,7 @@
 triangle index the kernels take from a queue, counter or record is checked
 against its array before the access; a violation sets an error bit and the
 call fails with "bounds check failed".  This stands in for a memory checker,
-which this GPU pool does not offer.
+which the GPUs these tests run on do not offer.
 
 The test builds that library, renders the small cases of every entry point
 with it in a child process (the Cornell box, the envmap scene with its NEE /
