@@ -57,30 +57,23 @@ struct GuideNet {
 
 // ------------------------------------------------------------- encoding
 // sin / cos of (2^(k-3) pi x) for k = 0..11 (periods from 16 scene units
-// down to 1/128): exact sincospi at k = 0, 4, 8, double-angle steps in
-// between (at most three, error ~1e-6).
+// down to 1/128): sincospi at k = 0 and 6, double-angle steps in between
+// (at most five; largest error 1.1e-5 over x in [-1, 1], below the fp16
+// spacing the encodings are rounded to near +-1).
 constexpr int kGFreqShift = 3;
+constexpr int kGFreqAnchor = 6;   // frequencies per sincospi
 __device__ __forceinline__ void encode_scalar_h2(float x, __half2* out) {
 #pragma unroll
-    for (int k0 = 0; k0 < kGFreq; k0 += 4) {
+    for (int k0 = 0; k0 < kGFreq; k0 += kGFreqAnchor) {
         float s, c;
         sincospif(x * ((float)(1 << k0) / (float)(1 << kGFreqShift)), &s, &c);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < kGFreqAnchor; k++) {
             out[k0 + k] = __floats2half2_rn(s, c);  // (sin, cos): sin at the lower address
             float s2 = 2.f * s * c, c2 = 1.f - 2.f * s * s;
             s = s2;
             c = c2;
         }
-    }
-}
-__device__ __forceinline__ void encode_scalar(float x, __half* out) {
-    __half2 h[kGFreq];
-    encode_scalar_h2(x, h);
-#pragma unroll
-    for (int k = 0; k < kGFreq; k++) {
-        out[2 * k] = __low2half(h[k]);
-        out[2 * k + 1] = __high2half(h[k]);
     }
 }
 
