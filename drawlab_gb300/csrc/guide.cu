@@ -210,9 +210,11 @@ __device__ __forceinline__ float record_grad_half(const float* o, float3 w, floa
 //                    tile's weight-gradient products run while the backward
 //                    epilogues and the next tile's first product go on.  At
 //                    the end each block writes its gradient sums from tensor
-//                    memory to global memory, in the parameter layout.
-//   k_guide_grad_reduce  sums the blocks' partials into the gradient (no
-//                    atomics), applying the loss's 1/n.
+//                    memory to global memory, feature-major (coalesced
+//                    stores; layout below).
+//   k_guide_grad_reduce  sums the blocks' partials in a fixed order (no
+//                    atomics) into the gradient, in the parameter layout,
+//                    applying the loss's 1/n.
 //
 // Loss scaling: the fp16 activation gradients leave out the loss's 1/n
 // (with n ~ 1e5 records most of them would be fp16 subnormals); they
