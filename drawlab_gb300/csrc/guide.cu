@@ -35,17 +35,24 @@ namespace dl {
 static_assert(kGImgTrainBytes == kGuideImageBytes, "image size");
 
 // Raw network outputs (40 per row) of n input rows, 128 rows per tile on
-// the tensor cores; each of a block's two warpgroups walks its own tiles.
-__global__ void __launch_bounds__(kTcThreads) k_guide_infer(const void* image, const float* in, float* out, int n,
-                                                             unsigned* err) {
+// the tensor cores; each of a block's five warpgroups walks its own tiles
+// (one block per SM: five tiles' chains of dependent layers overlap, one
+// weight copy in shared memory).
+constexpr int kInferGroups = 5;
+using InferSmem = GuideTcSmemT<kInferGroups>;
+constexpr int kInferThreads = kTcRows * kInferGroups;
+static_assert(sizeof(InferSmem) + 1024 <= 227 * 1024, "one inference block per SM");
+
+__global__ void __launch_bounds__(kInferThreads, 1) k_guide_infer(const void* image, const float* in, float* out,
+                                                                   int n, unsigned* err) {
     extern __shared__ __align__(16) unsigned char dyn_smem[];
-    GuideTcSmem& S = *reinterpret_cast<GuideTcSmem*>(dyn_smem);
+    InferSmem& S = *reinterpret_cast<InferSmem*>(dyn_smem);
     const int ntiles = (n + kTcRows - 1) / kTcRows;
-    if ((int)blockIdx.x * kTcGroups >= ntiles) return;
+    if ((int)blockIdx.x * kInferGroups >= ntiles) return;
     const int g = tc_group(), row = tc_row();
     uint32_t phase = 0;
     bool ok = guide_tc_begin(S, image, err);
-    for (int tile = blockIdx.x * kTcGroups + g; ok && tile < ntiles; tile += gridDim.x * kTcGroups) {
+    for (int tile = blockIdx.x * kInferGroups + g; ok && tile < ntiles; tile += gridDim.x * kInferGroups) {
         const int r = tile * kTcRows + row;
         float x[kGIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (r < n)
@@ -781,7 +788,7 @@ float guide_train(dl_guide* G, const void* d_recs, int64_t n, int steps) {
 // shared memory; the first call raises the kernel's shared-memory limit.
 static int infer_blocks_per_sm() {
     DL_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(GuideTcSmem)));
+                                 (int)sizeof(InferSmem)));
     DL_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int dev = 0;
     DL_CUDA(cudaGetDevice(&dev));
@@ -790,8 +797,8 @@ static int infer_blocks_per_sm() {
     cudaFuncAttributes fa;
     DL_CUDA(cudaFuncGetAttributes(&fa, k_guide_infer));
     const int regs_per_warp = ((fa.numRegs + 7) / 8) * 8 * 32;
-    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kTcThreads / 32));
-    const size_t smem = sizeof(GuideTcSmem) + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
+    const int by_regs = prop.regsPerMultiprocessor / std::max(1, regs_per_warp * (kInferThreads / 32));
+    const size_t smem = sizeof(InferSmem) + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
     return std::max(1, std::min(by_regs, (int)(prop.sharedMemPerMultiprocessor / smem)));
 }
 
@@ -801,8 +808,9 @@ void guide_forward(dl_guide* G, const float* d_in, float* d_out, int64_t n) {
     unsigned* err = reinterpret_cast<unsigned*>(G->scratch.as<char>() + kGuideErrOffset);
     DL_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
     const int64_t ntiles = (n + kTcRows - 1) / kTcRows;
-    const int blocks = (int)std::min<int64_t>((ntiles + kTcGroups - 1) / kTcGroups, (int64_t)G->ctx->num_sms * per_sm);
-    k_guide_infer<<<blocks, kTcThreads, sizeof(GuideTcSmem), st>>>(G->image.ptr, d_in, d_out, (int)n, err);
+    const int blocks =
+        (int)std::min<int64_t>((ntiles + kInferGroups - 1) / kInferGroups, (int64_t)G->ctx->num_sms * per_sm);
+    k_guide_infer<<<blocks, kInferThreads, sizeof(InferSmem), st>>>(G->image.ptr, d_in, d_out, (int)n, err);
     DL_CUDA(cudaGetLastError());
 }
 

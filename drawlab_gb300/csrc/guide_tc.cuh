@@ -1,9 +1,10 @@
 // The guiding network (guide.cuh) on the fifth-generation tensor cores.
 //
-// A block holds two warpgroups (256 threads) that share one copy of the
-// weights; each warpgroup evaluates its own 128 shading points at a time,
-// one row per thread, independently of the other (two tiles in flight per
-// block, synchronised by per-warpgroup named barriers).  Each thread writes
+// A block holds G warpgroups (two in the guided material kernels, five in
+// the standalone inference kernel) that share one copy of the weights; each
+// warpgroup evaluates its own 128 rows at a time, one row per thread,
+// independently of the others (G tiles in flight per block, synchronised by
+// per-warpgroup named barriers).  Each thread writes
 // its row's input encoding into its warpgroup's operand tile; the
 // warpgroup's first thread issues each layer as tcgen05.mma instructions
 // (M = 128 rows, N = 64 or 48 outputs, K = 16 per instruction) with both
@@ -35,10 +36,8 @@
 namespace dl {
 
 constexpr int kTcRows = 128;                     // rows per tile = threads per warpgroup
-constexpr int kTcGroups = 2;                     // warpgroups (tiles in flight) per block
-constexpr int kTcThreads = kTcRows * kTcGroups;  // threads per block
-constexpr int kTcCols = 64 * kTcGroups;          // tensor-memory columns per block (64 per warpgroup,
-                                                 // fp32 accumulators reused by every layer)
+constexpr int kTcGroups = 2;                     // warpgroups (tiles in flight) per guided block
+constexpr int kTcThreads = kTcRows * kTcGroups;  // threads per guided block
 constexpr uint64_t kTcWaitNs = 1000000000ull;
 constexpr unsigned kErrTensorWait = 2u;  // error-word bit: a tensor-core wait ran out
 
@@ -109,16 +108,24 @@ __device__ __forceinline__ void write_image(unsigned char* img, int i, float v) 
 // floats; odd, so the rows of a warp fall in distinct banks
 constexpr int kTcOutStride = kGStoredLobes + 1;
 
-struct GuideTcSmem {
+// Shared memory of a block of G warpgroups (tiles in flight) sharing one
+// weight copy; 64 tensor-memory columns per warpgroup (the allocation is
+// rounded up to a power of two).
+template <int G>
+struct GuideTcSmemT {
+    static constexpr int kGroups = G;
+    static constexpr uint32_t kCols = G <= 2 ? 128u : G <= 4 ? 256u : 512u;
+    static_assert(G >= 1 && G <= 8, "one to eight warpgroups");
     __half w[kGImgHalves];    // the image: weights ...
     float bias[kGImgBiases];  // ... and biases, contiguous
     // per warpgroup: encodings; then the hidden activations (K = 64 layout);
     // then the fp32 outputs (kTcOutStride floats per row), decoded in place
-    alignas(16) __half act[kTcGroups][kTcRows * kGEnc];
-    uint64_t bar_w, bar_mma[kTcGroups];
+    alignas(16) __half act[G][kTcRows * kGEnc];
+    uint64_t bar_w, bar_mma[G];
     uint32_t tmem;
     int fail;
 };
+using GuideTcSmem = GuideTcSmemT<kTcGroups>;
 static_assert(offsetof(GuideTcSmem, bias) == kGImgHalves * 2, "image layout");
 static_assert(offsetof(GuideTcSmem, act) % 16 == 0 && (kTcRows * kGEnc * 2) % 16 == 0, "operand alignment");
 static_assert(kTcRows * kTcOutStride * 4 <= kTcRows * kGEnc * 2, "outputs fit the operand tile");
@@ -142,24 +149,27 @@ __device__ __forceinline__ bool wg_or(int g, bool pred) {
     return r != 0;
 }
 
-__device__ __forceinline__ float* tc_out_row(GuideTcSmem& S, int g, int r) {
+template <class Sm>
+__device__ __forceinline__ float* tc_out_row(Sm& S, int g, int r) {
     return reinterpret_cast<float*>(S.act[g]) + r * kTcOutStride;
 }
 
-__device__ __forceinline__ void tc_record_failure(GuideTcSmem& S, unsigned* err) {
+template <class Sm>
+__device__ __forceinline__ void tc_record_failure(Sm& S, unsigned* err) {
     S.fail = 1;
     if (err) atomicOr(err, kErrTensorWait);
 }
 
 // Block start (all threads): barriers, tensor memory, the weight image.
 // Returns false (in every thread) when the weights did not arrive in time.
-__device__ __forceinline__ bool guide_tc_begin(GuideTcSmem& S, const void* image, unsigned* err) {
+template <class Sm>
+__device__ __forceinline__ bool guide_tc_begin(Sm& S, const void* image, unsigned* err) {
     if (threadIdx.x == 0) {
         tc::mbar_init(&S.bar_w, 1);
-        for (int g = 0; g < kTcGroups; g++) tc::mbar_init(&S.bar_mma[g], 1);
+        for (int g = 0; g < Sm::kGroups; g++) tc::mbar_init(&S.bar_mma[g], 1);
         S.fail = 0;
     }
-    if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, kTcCols);
+    if (threadIdx.x < 32) tc::tmem_alloc(&S.tmem, Sm::kCols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -172,7 +182,8 @@ __device__ __forceinline__ bool guide_tc_begin(GuideTcSmem& S, const void* image
 // Block end (all threads): after a failed wait, wait (bounded) for the
 // outstanding weight copy and the thread's warpgroup's outstanding layer
 // (`mma_phase`: that warpgroup's next parity), then free the tensor memory.
-__device__ __forceinline__ void guide_tc_end(GuideTcSmem& S, uint32_t mma_phase) {
+template <class Sm>
+__device__ __forceinline__ void guide_tc_end(Sm& S, uint32_t mma_phase) {
     tc::fence_before_sync();
     __syncthreads();
     if (S.fail) {
@@ -182,7 +193,7 @@ __device__ __forceinline__ void guide_tc_end(GuideTcSmem& S, uint32_t mma_phase)
     __syncthreads();
     if (threadIdx.x < 32) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(S.tmem, kTcCols);
+        tc::tmem_dealloc(S.tmem, Sm::kCols);
     }
 }
 
@@ -207,8 +218,8 @@ __device__ __forceinline__ void encode_row_tc(const float* in6, __half* act, int
 
 // One layer of warpgroup g: D (its tensor-memory columns) = act (128 x K)
 // W^T, W [N][K] in the image.
-template <int K, int N>
-__device__ __forceinline__ void tc_issue_layer(GuideTcSmem& S, int g, int w_off) {
+template <int K, int N, class Sm>
+__device__ __forceinline__ void tc_issue_layer(Sm& S, int g, int w_off) {
     constexpr uint32_t idesc = tc::idesc_f16_f32(kTcRows, N);
     const uint32_t a = tc::smem_addr(S.act[g]), b = tc::smem_addr(S.w + w_off);
     tc::fence_after_sync();
@@ -220,13 +231,15 @@ __device__ __forceinline__ void tc_issue_layer(GuideTcSmem& S, int g, int w_off)
 }
 
 // The warp's 32 accumulator lanes in its warpgroup's columns.
-__device__ __forceinline__ uint32_t tc_warp_tmem(const GuideTcSmem& S, int g) {
+template <class Sm>
+__device__ __forceinline__ uint32_t tc_warp_tmem(const Sm& S, int g) {
     return S.tmem + 64u * g + ((uint32_t)(tc_row() & ~31) << 16);
 }
 
 // Bias + ReLU of the warp's 32 rows (64 columns of tensor memory), written
 // as the next layer's operand (K = 64 layout).
-__device__ __forceinline__ void tc_hidden_epilogue(GuideTcSmem& S, int g, const float* bias) {
+template <class Sm>
+__device__ __forceinline__ void tc_hidden_epilogue(Sm& S, int g, const float* bias) {
     const int r = tc_row();
     const uint32_t t = tc_warp_tmem(S, g);
     __half* act = S.act[g];
@@ -253,7 +266,8 @@ __device__ __forceinline__ void tc_hidden_epilogue(GuideTcSmem& S, int g, const 
 // tc_out_row(S, g, tc_row()).  `phase` is the parity of the next completion
 // of S.bar_mma[g], kept by every thread of the warpgroup.  Returns false
 // (the same in every thread of the warpgroup) after a wait ran out.
-__device__ __forceinline__ bool guide_tc_forward(GuideTcSmem& S, int g, uint32_t& phase, unsigned* err) {
+template <class Sm>
+__device__ __forceinline__ bool guide_tc_forward(Sm& S, int g, uint32_t& phase, unsigned* err) {
     bool failed = false;
     const bool issuer = tc_row() == 0;
     auto wait = [&]() {
