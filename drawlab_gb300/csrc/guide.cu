@@ -273,8 +273,9 @@ struct GuideTrSmem {
 };
 static_assert(offsetof(GuideTrSmem, w2t) == kGImgW2T && offsetof(GuideTrSmem, w3t) == kGImgW3T, "image layout");
 static_assert(sizeof(GuideTrSmem) + 1024 <= 227 * 1024, "one training block per SM");
-// no other tensor-memory user of this library (the guided material and
-// inference blocks, 107 KB) fits beside a block: its 512 columns are free
+// no other tensor-memory user of this library (the guided material blocks,
+// 107 KB; the inference block, 218 KB) fits beside a block: its 512 columns
+// are free
 static_assert(sizeof(GuideTrSmem) + 1024 + 107 * 1024 > 228 * 1024, "one tensor-memory user per SM");
 
 __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
