@@ -242,7 +242,8 @@ def cpu_baseline(scene_data):
 def ref_blocks_per_step(cores, steps):
     """Blocks of the 64-block subset one reference step renders: at least one
     per host core (so no core idles), up to four per core while K steps stay
-    within a few minutes (about 0.5 s of one core per block)."""
+    within a few minutes (a block at 64 spp and depth 16 takes about 8 s of
+    one core)."""
     per_core = max(1, min(4, 16 // max(1, steps)))
     return max(1, min(CPU_BLOCKS, cores * per_core))
 
